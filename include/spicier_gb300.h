@@ -1,0 +1,354 @@
+/*
+ * spicier_gb300.h — C ABI of the GB300 batched-sweep backend.
+ *
+ * This header is the drop-in boundary for Spicier's batched-sweep hot path.
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (SP_OK = 0, negative = error) and never aborts the process.
+ *
+ * Reference interfaces replaced (paths relative to the Spicier repository):
+ *   BatchedLuSolver trait ........ crates/spicier-batched-sweep/src/solver.rs:107-135
+ *   BatchedSolveResult ........... crates/spicier-batched-sweep/src/solver.rs:44-75
+ *   GpuBatchConfig ............... crates/spicier-batched-sweep/src/solver.rs:15-40
+ *   BackendType .................. crates/spicier-batched-sweep/src/solver.rs:79-92
+ *   BatchedSweepError ............ crates/spicier-batched-sweep/src/error.rs:7-43
+ *   CudaBatchedLuSolver::solve_batch crates/spicier-backend-cuda/src/batched_lu.rs:373-494
+ *   ConvergenceCriteria .......... crates/spicier-solver/src/newton.rs:9-34
+ *   Gmin/SourceSteppingParams .... crates/spicier-solver/src/newton.rs:173-231
+ *   solve_newton_raphson ......... crates/spicier-solver/src/newton.rs:70-131 (batched here)
+ *   hash RNG ..................... crates/spicier-batched-sweep/src/rng.rs:39-227
+ *   SweepStatistics/Accumulator .. crates/spicier-batched-sweep/src/statistics.rs:35-160
+ *   Histogram / YieldSpec ........ crates/spicier-batched-sweep/src/statistics.rs:205-386
+ *   AdaptiveTransientParams ...... crates/spicier-solver/src/transient/types.rs:78-107
+ *   GmresConfig .................. crates/spicier-solver/src/gmres/mod.rs:34-51
+ *
+ * Ownership: the caller owns every buffer passed in.  Functions suffixed
+ * _device take device pointers and a cudaStream_t passed as void*; they
+ * enqueue work and return without synchronising.  Functions without the
+ * suffix take host pointers, copy in, compute, copy out and synchronise.
+ *
+ * Threading: an sp_ctx may be used from several host threads; each call
+ * serialises on the context's internal lock (the reference trait is
+ * Send + Sync).  Device-pointer calls run on the caller's stream.
+ */
+#ifndef SPICIER_GB300_H
+#define SPICIER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* Status codes: mirror of BatchedSweepError (error.rs:7-43).             */
+/* ---------------------------------------------------------------------- */
+enum sp_status {
+    SP_OK = 0,
+    SP_ERR_NO_BACKEND = -1,        /* NoBackendAvailable                  */
+    SP_ERR_BACKEND_INIT = -2,      /* BackendInit(String)                 */
+    SP_ERR_MEMORY_ALLOC = -3,      /* MemoryAlloc(String)                 */
+    SP_ERR_TRANSFER = -4,          /* Transfer(String)                    */
+    SP_ERR_INVALID_DIMENSION = -5, /* InvalidDimension(String)            */
+    SP_ERR_BATCH_TOO_LARGE = -6,   /* BatchTooLarge { size, max }         */
+    SP_ERR_SINGULAR_BATCH = -7,    /* SingularBatch (reserved)            */
+    SP_ERR_BACKEND = -8,           /* Backend(String)                     */
+    SP_ERR_SOLVER = -9,            /* Solver(spicier_solver::Error)       */
+    SP_ERR_INVALID_ARGUMENT = -10  /* null pointer / bad enum value       */
+};
+
+/* BackendType (solver.rs:79-92) with one added tag for this backend. */
+enum sp_backend_type {
+    SP_BACKEND_CUDA = 0,
+    SP_BACKEND_METAL = 1,
+    SP_BACKEND_MPS = 2,
+    SP_BACKEND_ACCELERATE = 3,
+    SP_BACKEND_FAER = 4,
+    SP_BACKEND_CPU = 5,
+    SP_BACKEND_GB300 = 6
+};
+
+/* GpuBatchConfig (solver.rs:15-40).  Defaults here: min_batch_size 16,
+ * min_matrix_size 1 (the fused kernels pay off from n = 1), and
+ * max_batch_per_launch 1<<26 instead of the cuBLAS path's 65 535. */
+typedef struct sp_batch_config {
+    uint64_t min_batch_size;
+    uint64_t min_matrix_size;
+    uint64_t max_batch_per_launch;
+} sp_batch_config;
+
+/* Arithmetic used by a solve. */
+enum sp_precision {
+    SP_PREC_FP64 = 0,       /* plain FP64 everywhere (FMA contraction allowed)       */
+    SP_PREC_MIXED = 1,      /* FP32 factorisation / Krylov, FP64 residual + update   */
+    SP_PREC_FP64_EXACT = 2  /* plain FP64 in the reference's exact operation order,
+                               no FMA contraction: bit-identical to the reference on
+                               circuits without exp/log device models               */
+};
+
+typedef struct sp_ctx sp_ctx;
+
+/* Context lifecycle.  `device` is a CUDA ordinal. */
+int sp_ctx_create(int device, sp_ctx** out);
+int sp_ctx_destroy(sp_ctx* ctx);
+/* Text of the last error on this context ("" if none).  Never NULL. */
+const char* sp_ctx_last_error(const sp_ctx* ctx);
+/* Library version string, e.g. "spicier-gb300 0.1.0 sm_103a". */
+const char* sp_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* BatchedLuSolver (solver.rs:107-135)                                    */
+/* ---------------------------------------------------------------------- */
+
+/* BatchedLuSolver::backend_type — always SP_BACKEND_GB300. */
+int sp_backend_type(void);
+/* BatchedLuSolver::should_use_gpu — 1/0. */
+int sp_should_use_gpu(const sp_ctx* ctx, size_t matrix_size, size_t batch_size);
+/* BatchedLuSolver::config. */
+int sp_get_config(const sp_ctx* ctx, sp_batch_config* out);
+int sp_set_config(sp_ctx* ctx, const sp_batch_config* cfg);
+
+/* BatchedLuSolver::solve_batch (solver.rs:119-125).
+ * matrices: batch*n*n column-major FP64; rhs: batch*n.  On return
+ * solutions[batch*n] holds x; singular systems get an all-zero solution and
+ * their index in singular_indices (capacity batch), count in *num_singular.
+ * Singularity is not an error (CpuBatchedSolver semantics, solver.rs:367-377).
+ * Errors: INVALID_DIMENSION (n == 0 with batch > 0), BATCH_TOO_LARGE. */
+int sp_solve_batch(sp_ctx* ctx, const double* matrices, const double* rhs,
+                   size_t n, size_t batch, double* solutions,
+                   uint64_t* singular_indices, uint64_t* num_singular);
+
+/* Same, on device buffers.  singular_flags[batch] receives 1 for a singular
+ * system, else 0.  precision: SP_PREC_FP64 (partial-pivot LU in FP64) or
+ * SP_PREC_MIXED (FP32 partial-pivot LU + FP64 iterative refinement,
+ * refine_steps sweeps; falls back to an FP64 factorisation for a system whose
+ * refinement does not reach FP64 accuracy). */
+int sp_solve_batch_device(sp_ctx* ctx, const double* d_matrices, const double* d_rhs,
+                          size_t n, size_t batch, double* d_solutions,
+                          uint8_t* d_singular_flags, int precision, int refine_steps,
+                          void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Circuits                                                               */
+/* ---------------------------------------------------------------------- */
+
+/* Element kinds: the device set of the Newton path.
+ * Field slots (indices into the per-sample parameter vector) per kind:
+ *   R:    f[0] resistance (ohm)                          passive.rs:53-59
+ *   C:    f[0] capacitance (F); open at DC                passive.rs:232-240
+ *   L:    f[0] inductance (H); 0 V source at DC           passive.rs:318-325
+ *   V:    f[0] DC voltage                                 sources.rs:96-101
+ *   I:    f[0] DC current (flows pos -> neg inside)       sources.rs:230-236
+ *   D:    f[0] IS, f[1] N                                 diode.rs:11-38
+ *   NMOS/PMOS: f[0] VTO, f[1] KP, f[2] LAMBDA, f[3] W, f[4] L, f[5] NF
+ *                                                          mosfet/level1.rs:23-71
+ *   NPN/PNP: f[0] IS, f[1] BF, f[2] BR, f[3] NF, f[4] NR, f[5] VAF (<=0: inf)
+ *                                                          bjt.rs:23-76
+ * node[] holds MNA node indices (0-based, ground = -1):
+ *   two-terminal: node[0] = pos/anode, node[1] = neg/cathode
+ *   MOSFET: node[0] = drain, node[1] = gate, node[2] = source
+ *   BJT:    node[0] = collector, node[1] = base, node[2] = emitter
+ * branch: index of the element's current variable (V and L only), else -1;
+ *   its MNA row is num_nodes + branch.
+ * wave: index into sp_circuit.pulses for a time-varying V/I, else -1. */
+enum sp_element_kind {
+    SP_EL_R = 1,
+    SP_EL_C = 2,
+    SP_EL_L = 3,
+    SP_EL_V = 4,
+    SP_EL_I = 5,
+    SP_EL_D = 6,
+    SP_EL_NMOS = 7,
+    SP_EL_PMOS = 8,
+    SP_EL_NPN = 9,
+    SP_EL_PNP = 10
+};
+
+#define SP_MAX_FIELDS 6
+
+typedef struct sp_element {
+    int32_t kind;
+    int32_t node[3];
+    int32_t branch;
+    int32_t wave;
+    int32_t field[SP_MAX_FIELDS];
+} sp_element;
+
+/* How one per-sample parameter is produced (sweep index s, seed):
+ *   FIXED:       a
+ *   GAUSS:       gaussian_scaled(seed, s, rng_index, a, b) (rng.rs:148-150),
+ *                b is the absolute sigma
+ *   UNIFORM:     a + uniform(seed, s, rng_index) * (b - a)
+ *   LOGUNIFORM:  a * exp(uniform(seed, s, rng_index) * log(b / a))
+ *   TABLE:       column `rng_index` of a caller-supplied [samples][table_cols]
+ *                table (host generators: LCG Monte Carlo, corners, linear). */
+enum sp_draw_kind {
+    SP_DRAW_FIXED = 0,
+    SP_DRAW_GAUSS = 1,
+    SP_DRAW_UNIFORM = 2,
+    SP_DRAW_LOGUNIFORM = 3,
+    SP_DRAW_TABLE = 4
+};
+
+typedef struct sp_param {
+    int32_t kind;
+    uint32_t rng_index;
+    double a;
+    double b;
+} sp_param;
+
+/* PULSE(v1 v2 td tr tf pw per), waveforms.rs:159-182. */
+typedef struct sp_pulse {
+    double v1, v2, td, tr, tf, pw, per;
+} sp_pulse;
+
+typedef struct sp_circuit {
+    int32_t num_nodes;     /* excluding ground                          */
+    int32_t num_branches;  /* current variables: V sources + inductors  */
+    int32_t num_elements;
+    int32_t num_params;
+    int32_t num_pulses;
+    int32_t reserved;
+    const sp_element* elements;
+    const sp_param* params;
+    const sp_pulse* pulses;
+    /* Optional initial guess [num_nodes + num_branches] used when no per-sample
+     * warm start is given (a .nodeset); NULL means zero, the reference's
+     * default (newton.rs:80-83). */
+    const double* nodeset;
+} sp_circuit;
+
+/* ConvergenceCriteria (newton.rs:9-34) + stepping parameters
+ * (newton.rs:173-231) + backend choices. */
+enum sp_fallback_bits {
+    SP_FALLBACK_GMIN = 1,    /* solve_with_gmin_stepping on a miss           */
+    SP_FALLBACK_SOURCE = 2   /* solve_with_source_stepping after gmin misses */
+};
+
+typedef struct sp_newton_config {
+    double v_abstol;            /* 1e-6  */
+    double v_reltol;            /* 1e-3  */
+    double i_abstol;            /* 1e-12 */
+    double gmin;                /* 1e-12 (unused by plain Newton, as in the reference) */
+    int32_t max_iterations;     /* 50    */
+    int32_t precision;          /* sp_precision */
+    int32_t fallback;           /* sp_fallback_bits */
+    int32_t refine_steps;       /* linear refinement sweeps per Newton step (mixed) */
+    double gmin_initial;        /* 1e-3  */
+    double gmin_final;          /* 1e-12 */
+    double gmin_reduction;      /* 10    */
+    int32_t gmin_max_attempts;  /* 5     */
+    int32_t src_max_attempts;   /* 5     */
+    double src_initial;         /* 0.1   */
+    double src_step;            /* 0.1   */
+    double src_min_step;        /* 0.01  */
+} sp_newton_config;
+
+/* Fill *cfg with the reference defaults (plain FP64, gmin+source fallback). */
+void sp_newton_config_default(sp_newton_config* cfg);
+
+/* Per-sample status byte (ConvergenceStatus, convergence.rs:41-50, with
+ * flag bits saying which path produced the answer). */
+enum sp_sample_status {
+    SP_ST_CONVERGED = 0,
+    SP_ST_FAILED = 1,      /* iteration caps hit on every path              */
+    SP_ST_SINGULAR = 2,    /* a linearised system had a zero pivot           */
+    SP_ST_NONFINITE = 3,   /* NaN/Inf appeared in the iterate                */
+    SP_ST_MASK = 0x0f,
+    SP_ST_FLAG_WARM = 0x10,     /* started from the caller's warm start       */
+    SP_ST_FLAG_COLD = 0x20,     /* warm start missed; cold Newton was used    */
+    SP_ST_FLAG_GMIN = 0x40,     /* answer came from gmin stepping            */
+    SP_ST_FLAG_SOURCE = 0x80    /* answer came from source stepping          */
+};
+
+/* StatisticsAccumulator (statistics.rs:113-160): raw moments of one
+ * unknown over the converged samples. */
+typedef struct sp_moments {
+    uint64_t count;
+    double sum;
+    double sum_sq;
+    double min;
+    double max;
+} sp_moments;
+
+/* A circuit uploaded to the device once and reused across sweeps. */
+typedef struct sp_topology sp_topology;
+int sp_topology_create(sp_ctx* ctx, const sp_circuit* circuit, sp_topology** out);
+int sp_topology_destroy(sp_topology* topo);
+/* Number of MNA unknowns (nodes + branches). */
+int sp_topology_size(const sp_topology* topo);
+
+/* Batched DC operating points on device buffers.
+ *   Samples are sweep indices first_index .. first_index + num_samples - 1;
+ *   draws are keyed by (seed, sweep index, rng_index) so any split of a sweep
+ *   gives identical results.
+ *   d_table: [num_samples][table_cols] FP64 for SP_DRAW_TABLE parameters
+ *            (may be NULL when the circuit has none).
+ *   d_x0:    optional [num_samples][n] warm starts.  NULL: start from the
+ *            circuit's nodeset, or zero without one (newton.rs:80-83).  With
+ *            a warm start, a miss restarts cold from the nodeset (or zero)
+ *            before the gmin/source-stepping fallbacks.
+ *   d_x:     [num_samples][n] solutions (written for every sample).
+ *   d_iters: [num_samples] total Newton iterations over all paths (optional).
+ *   d_status:[num_samples] sp_sample_status bytes (optional).
+ *   d_resid: [num_samples] max over node rows of |KCL residual| (A) of the
+ *            returned x, evaluated in FP64 (optional).
+ *   d_params:[num_samples][num_params] the drawn parameters (optional).
+ *   d_moments: [n] moments over converged samples (optional). */
+int sp_newton_dc_device(sp_ctx* ctx, const sp_topology* topo,
+                        const sp_newton_config* cfg, uint64_t seed,
+                        uint64_t first_index, uint64_t num_samples,
+                        const double* d_table, uint32_t table_cols,
+                        const double* d_x0, double* d_x, int32_t* d_iters,
+                        uint8_t* d_status, double* d_resid, double* d_params,
+                        sp_moments* d_moments, void* stream);
+
+/* Same on host buffers (copies in and out; synchronises). */
+int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit,
+                 const sp_newton_config* cfg, uint64_t seed,
+                 uint64_t first_index, uint64_t num_samples,
+                 const double* table, uint32_t table_cols,
+                 const double* x0, double* x, int32_t* iters,
+                 uint8_t* status, double* resid, double* params,
+                 sp_moments* moments);
+
+/* Draw the per-sample parameter vectors only ([num_samples][num_params]). */
+int sp_draw_params_device(sp_ctx* ctx, const sp_topology* topo, uint64_t seed,
+                          uint64_t first_index, uint64_t num_samples,
+                          const double* d_table, uint32_t table_cols,
+                          double* d_params, void* stream);
+
+/* Raw hash RNG on device (rng.rs:39-150): out[i] for sweep index
+ * first_index + i and parameter param_index.  kind: 0 uniform, 1 gaussian,
+ * 2 uniform_f32 (as double), 3 gaussian_f32 (as double). */
+int sp_rng_fill_device(sp_ctx* ctx, int kind, uint64_t seed, uint64_t first_index,
+                       uint32_t param_index, uint64_t count, double* d_out, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Kernel timing (tracing).  The reference has only log macros and ad-hoc  */
+/* timers (crates/spicier-backend-metal/src/gpu_newton.rs:128); this adds  */
+/* CUDA-event timing around every kernel the library launches.             */
+/* ---------------------------------------------------------------------- */
+typedef struct sp_kernel_time {
+    char name[48];
+    uint64_t launches;
+    double total_ms;
+} sp_kernel_time;
+
+/* Start (on != 0) or stop recording events around each launch. */
+int sp_profile_enable(sp_ctx* ctx, int on);
+/* Synchronise, aggregate the recorded launches by kernel name into out
+ * (capacity cap), set *count, and clear the record. */
+int sp_profile_read(sp_ctx* ctx, sp_kernel_time* out, int cap, int* count);
+
+/* Moments of column `col` of a [rows][ld] FP64 matrix restricted to rows
+ * whose mask byte (optional) has (mask & SP_ST_MASK) == SP_ST_CONVERGED. */
+int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld,
+                      uint32_t cols, const uint8_t* d_status, sp_moments* d_out,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPICIER_GB300_H */

@@ -1,0 +1,136 @@
+"""CPU oracle for the batched Newton sweep — TEST INFRASTRUCTURE ONLY.
+
+The oracle is a C++ restatement of Spicier's own CPU path
+(crates/spicier-solver/src/newton.rs, crates/spicier-devices/src/*,
+crates/spicier-core/src/mna.rs, crates/spicier-batched-sweep/src/rng.rs …),
+compiled with -ffp-contract=off so that its IEEE operation sequence matches
+the Rust reference.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's
+CPU-baseline leg may load it; it is the checker, never the thing measured as
+the product.
+
+Parity pinning: the reference cannot be compiled in this environment (Rust),
+so the oracle is pinned against the reference's own unit-test known answers
+(tests/test_oracle_pins.py) and against golden vectors generated by
+tests/golden/make_golden.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle_spicier.so")
+SOURCES = ["oracle_capi.cpp"]
+HEADERS = ["oracle_core.hpp", "oracle_transient.hpp", "oracle_gmres.hpp"]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library (g++, -O2, no FMA contraction)."""
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    deps = srcs + [os.path.join(HERE, h) for h in HEADERS if os.path.exists(os.path.join(HERE, h))]
+    deps.append(os.path.join(HERE, "..", "include", "spicier_gb300.h"))
+    if not force and os.path.exists(LIB_PATH):
+        mt = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(d) <= mt for d in deps):
+            return LIB_PATH
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+           "-fno-fast-math", "-pthread", "-o", LIB_PATH + ".tmp"] + srcs
+    subprocess.run(cmd, check=True)
+    os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            _lib = _bind(C.CDLL(LIB_PATH))
+        return _lib
+
+
+def _bind(L):
+    from spicier_gb300 import _abi as abi
+    d, u64, u32, i32 = C.c_double, C.c_uint64, C.c_uint32, C.c_int
+    P = C.POINTER
+    sig = {
+        "or_splitmix64": (u64, [u64]),
+        "or_combine_indices": (u64, [u64, u32, u32]),
+        "or_uniform": (d, [u64, u32, u32]),
+        "or_uniform_f32": (C.c_float, [u64, u32, u32]),
+        "or_gaussian": (d, [u64, u32, u32]),
+        "or_gaussian_f32": (C.c_float, [u64, u32, u32]),
+        "or_rng_fill": (None, [i32, u64, u64, u32, u64, P(d)]),
+        "or_mos_evaluate": (i32, [i32, P(d), d, d, P(d)]),
+        "or_diode_evaluate": (None, [d, d, d, P(d)]),
+        "or_limit_voltage": (d, [d, d]),
+        "or_thermal_voltage": (d, [d]),
+        "or_bjt_evaluate": (None, [i32, P(d), d, d, P(d)]),
+        "or_stamp_dc": (i32, [P(abi.SpCircuit), P(d), P(d), i32, d, P(d), P(d)]),
+        "or_lu_solve": (i32, [i32, P(d), P(d)]),
+        "or_solve_batch": (None, [P(d), P(d), u64, u64, P(d), P(C.c_uint8), i32]),
+        "or_draw_params": (i32, [P(abi.SpCircuit), u64, u64, u64, P(d), u32, P(d)]),
+        "or_newton_single": (i32, [P(abi.SpCircuit), P(d), P(abi.SpNewtonConfig), i32, d, P(d), P(i32)]),
+        "or_stepping": (i32, [P(abi.SpCircuit), P(d), P(abi.SpNewtonConfig), i32, P(d), P(i32)]),
+        "or_newton_dc": (i32, [P(abi.SpCircuit), P(abi.SpNewtonConfig), u64, u64, u64, P(d), u32,
+                               P(d), P(d), P(C.c_int32), P(C.c_uint8), P(d), i32]),
+        "or_moments": (None, [P(d), u64, u32, u32, P(C.c_uint8), P(abi.SpMoments)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
+    return L
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def newton_dc(circuit, cfg, seed, count, first=0, table=None, x0=None, threads=0):
+    """Oracle sweep: returns (x[count,n], iters[count], status[count], params[count,np])."""
+    L = lib()
+    n, npar = circuit.n, len(circuit.params)
+    x = np.zeros((count, n))
+    iters = np.zeros(count, np.int32)
+    status = np.zeros(count, np.uint8)
+    params = np.zeros((count, max(npar, 1)))
+    cols = 0
+    if table is not None:
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        cols = table.shape[1]
+    if x0 is not None:
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+    cc = circuit.to_c()
+    L.or_newton_dc(C.byref(cc), C.byref(cfg), seed, first, count, _dp(table), cols, _dp(x0), _dp(x),
+                   iters.ctypes.data_as(C.POINTER(C.c_int32)),
+                   status.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(params), threads)
+    return x, iters, status, params[:, :npar]
+
+
+def draw_params(circuit, seed, count, first=0, table=None):
+    L = lib()
+    out = np.zeros((count, max(len(circuit.params), 1)))
+    cols = 0
+    if table is not None:
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        cols = table.shape[1]
+    cc = circuit.to_c()
+    L.or_draw_params(C.byref(cc), seed, first, count, _dp(table), cols, _dp(out))
+    return out[:, :len(circuit.params)]
+
+
+def solve_batch(mats, rhs, n, batch, threads=0):
+    L = lib()
+    mats = np.ascontiguousarray(mats, dtype=np.float64)
+    rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+    sol = np.zeros(batch * n)
+    sing = np.zeros(batch, np.uint8)
+    L.or_solve_batch(_dp(mats), _dp(rhs), n, batch, _dp(sol), sing.ctypes.data_as(C.POINTER(C.c_uint8)), threads)
+    return sol, sing

@@ -1,0 +1,192 @@
+// C ABI of the CPU oracle (TEST INFRASTRUCTURE ONLY; see oracle_core.hpp).
+//
+// Loaded with ctypes by tests/ and by bench.py's CPU-baseline leg.  The
+// multi-sample entry points spread samples over a pool of std::threads with
+// an atomic work counter, the shape of solve_batched_sweep_parallel's rayon
+// par_iter (crates/spicier-batched-sweep/src/parallel.rs:142-156): one
+// independent solver state per worker, samples handed out in small chunks.
+#include <algorithm>
+#include <atomic>
+#include <thread>
+
+#include "oracle_core.hpp"
+
+
+using namespace oracle;
+
+namespace {
+
+template <class F>
+void parallel_for(uint64_t count, int threads, F&& body) {
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (threads == 1 || count < 2) {
+        body(0, 0, count);
+        return;
+    }
+    std::atomic<uint64_t> next{0};
+    const uint64_t chunk = 16;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        pool.emplace_back([&, t] {
+            for (;;) {
+                uint64_t lo = next.fetch_add(chunk);
+                if (lo >= count) break;
+                body(t, lo, std::min(count, lo + chunk));
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t or_splitmix64(uint64_t x) { return splitmix64(x); }
+uint64_t or_combine_indices(uint64_t seed, uint32_t s, uint32_t p) { return combine_indices(seed, s, p); }
+double or_uniform(uint64_t seed, uint32_t s, uint32_t p) { return uniform(seed, s, p); }
+float or_uniform_f32(uint64_t seed, uint32_t s, uint32_t p) { return uniform_f32(seed, s, p); }
+double or_gaussian(uint64_t seed, uint32_t s, uint32_t p) { return gaussian(seed, s, p); }
+float or_gaussian_f32(uint64_t seed, uint32_t s, uint32_t p) { return gaussian_f32(seed, s, p); }
+
+// kind: 0 uniform, 1 gaussian, 2 uniform_f32, 3 gaussian_f32 (sp_rng_fill_device).
+void or_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t param, uint64_t count,
+                 double* out) {
+    for (uint64_t i = 0; i < count; ++i) {
+        uint32_t s = (uint32_t)(first + i);
+        switch (kind) {
+            case 0: out[i] = uniform(seed, s, param); break;
+            case 1: out[i] = gaussian(seed, s, param); break;
+            case 2: out[i] = (double)uniform_f32(seed, s, param); break;
+            default: out[i] = (double)gaussian_f32(seed, s, param); break;
+        }
+    }
+}
+
+int or_mos_evaluate(int pmos, const double* p6, double vgs, double vds, double* out3) {
+    MosParams mp{p6[0], p6[1], p6[2], p6[3], p6[4], p6[5]};
+    return mos_evaluate(pmos != 0, mp, vgs, vds, &out3[0], &out3[1], &out3[2]);
+}
+
+void or_diode_evaluate(double is, double n, double vd, double* out2) {
+    diode_evaluate(is, n, vd, &out2[0], &out2[1]);
+}
+
+double or_limit_voltage(double vd, double nvt) { return limit_voltage(vd, nvt); }
+double or_thermal_voltage(double t) { return thermal_voltage(t); }
+
+void or_bjt_evaluate(int pnp, const double* p6, double vbe, double vce, double* out6) {
+    BjtParams bp{p6[0], p6[1], p6[2], p6[3], p6[4], p6[5]};
+    bjt_evaluate(pnp != 0, bp, vbe, vce, out6);
+}
+
+// mode: 0 plain, 1 gmin (aux = gmin), 2 source-scaled (aux = factor).
+// A receives the column-major dense matrix, b the RHS.
+int or_stamp_dc(const sp_circuit* c, const double* P, const double* x, int mode, double aux,
+                double* A, double* b) {
+    Mna m;
+    m.init(c->num_nodes, c->num_branches);
+    stamp_dc(*c, P, x, m, mode == 2, aux);
+    if (mode == 1) m.gmin(aux);
+    std::copy(m.A.begin(), m.A.end(), A);
+    std::copy(m.b.begin(), m.b.end(), b);
+    return 0;
+}
+
+// nalgebra-style LU solve in place; returns 1 when singular.
+int or_lu_solve(int n, double* A, double* b) { return lu_solve(n, A, b) ? 0 : 1; }
+
+// CpuBatchedSolver::solve_batch (crates/spicier-batched-sweep/src/solver.rs:326-384):
+// singular systems get zero solutions and singular[i] = 1.
+void or_solve_batch(const double* mats, const double* rhs, uint64_t n, uint64_t batch,
+                    double* sol, uint8_t* singular, int threads) {
+    parallel_for(batch, threads, [&](int, uint64_t lo, uint64_t hi) {
+        std::vector<double> A(n * n);
+        for (uint64_t i = lo; i < hi; ++i) {
+            std::copy(mats + i * n * n, mats + (i + 1) * n * n, A.begin());
+            double* x = sol + i * n;
+            std::copy(rhs + i * n, rhs + (i + 1) * n, x);
+            bool ok = lu_solve((int)n, A.data(), x);
+            if (!ok) std::fill(x, x + n, 0.0);
+            singular[i] = ok ? 0 : 1;
+        }
+    });
+}
+
+int or_draw_params(const sp_circuit* c, uint64_t seed, uint64_t first, uint64_t count,
+                   const double* table, uint32_t cols, double* out) {
+    for (uint64_t i = 0; i < count; ++i) {
+        const double* row = table ? table + i * cols : nullptr;
+        for (int k = 0; k < c->num_params; ++k)
+            out[i * c->num_params + k] = draw_param(c->params[k], seed, (uint32_t)(first + i), row);
+    }
+    return 0;
+}
+
+// One Newton-Raphson solve (mode 0 plain, 1 gmin with aux, 2 scaled with aux).
+// Returns bit0 converged, bit1 singular; *iters iterations.  x: guess in, result out.
+int or_newton_single(const sp_circuit* c, const double* P, const sp_newton_config* cfg, int mode,
+                     double aux, double* x, int* iters) {
+    Mna m;
+    m.init(c->num_nodes, c->num_branches);
+    StampMode sm = mode == 1 ? StampMode::Gmin : mode == 2 ? StampMode::Scaled : StampMode::Plain;
+    NrOutcome r = newton(*c, P, *cfg, sm, aux, x, m);
+    *iters = r.iterations;
+    return (r.converged ? 1 : 0) | (r.singular ? 2 : 0);
+}
+
+// which: 0 gmin stepping, 1 source stepping.  out3 = {converged, total_iterations, num_levels}.
+int or_stepping(const sp_circuit* c, const double* P, const sp_newton_config* cfg, int which,
+                double* x, int* out3) {
+    Mna m;
+    m.init(c->num_nodes, c->num_branches);
+    SteppingOutcome s =
+        which == 0 ? gmin_stepping(*c, P, *cfg, x, m) : source_stepping(*c, P, *cfg, x, m);
+    out3[0] = s.converged;
+    out3[1] = s.total_iterations;
+    out3[2] = s.num_levels;
+    return s.singular ? 1 : 0;
+}
+
+// Batched DC operating points: the CPU restatement of sp_newton_dc.
+int or_newton_dc(const sp_circuit* c, const sp_newton_config* cfg, uint64_t seed, uint64_t first,
+                 uint64_t count, const double* table, uint32_t cols, const double* x0, double* x,
+                 int32_t* iters, uint8_t* status, double* params, int threads) {
+    const int n = c->num_nodes + c->num_branches;
+    const int np = c->num_params;
+    parallel_for(count, threads, [&](int, uint64_t lo, uint64_t hi) {
+        Mna m;
+        m.init(c->num_nodes, c->num_branches);
+        std::vector<double> P(np);
+        for (uint64_t i = lo; i < hi; ++i) {
+            const double* row = table ? table + i * cols : nullptr;
+            for (int k = 0; k < np; ++k)
+                P[k] = draw_param(c->params[k], seed, (uint32_t)(first + i), row);
+            if (params) std::copy(P.begin(), P.end(), params + i * np);
+            int it = 0;
+            uint8_t st = dc_pipeline(*c, P.data(), *cfg, x0 ? x0 + i * n : nullptr, x + i * n, &it, m);
+            if (iters) iters[i] = it;
+            if (status) status[i] = st;
+        }
+    });
+    return 0;
+}
+
+// StatisticsAccumulator over column `col` (statistics.rs:113-160), samples in
+// index order, optionally restricted to converged status bytes.
+void or_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t col,
+                const uint8_t* status, sp_moments* out) {
+    sp_moments m{0, 0.0, 0.0, INFINITY, -INFINITY};
+    for (uint64_t i = 0; i < rows; ++i) {
+        if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+        double v = values[i * ld + col];
+        m.count += 1;
+        m.sum += v;
+        m.sum_sq += v * v;
+        m.min = std::fmin(m.min, v);
+        m.max = std::fmax(m.max, v);
+    }
+    *out = m;
+}
+
+}  // extern "C"

@@ -1,0 +1,162 @@
+"""ctypes mirror of ``include/spicier_gb300.h``.
+
+Struct layouts, enum values and defaults here must match the header byte for
+byte; ``tests/test_abi.py`` checks sizes and offsets against the compiled
+library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+# sp_status (BatchedSweepError, crates/spicier-batched-sweep/src/error.rs:7-43)
+SP_OK = 0
+SP_ERR_NO_BACKEND = -1
+SP_ERR_BACKEND_INIT = -2
+SP_ERR_MEMORY_ALLOC = -3
+SP_ERR_TRANSFER = -4
+SP_ERR_INVALID_DIMENSION = -5
+SP_ERR_BATCH_TOO_LARGE = -6
+SP_ERR_SINGULAR_BATCH = -7
+SP_ERR_BACKEND = -8
+SP_ERR_SOLVER = -9
+SP_ERR_INVALID_ARGUMENT = -10
+
+STATUS_NAMES = {
+    SP_ERR_NO_BACKEND: "NoBackendAvailable",
+    SP_ERR_BACKEND_INIT: "BackendInit",
+    SP_ERR_MEMORY_ALLOC: "MemoryAlloc",
+    SP_ERR_TRANSFER: "Transfer",
+    SP_ERR_INVALID_DIMENSION: "InvalidDimension",
+    SP_ERR_BATCH_TOO_LARGE: "BatchTooLarge",
+    SP_ERR_SINGULAR_BATCH: "SingularBatch",
+    SP_ERR_BACKEND: "Backend",
+    SP_ERR_SOLVER: "Solver",
+    SP_ERR_INVALID_ARGUMENT: "InvalidArgument",
+}
+
+# sp_backend_type (BackendType, crates/spicier-batched-sweep/src/solver.rs:79-92)
+SP_BACKEND_CUDA, SP_BACKEND_METAL, SP_BACKEND_MPS = 0, 1, 2
+SP_BACKEND_ACCELERATE, SP_BACKEND_FAER, SP_BACKEND_CPU, SP_BACKEND_GB300 = 3, 4, 5, 6
+
+SP_PREC_FP64 = 0
+SP_PREC_MIXED = 1
+SP_PREC_FP64_EXACT = 2
+
+# sp_element_kind
+SP_EL_R, SP_EL_C, SP_EL_L, SP_EL_V, SP_EL_I = 1, 2, 3, 4, 5
+SP_EL_D, SP_EL_NMOS, SP_EL_PMOS, SP_EL_NPN, SP_EL_PNP = 6, 7, 8, 9, 10
+SP_MAX_FIELDS = 6
+
+# sp_draw_kind
+SP_DRAW_FIXED, SP_DRAW_GAUSS, SP_DRAW_UNIFORM, SP_DRAW_LOGUNIFORM, SP_DRAW_TABLE = 0, 1, 2, 3, 4
+
+# sp_fallback_bits
+SP_FALLBACK_GMIN = 1
+SP_FALLBACK_SOURCE = 2
+
+# sp_sample_status
+SP_ST_CONVERGED = 0
+SP_ST_FAILED = 1
+SP_ST_SINGULAR = 2
+SP_ST_NONFINITE = 3
+SP_ST_MASK = 0x0F
+SP_ST_FLAG_WARM = 0x10
+SP_ST_FLAG_COLD = 0x20
+SP_ST_FLAG_GMIN = 0x40
+SP_ST_FLAG_SOURCE = 0x80
+
+
+class SpBatchConfig(C.Structure):
+    _fields_ = [
+        ("min_batch_size", C.c_uint64),
+        ("min_matrix_size", C.c_uint64),
+        ("max_batch_per_launch", C.c_uint64),
+    ]
+
+
+class SpElement(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("node", C.c_int32 * 3),
+        ("branch", C.c_int32),
+        ("wave", C.c_int32),
+        ("field", C.c_int32 * SP_MAX_FIELDS),
+    ]
+
+
+class SpParam(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("rng_index", C.c_uint32),
+        ("a", C.c_double),
+        ("b", C.c_double),
+    ]
+
+
+class SpPulse(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("v1", "v2", "td", "tr", "tf", "pw", "per")]
+
+
+class SpCircuit(C.Structure):
+    _fields_ = [
+        ("num_nodes", C.c_int32),
+        ("num_branches", C.c_int32),
+        ("num_elements", C.c_int32),
+        ("num_params", C.c_int32),
+        ("num_pulses", C.c_int32),
+        ("reserved", C.c_int32),
+        ("elements", C.POINTER(SpElement)),
+        ("params", C.POINTER(SpParam)),
+        ("pulses", C.POINTER(SpPulse)),
+        ("nodeset", C.POINTER(C.c_double)),
+    ]
+
+
+class SpNewtonConfig(C.Structure):
+    _fields_ = [
+        ("v_abstol", C.c_double),
+        ("v_reltol", C.c_double),
+        ("i_abstol", C.c_double),
+        ("gmin", C.c_double),
+        ("max_iterations", C.c_int32),
+        ("precision", C.c_int32),
+        ("fallback", C.c_int32),
+        ("refine_steps", C.c_int32),
+        ("gmin_initial", C.c_double),
+        ("gmin_final", C.c_double),
+        ("gmin_reduction", C.c_double),
+        ("gmin_max_attempts", C.c_int32),
+        ("src_max_attempts", C.c_int32),
+        ("src_initial", C.c_double),
+        ("src_step", C.c_double),
+        ("src_min_step", C.c_double),
+    ]
+
+
+class SpMoments(C.Structure):
+    _fields_ = [
+        ("count", C.c_uint64),
+        ("sum", C.c_double),
+        ("sum_sq", C.c_double),
+        ("min", C.c_double),
+        ("max", C.c_double),
+    ]
+
+
+def newton_config(
+    precision: int = SP_PREC_FP64,
+    fallback: int = SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE,
+    max_iterations: int = 50,
+    v_abstol: float = 1e-6,
+    v_reltol: float = 1e-3,
+    i_abstol: float = 1e-12,
+    refine_steps: int = 0,
+) -> SpNewtonConfig:
+    """ConvergenceCriteria::default() + Gmin/SourceSteppingParams::default()
+    (crates/spicier-solver/src/newton.rs:24-34, 187-196, 222-231)."""
+    c = SpNewtonConfig()
+    c.v_abstol, c.v_reltol, c.i_abstol, c.gmin = v_abstol, v_reltol, i_abstol, 1e-12
+    c.max_iterations, c.precision, c.fallback, c.refine_steps = max_iterations, precision, fallback, refine_steps
+    c.gmin_initial, c.gmin_final, c.gmin_reduction, c.gmin_max_attempts = 1e-3, 1e-12, 10.0, 5
+    c.src_max_attempts, c.src_initial, c.src_step, c.src_min_step = 5, 0.1, 0.1, 0.01
+    return c

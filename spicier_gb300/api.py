@@ -1,0 +1,422 @@
+"""Host-side mirror of Spicier's batched-sweep interface over the C ABI.
+
+Names, argument meanings and error behaviour follow the reference:
+  BatchedLuSolver / BatchedSolveResult / GpuBatchConfig / BackendType
+      crates/spicier-batched-sweep/src/solver.rs:15-135
+  BatchedSweepError -> SpicierError (kind = variant name)
+      crates/spicier-batched-sweep/src/error.rs:7-43
+  ParameterVariation, SweepPoint, Monte Carlo / corner / linear generators
+      crates/spicier-solver/src/sweep.rs:15-266
+  solve_batched_sweep_gpu, GpuBatchedSweepResult
+      crates/spicier-batched-sweep/src/sweep.rs:15-217
+  ConvergenceCriteria + stepping parameters -> _abi.newton_config()
+      crates/spicier-solver/src/newton.rs:9-34, 173-231
+The Newton sweep (solve_newton_sweep_gpu) has no counterpart in the
+reference's sweep API, which is linear-only; it batches solve_newton_raphson
+(crates/spicier-solver/src/newton.rs:70-131) per sweep point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _abi as abi
+from ._lib import SpicierError, check, load
+from .circuit import Circuit
+
+MAX_BATCH_SIZE = 65535  # the reference's cuBLAS cap (solver.rs:5); not a limit here
+MIN_BATCH_SIZE = 16
+MIN_MATRIX_SIZE = 32
+
+
+def _vp(a) -> Optional[int]:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())  # torch tensor
+
+
+class BackendType(enum.IntEnum):
+    Cuda = abi.SP_BACKEND_CUDA
+    Metal = abi.SP_BACKEND_METAL
+    Mps = abi.SP_BACKEND_MPS
+    Accelerate = abi.SP_BACKEND_ACCELERATE
+    Faer = abi.SP_BACKEND_FAER
+    Cpu = abi.SP_BACKEND_CPU
+    Gb300 = abi.SP_BACKEND_GB300
+
+
+@dataclass
+class GpuBatchConfig:
+    min_batch_size: int = MIN_BATCH_SIZE
+    min_matrix_size: int = 1
+    max_batch_per_launch: int = 1 << 26
+
+    def should_use_gpu(self, matrix_size: int, batch_size: int) -> bool:
+        return matrix_size >= self.min_matrix_size and batch_size >= self.min_batch_size
+
+
+@dataclass
+class BatchedSolveResult:
+    solutions: np.ndarray
+    singular_indices: List[int]
+    n: int
+    batch_size: int
+
+    def solution(self, index: int):
+        if index >= self.batch_size:
+            return None
+        return self.solutions[index * self.n:(index + 1) * self.n]
+
+    def is_singular(self, index: int) -> bool:
+        return index in self.singular_indices
+
+    def num_solved(self) -> int:
+        return self.batch_size - len(self.singular_indices)
+
+
+@dataclass
+class NewtonResult:
+    """Per-sample outputs of a batched DC operating-point sweep."""
+    x: np.ndarray
+    iters: np.ndarray
+    status: np.ndarray
+    resid: Optional[np.ndarray] = None
+    params: Optional[np.ndarray] = None
+    moments: Optional[list] = None
+
+    @property
+    def converged(self) -> np.ndarray:
+        return (self.status & abi.SP_ST_MASK) == abi.SP_ST_CONVERGED
+
+    @property
+    def converged_count(self) -> int:
+        return int(self.converged.sum())
+
+
+class Topology:
+    """A circuit uploaded to the device (sp_topology)."""
+
+    def __init__(self, ctx: "Context", circuit: Circuit):
+        self.ctx = ctx
+        self.circuit = circuit
+        self._ptr = C.c_void_p()
+        cc = circuit.to_c()
+        check(ctx._ptr, load().sp_topology_create(ctx._ptr, C.byref(cc), C.byref(self._ptr)))
+        self.n = load().sp_topology_size(self._ptr)
+
+    def close(self):
+        if self._ptr:
+            load().sp_topology_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One device context (sp_ctx)."""
+
+    def __init__(self, device: int = 0):
+        L = load()
+        self._ptr = C.c_void_p()
+        rc = L.sp_ctx_create(device, C.byref(self._ptr))
+        if rc != 0:
+            raise SpicierError(rc, f"cannot open CUDA device {device}")
+        self.device = device
+
+    def close(self):
+        if self._ptr:
+            load().sp_ctx_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def version() -> str:
+        return load().sp_version().decode()
+
+    # -- BatchedLuSolver ---------------------------------------------------
+    def config(self) -> GpuBatchConfig:
+        c = abi.SpBatchConfig()
+        check(self._ptr, load().sp_get_config(self._ptr, C.byref(c)))
+        return GpuBatchConfig(c.min_batch_size, c.min_matrix_size, c.max_batch_per_launch)
+
+    def set_config(self, cfg: GpuBatchConfig):
+        c = abi.SpBatchConfig(cfg.min_batch_size, cfg.min_matrix_size, cfg.max_batch_per_launch)
+        check(self._ptr, load().sp_set_config(self._ptr, C.byref(c)))
+
+    def solve_batch(self, matrices, rhs, n: int, batch_size: int) -> BatchedSolveResult:
+        mats = np.ascontiguousarray(matrices, dtype=np.float64).ravel()
+        b = np.ascontiguousarray(rhs, dtype=np.float64).ravel()
+        if mats.size != batch_size * n * n:
+            raise SpicierError(abi.SP_ERR_INVALID_DIMENSION,
+                               f"Expected {batch_size * n * n} matrix elements, got {mats.size}")
+        if b.size != batch_size * n:
+            raise SpicierError(abi.SP_ERR_INVALID_DIMENSION, f"Expected {batch_size * n} RHS elements, got {b.size}")
+        sol = np.zeros(batch_size * n)
+        sing = np.zeros(max(batch_size, 1), np.uint64)
+        ns = C.c_uint64(0)
+        check(self._ptr, load().sp_solve_batch(self._ptr, _vp(mats), _vp(b), n, batch_size, _vp(sol), _vp(sing),
+                                               C.byref(ns)))
+        return BatchedSolveResult(sol, [int(i) for i in sing[:ns.value]], n, batch_size)
+
+    def solve_batch_device(self, d_mats, d_rhs, n, batch, d_sol, d_sing, precision=abi.SP_PREC_FP64,
+                           refine_steps=2, stream=0):
+        check(self._ptr, load().sp_solve_batch_device(self._ptr, _vp(d_mats), _vp(d_rhs), n, batch, _vp(d_sol),
+                                                      _vp(d_sing), precision, refine_steps, stream))
+
+    # -- Newton sweeps -------------------------------------------------------
+    def topology(self, circuit: Circuit) -> Topology:
+        return Topology(self, circuit)
+
+    def newton_dc(self, circuit: Circuit, cfg: abi.SpNewtonConfig, seed: int, count: int, first: int = 0,
+                  table=None, x0=None, params: bool = False, resid: bool = True,
+                  moments: bool = False) -> NewtonResult:
+        """Host-buffer batched DC operating points (sp_newton_dc)."""
+        n = circuit.n
+        x = np.zeros((count, n))
+        iters = np.zeros(count, np.int32)
+        status = np.zeros(count, np.uint8)
+        r = np.zeros(count) if resid else None
+        p = np.zeros((count, max(len(circuit.params), 1))) if params else None
+        m = (abi.SpMoments * n)() if moments else None
+        cols = 0
+        if table is not None:
+            table = np.ascontiguousarray(table, dtype=np.float64)
+            cols = table.shape[1]
+        if x0 is not None:
+            x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        cc = circuit.to_c()
+        check(self._ptr, load().sp_newton_dc(self._ptr, C.byref(cc), C.byref(cfg), seed, first, count, _vp(table),
+                                             cols, _vp(x0), _vp(x), _vp(iters), _vp(status), _vp(r), _vp(p),
+                                             C.cast(m, C.c_void_p) if m is not None else None))
+        mom = None
+        if m is not None:
+            mom = [dict(count=mm.count, sum=mm.sum, sum_sq=mm.sum_sq, min=mm.min, max=mm.max) for mm in m]
+        return NewtonResult(x, iters, status, r, p[:, :len(circuit.params)] if p is not None else None, mom)
+
+    def newton_dc_device(self, topo: Topology, cfg: abi.SpNewtonConfig, seed: int, count: int, x, first: int = 0,
+                         table=None, x0=None, iters=None, status=None, resid=None, params=None, moments=None,
+                         stream: int = 0):
+        """Device-buffer batched DC operating points (sp_newton_dc_device);
+        buffers are torch CUDA tensors (or raw device pointers via .data_ptr())."""
+        cols = 0 if table is None else int(table.shape[1])
+        check(self._ptr, load().sp_newton_dc_device(self._ptr, topo._ptr, C.byref(cfg), seed, first, count,
+                                                    _vp(table), cols, _vp(x0), _vp(x), _vp(iters), _vp(status),
+                                                    _vp(resid), _vp(params), _vp(moments), stream))
+
+    def rng_fill_device(self, kind: int, seed: int, first: int, param: int, count: int, out, stream: int = 0):
+        check(self._ptr, load().sp_rng_fill_device(self._ptr, kind, seed, first, param, count, _vp(out), stream))
+
+    def profile_enable(self, on: bool = True):
+        check(self._ptr, load().sp_profile_enable(self._ptr, 1 if on else 0))
+
+    def profile_read(self) -> dict:
+        """{kernel name: (launches, total_ms)} since the last read."""
+        from ._lib import SpKernelTime
+        buf = (SpKernelTime * 64)()
+        cnt = C.c_int(0)
+        check(self._ptr, load().sp_profile_read(self._ptr, buf, 64, C.byref(cnt)))
+        return {buf[i].name.decode(): (int(buf[i].launches), float(buf[i].total_ms)) for i in range(cnt.value)}
+
+    def moments_device(self, values, rows, ld, cols, status, out, stream: int = 0):
+        check(self._ptr, load().sp_moments_device(self._ptr, _vp(values), rows, ld, cols, _vp(status), _vp(out),
+                                                  stream))
+
+
+# ---------------------------------------------------------------------------
+# BatchedLuSolver mirror and the sweep API
+# ---------------------------------------------------------------------------
+class Gb300BatchedSolver:
+    """BatchedLuSolver implementation backed by the GB300 kernels."""
+
+    def __init__(self, config: Optional[GpuBatchConfig] = None, device: int = 0):
+        self.ctx = Context(device)
+        if config is not None:
+            self.ctx.set_config(config)
+
+    def solve_batch(self, matrices, rhs, n: int, batch_size: int) -> BatchedSolveResult:
+        return self.ctx.solve_batch(matrices, rhs, n, batch_size)
+
+    def should_use_gpu(self, matrix_size: int, batch_size: int) -> bool:
+        return self.ctx.config().should_use_gpu(matrix_size, batch_size)
+
+    def backend_type(self) -> BackendType:
+        return BackendType(load().sp_backend_type())
+
+    def config(self) -> GpuBatchConfig:
+        return self.ctx.config()
+
+
+class BackendSelector:
+    """BackendSelector (solver.rs:137-312) reduced to the one backend here."""
+
+    def __init__(self, device: int = 0, config: Optional[GpuBatchConfig] = None):
+        self.device = device
+        self.config = config or GpuBatchConfig()
+
+    @staticmethod
+    def auto():
+        return BackendSelector()
+
+    def create_solver(self) -> Gb300BatchedSolver:
+        return Gb300BatchedSolver(self.config, self.device)
+
+
+@dataclass
+class ParameterVariation:
+    """crates/spicier-solver/src/sweep.rs:15-54 (defaults +-10 %, sigma 5 %)."""
+    name: str
+    nominal: float
+    min: float = math.nan
+    max: float = math.nan
+    sigma: float = 0.05
+
+    def __post_init__(self):
+        if math.isnan(self.min):
+            self.min = self.nominal * 0.9
+        if math.isnan(self.max):
+            self.max = self.nominal * 1.1
+
+    def with_bounds(self, lo, hi):
+        self.min, self.max = lo, hi
+        return self
+
+    def with_sigma(self, s):
+        self.sigma = s
+        return self
+
+
+@dataclass
+class SweepPoint:
+    parameters: List[float]
+
+
+class MonteCarloGenerator:
+    """LCG Monte Carlo generator (sweep.rs:145-200), seed default 12345."""
+
+    def __init__(self, num_samples: int, seed: int = 12345):
+        self.num_samples, self.seed = num_samples, seed
+
+    def with_seed(self, seed):
+        self.seed = seed
+        return self
+
+    def generate(self, variations: Sequence[ParameterVariation]) -> List[SweepPoint]:
+        state = self.seed & 0xFFFFFFFFFFFFFFFF
+
+        def nxt():
+            nonlocal state
+            state = (state * 6364136223846793005 + 1) & 0xFFFFFFFFFFFFFFFF
+            return (state >> 33) / float(1 << 31)
+
+        pts = []
+        for _ in range(self.num_samples):
+            vals = []
+            for v in variations:
+                u1 = max(nxt(), 1e-10)
+                u2 = nxt()
+                z = math.sqrt(-2.0 * math.log(u1)) * math.cos(2.0 * math.pi * u2)
+                vals.append(min(max(v.nominal + z * v.sigma * v.nominal, v.min), v.max))
+            pts.append(SweepPoint(vals))
+        return pts
+
+
+class CornerGenerator:
+    """All 2^k min/max corners, bit j -> parameter j (sweep.rs:202-227)."""
+
+    def generate(self, variations):
+        if not variations:
+            return [SweepPoint([])]
+        k = len(variations)
+        return [SweepPoint([v.max if (i >> j) & 1 else v.min for j, v in enumerate(variations)])
+                for i in range(1 << k)]
+
+
+class LinearSweepGenerator:
+    """min..max in num_points steps, all parameters together (sweep.rs:229-266)."""
+
+    def __init__(self, num_points: int):
+        self.num_points = num_points
+
+    def generate(self, variations):
+        if not variations:
+            return [SweepPoint([])]
+        out = []
+        for i in range(self.num_points):
+            t = i / (self.num_points - 1) if self.num_points > 1 else 0.5
+            out.append(SweepPoint([v.min + t * (v.max - v.min) for v in variations]))
+        return out
+
+
+@dataclass
+class GpuBatchedSweepResult:
+    """crates/spicier-batched-sweep/src/sweep.rs:15-55."""
+    solutions: List[np.ndarray]
+    points: List[SweepPoint]
+    converged_count: int
+    total_count: int
+    singular_indices: List[int]
+    used_gpu: bool
+    backend_used: BackendType
+
+    def node_voltages(self, node_index: int):
+        return [s[node_index] for s in self.solutions]
+
+
+def solve_batched_sweep_gpu(backend: BackendSelector, factory, generator, variations,
+                            criteria=None, config: Optional[GpuBatchConfig] = None) -> GpuBatchedSweepResult:
+    """Linear sweep through BatchedLuSolver::solve_batch (sweep.rs:101-217):
+    generate points, let ``factory.create_stamper(params)`` stamp each
+    point's dense system (stamp_linear(matrix, rhs) on numpy arrays), solve the
+    batch on the GPU.  ``criteria`` is accepted and unused, as in the reference."""
+    points = generator.generate(variations)
+    total = len(points)
+    if total == 0:
+        return GpuBatchedSweepResult([], [], 0, 0, [], False, BackendType.Cpu)
+    first = factory.create_stamper(points[0].parameters)
+    size = first.num_nodes() + first.num_vsources()
+    solver = backend.create_solver()
+    mats = np.zeros((total, size, size))
+    rhs = np.zeros((total, size))
+    for i, p in enumerate(points):
+        st = factory.create_stamper(p.parameters)
+        m = np.zeros((size, size))
+        b = np.zeros(size)
+        st.stamp_linear(m, b)
+        mats[i] = m.T  # column-major
+        rhs[i] = b
+    res = solver.solve_batch(mats.ravel(), rhs.ravel(), size, total)
+    sols = [res.solution(i).copy() for i in range(total)]
+    return GpuBatchedSweepResult(sols, points, total - len(res.singular_indices), total, res.singular_indices,
+                                 True, solver.backend_type())
+
+
+def solve_newton_sweep_gpu(ctx: Context, circuit: Circuit, seed: int, num_samples: int,
+                           criteria: Optional[abi.SpNewtonConfig] = None, generator=None, variations=None,
+                           x0=None) -> NewtonResult:
+    """Nonlinear sweep: every point solved by batched Newton on the GPU.
+    Parameters drawn by the hash RNG inside the kernel (seed), or — when a
+    host ``generator`` is given — taken from its points as a table whose
+    columns the circuit references with ``Table(col)``."""
+    cfg = criteria or abi.newton_config()
+    table = None
+    if generator is not None:
+        pts = generator.generate(variations or [])
+        table = np.array([p.parameters for p in pts], dtype=np.float64)
+        num_samples = len(pts)
+    return ctx.newton_dc(circuit, cfg, seed, num_samples, table=table, x0=x0, resid=True)

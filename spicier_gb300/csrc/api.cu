@@ -1,0 +1,623 @@
+// C ABI of libspicier_gb300 (declarations and reference citations in
+// include/spicier_gb300.h).  Host-side orchestration only: argument checks,
+// the device copy of a circuit, scratch management and kernel launches.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+using namespace sp;
+
+namespace {
+
+int fail(sp_ctx* ctx, int code, const char* fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->last_error = buf;
+    }
+    return code;
+}
+
+int cuda_fail(sp_ctx* ctx, cudaError_t e, const char* what) {
+    int code = (e == cudaErrorMemoryAllocation) ? SP_ERR_MEMORY_ALLOC : SP_ERR_BACKEND;
+    return fail(ctx, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SP_CUDA(ctx, expr, what)                           \
+    do {                                                   \
+        cudaError_t e_ = (expr);                           \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Grow-only device scratch owned by the context.
+int ensure_scratch(sp_ctx* ctx, size_t bytes) {
+    if (bytes <= ctx->scratch_bytes) return SP_OK;
+    if (ctx->scratch) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronise before scratch growth");
+        cudaFree(ctx->scratch);
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+    }
+    size_t want = align256(bytes + bytes / 4);
+    cudaError_t e = cudaMalloc(&ctx->scratch, want);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scratch allocation");
+    ctx->scratch_bytes = want;
+    return SP_OK;
+}
+
+// Threads per block of the thread-per-sample kernels: the largest multiple of
+// 32 up to 128 whose shared-memory work area stays within ~110 KB (two blocks
+// per SM on a 228 KB SM).
+int pick_block(size_t per_thread, int max_smem) {
+    int block = 128;
+    while (block > 32 && per_thread * block > 110 * 1024) block -= 32;
+    if (per_thread * block > (size_t)max_smem) return 0;
+    return block;
+}
+
+// Calls on different streams share the context's scratch: each call orders
+// itself after the previous user (skipped while the stream is being captured
+// into a CUDA graph, where the caller orders the work).
+struct ScratchOrder {
+    sp_ctx* ctx;
+    cudaStream_t st;
+    bool capturing = false;
+    ScratchOrder(sp_ctx* c, cudaStream_t s) : ctx(c), st(s) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cs);
+        capturing = cs != cudaStreamCaptureStatusNone;
+        if (!capturing) cudaStreamWaitEvent(st, ctx->scratch_done, 0);
+    }
+    ~ScratchOrder() {
+        if (!capturing) cudaEventRecord(ctx->scratch_done, st);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* sp_version(void) { return "spicier-gb300 0.1.0 sm_103a"; }
+
+int sp_backend_type(void) { return SP_BACKEND_GB300; }
+
+int sp_ctx_create(int device, sp_ctx** out) {
+    if (!out) return SP_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SP_ERR_NO_BACKEND;
+    if (device < 0 || device >= ndev) return SP_ERR_INVALID_ARGUMENT;
+    sp_ctx* ctx = new sp_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = prepare_exact_kernels(ctx->max_smem);
+    if (e == cudaSuccess) e = prepare_fast_kernels(ctx->max_smem);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return SP_ERR_BACKEND_INIT;
+    }
+    *out = ctx;
+    return SP_OK;
+}
+
+int sp_ctx_destroy(sp_ctx* ctx) {
+    if (!ctx) return SP_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaDeviceSynchronize();
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
+    for (auto& r : ctx->recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    delete ctx;
+    return SP_OK;
+}
+
+const char* sp_ctx_last_error(const sp_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int sp_should_use_gpu(const sp_ctx* ctx, size_t matrix_size, size_t batch_size) {
+    if (!ctx) return 0;
+    return matrix_size >= ctx->cfg.min_matrix_size && batch_size >= ctx->cfg.min_batch_size;
+}
+
+int sp_get_config(const sp_ctx* ctx, sp_batch_config* out) {
+    if (!ctx || !out) return SP_ERR_INVALID_ARGUMENT;
+    *out = ctx->cfg;
+    return SP_OK;
+}
+
+int sp_set_config(sp_ctx* ctx, const sp_batch_config* cfg) {
+    if (!ctx || !cfg) return SP_ERR_INVALID_ARGUMENT;
+    if (cfg->max_batch_per_launch == 0) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "max_batch_per_launch == 0");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->cfg = *cfg;
+    return SP_OK;
+}
+
+void sp_newton_config_default(sp_newton_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof *c);
+    c->v_abstol = 1e-6;
+    c->v_reltol = 1e-3;
+    c->i_abstol = 1e-12;
+    c->gmin = 1e-12;
+    c->max_iterations = 50;
+    c->precision = SP_PREC_FP64;
+    c->fallback = SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE;
+    c->refine_steps = 0;
+    c->gmin_initial = 1e-3;
+    c->gmin_final = 1e-12;
+    c->gmin_reduction = 10.0;
+    c->gmin_max_attempts = 5;
+    c->src_max_attempts = 5;
+    c->src_initial = 0.1;
+    c->src_step = 0.1;
+    c->src_min_step = 0.01;
+}
+
+// ---------------------------------------------------------------------------
+// solve_batch
+// ---------------------------------------------------------------------------
+static int solve_batch_device_locked(sp_ctx* ctx, const double* d_m, const double* d_r, size_t n,
+                                     size_t batch, double* d_x, uint8_t* d_s, int precision,
+                                     int refine_steps, cudaStream_t st) {
+    if (batch == 0) return SP_OK;
+    if (n == 0) return fail(ctx, SP_ERR_INVALID_DIMENSION, "Expected n > 0, got 0");
+    if (batch > ctx->cfg.max_batch_per_launch)
+        return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %zu exceeds maximum %llu", batch,
+                    (unsigned long long)ctx->cfg.max_batch_per_launch);
+    if (n > (size_t)kMaxDenseN)
+        return fail(ctx, SP_ERR_INVALID_DIMENSION, "n = %zu exceeds the batched dense LU limit %d", n,
+                    kMaxDenseN);
+    ProfScope prof(ctx, precision == SP_PREC_MIXED ? "lu_batch_mixed" : "lu_batch_fp64", st);
+    cudaError_t e = (precision == SP_PREC_MIXED)
+                        ? launch_lu_batch_mixed(d_m, d_r, (int)n, batch, d_x, d_s, refine_steps, st)
+                        : launch_lu_batch_exact(d_m, d_r, (int)n, batch, d_x, d_s, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "solve_batch launch");
+    return SP_OK;
+}
+
+int sp_solve_batch_device(sp_ctx* ctx, const double* d_matrices, const double* d_rhs, size_t n,
+                          size_t batch, double* d_solutions, uint8_t* d_singular_flags, int precision,
+                          int refine_steps, void* stream) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    if (batch && (!d_matrices || !d_rhs || !d_solutions || !d_singular_flags))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return solve_batch_device_locked(ctx, d_matrices, d_rhs, n, batch, d_solutions, d_singular_flags,
+                                     precision, refine_steps, (cudaStream_t)stream);
+}
+
+int sp_solve_batch(sp_ctx* ctx, const double* matrices, const double* rhs, size_t n, size_t batch,
+                   double* solutions, uint64_t* singular_indices, uint64_t* num_singular) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    if (num_singular) *num_singular = 0;
+    if (batch == 0) return SP_OK;
+    if (!matrices || !rhs || !solutions) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (n == 0) return fail(ctx, SP_ERR_INVALID_DIMENSION, "Expected n > 0, got 0");
+    size_t bm = align256(batch * n * n * 8), br = align256(batch * n * 8), bs = align256(batch);
+    int rc = ensure_scratch(ctx, bm + 2 * br + bs);
+    if (rc) return rc;
+    char* base = (char*)ctx->scratch;
+    double* d_m = (double*)base;
+    double* d_r = (double*)(base + bm);
+    double* d_x = (double*)(base + bm + br);
+    uint8_t* d_s = (uint8_t*)(base + bm + 2 * br);
+    cudaStream_t st = ctx->stream;
+    SP_CUDA(ctx, cudaMemcpyAsync(d_m, matrices, batch * n * n * 8, cudaMemcpyHostToDevice, st), "H2D matrices");
+    SP_CUDA(ctx, cudaMemcpyAsync(d_r, rhs, batch * n * 8, cudaMemcpyHostToDevice, st), "H2D rhs");
+    rc = solve_batch_device_locked(ctx, d_m, d_r, n, batch, d_x, d_s, SP_PREC_FP64, 0, st);
+    if (rc) return rc;
+    std::vector<uint8_t> flags(batch);
+    SP_CUDA(ctx, cudaMemcpyAsync(solutions, d_x, batch * n * 8, cudaMemcpyDeviceToHost, st), "D2H solutions");
+    SP_CUDA(ctx, cudaMemcpyAsync(flags.data(), d_s, batch, cudaMemcpyDeviceToHost, st), "D2H flags");
+    SP_CUDA(ctx, cudaStreamSynchronize(st), "solve_batch");
+    uint64_t ns = 0;
+    for (size_t i = 0; i < batch; ++i)
+        if (flags[i]) {
+            if (singular_indices) singular_indices[ns] = i;
+            ++ns;
+        }
+    if (num_singular) *num_singular = ns;
+    return SP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Topology
+// ---------------------------------------------------------------------------
+static int validate_circuit(sp_ctx* ctx, const sp_circuit* c) {
+    if (!c || c->num_nodes < 0 || c->num_branches < 0 || c->num_elements < 0 || c->num_params < 0 ||
+        c->num_pulses < 0)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad circuit header");
+    if (c->num_elements && !c->elements) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null elements");
+    if (c->num_params && !c->params) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null params");
+    const int nn = c->num_nodes;
+    for (int e = 0; e < c->num_elements; ++e) {
+        const sp_element& el = c->elements[e];
+        if (el.kind < SP_EL_R || el.kind > SP_EL_PNP)
+            return fail(ctx, SP_ERR_INVALID_ARGUMENT, "element %d: bad kind %d", e, el.kind);
+        int terms = (el.kind >= SP_EL_NMOS) ? 3 : 2;
+        for (int t = 0; t < terms; ++t)
+            if (el.node[t] < -1 || el.node[t] >= nn)
+                return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: node %d out of range", e, el.node[t]);
+        int nf = (el.kind == SP_EL_D) ? 2 : (el.kind >= SP_EL_NMOS ? 6 : 1);
+        for (int f = 0; f < nf; ++f)
+            if (el.field[f] < 0 || el.field[f] >= c->num_params)
+                return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: field slot %d out of range", e,
+                            el.field[f]);
+        bool needs_branch = el.kind == SP_EL_V || el.kind == SP_EL_L;
+        if (needs_branch && (el.branch < 0 || el.branch >= c->num_branches))
+            return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: branch %d out of range", e, el.branch);
+        if (el.wave >= c->num_pulses)
+            return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: pulse %d out of range", e, el.wave);
+    }
+    for (int k = 0; k < c->num_params; ++k)
+        if (c->params[k].kind < SP_DRAW_FIXED || c->params[k].kind > SP_DRAW_TABLE)
+            return fail(ctx, SP_ERR_INVALID_ARGUMENT, "param %d: bad draw kind", k);
+    return SP_OK;
+}
+
+int sp_topology_create(sp_ctx* ctx, const sp_circuit* c, sp_topology** out) {
+    if (!ctx || !out) return SP_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int rc = validate_circuit(ctx, c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    sp_topology* t = new sp_topology();
+    t->ctx = ctx;
+    t->num_nodes = c->num_nodes;
+    t->num_branches = c->num_branches;
+    t->n = c->num_nodes + c->num_branches;
+    t->num_elements = c->num_elements;
+    t->num_params = c->num_params;
+    t->num_pulses = c->num_pulses;
+    std::vector<int> doff(c->num_elements);
+    int nd = 0;
+    for (int e = 0; e < c->num_elements; ++e) {
+        doff[e] = nd;
+        nd += derived_count(c->elements[e].kind);
+    }
+    t->num_derived = nd;
+    for (int k = 0; k < c->num_params; ++k)
+        if (c->params[k].kind == SP_DRAW_TABLE) {
+            t->has_table = true;
+            t->min_table_cols = std::max(t->min_table_cols, c->params[k].rng_index + 1);
+        }
+    size_t be = align256(sizeof(sp_element) * c->num_elements);
+    size_t bp = align256(sizeof(sp_param) * c->num_params);
+    size_t bu = align256(sizeof(sp_pulse) * c->num_pulses);
+    size_t bo = align256(sizeof(int) * c->num_elements);
+    size_t bn = align256(sizeof(double) * t->n);
+    cudaError_t e = cudaMalloc(&t->dev, be + bp + bu + bo + bn + 256);
+    if (e != cudaSuccess) {
+        delete t;
+        return cuda_fail(ctx, e, "topology allocation");
+    }
+    char* b = (char*)t->dev;
+    sp_element* del = (sp_element*)b;
+    sp_param* dpar = (sp_param*)(b + be);
+    sp_pulse* dpul = (sp_pulse*)(b + be + bp);
+    int* ddoff = (int*)(b + be + bp + bu);
+    double* dns = (double*)(b + be + bp + bu + bo);
+    if (c->num_elements) e = cudaMemcpy(del, c->elements, sizeof(sp_element) * c->num_elements, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && c->num_params)
+        e = cudaMemcpy(dpar, c->params, sizeof(sp_param) * c->num_params, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && c->num_pulses)
+        e = cudaMemcpy(dpul, c->pulses, sizeof(sp_pulse) * c->num_pulses, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && c->num_elements)
+        e = cudaMemcpy(ddoff, doff.data(), sizeof(int) * c->num_elements, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && c->nodeset) e = cudaMemcpy(dns, c->nodeset, sizeof(double) * t->n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(t->dev);
+        delete t;
+        return cuda_fail(ctx, e, "topology upload");
+    }
+    t->dc = DevCircuit{c->num_nodes, c->num_branches, t->n, c->num_elements, c->num_params, nd,
+                       del, dpar, dpul, ddoff, c->nodeset ? dns : nullptr};
+    *out = t;
+    return SP_OK;
+}
+
+int sp_topology_destroy(sp_topology* t) {
+    if (!t) return SP_OK;
+    cudaSetDevice(t->ctx->device);
+    cudaDeviceSynchronize();
+    if (t->dev) cudaFree(t->dev);
+    delete t;
+    return SP_OK;
+}
+
+int sp_topology_size(const sp_topology* t) { return t ? t->n : 0; }
+
+// ---------------------------------------------------------------------------
+// Batched DC operating points
+// ---------------------------------------------------------------------------
+struct NewtonScratch {
+    double* params;
+    double* derived;
+    uint32_t* fail_list;
+    unsigned int* counters;  // [0] fail count, [1] undecided roundings
+    sp_moments* partial;
+    uint32_t moment_blocks;
+};
+
+static int newton_scratch(sp_ctx* ctx, const sp_topology* t, uint64_t count, NewtonScratch& s) {
+    size_t bp = align256(8 * (size_t)t->num_params * count);
+    size_t bd = align256(8 * (size_t)t->num_derived * count);
+    size_t bl = align256(4 * count);
+    size_t bc = 256;
+    uint32_t mb = (uint32_t)std::min<uint64_t>(256, std::max<uint64_t>(1, count / 1024));
+    size_t bm = align256(sizeof(sp_moments) * mb * (size_t)t->n);
+    int rc = ensure_scratch(ctx, bp + bd + bl + bc + bm);
+    if (rc) return rc;
+    char* b = (char*)ctx->scratch;
+    s.params = (double*)b;
+    s.derived = (double*)(b + bp);
+    s.fail_list = (uint32_t*)(b + bp + bd);
+    s.counters = (unsigned int*)(b + bp + bd + bl);
+    s.partial = (sp_moments*)(b + bp + bd + bl + bc);
+    s.moment_blocks = mb;
+    return SP_OK;
+}
+
+static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_config* cfg, uint64_t seed,
+                            uint64_t first_index, uint64_t count, const double* d_table, uint32_t table_cols,
+                            const double* d_x0, double* d_x, int32_t* d_iters, uint8_t* d_status,
+                            double* d_resid, double* d_params, sp_moments* d_moments, cudaStream_t st) {
+    if (count == 0) return SP_OK;
+    if (!d_x) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null output x");
+    if (count > ctx->cfg.max_batch_per_launch)
+        return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %llu exceeds maximum %llu",
+                    (unsigned long long)count, (unsigned long long)ctx->cfg.max_batch_per_launch);
+    if (count > 0xffffffffull) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "more than 2^32 samples per call");
+    if (first_index + count > 0x100000000ull)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "sweep index beyond u32 (rng.rs keys sweeps by u32)");
+    if (t->has_table && !d_table) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "circuit needs a parameter table");
+    if (t->has_table && table_cols < t->min_table_cols)
+        return fail(ctx, SP_ERR_INVALID_DIMENSION, "table has %u columns, circuit reads %u", table_cols,
+                    t->min_table_cols);
+    if (t->n == 0) return fail(ctx, SP_ERR_INVALID_DIMENSION, "empty circuit");
+    if (t->n > kMaxDenseN)
+        return fail(ctx, SP_ERR_INVALID_DIMENSION, "MNA size %d exceeds the dense Newton limit %d", t->n,
+                    kMaxDenseN);
+    const int prec = cfg->precision;
+    if (prec != SP_PREC_FP64 && prec != SP_PREC_MIXED && prec != SP_PREC_FP64_EXACT)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad precision %d", prec);
+    if (cfg->max_iterations <= 0) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "max_iterations <= 0");
+    NewtonScratch s;
+    int rc = newton_scratch(ctx, t, count, s);
+    if (rc) return rc;
+    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 8, st), "clear counters");
+    DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
+                 s.counters + 1};
+    {
+        ProfScope prof(ctx, "draw_params", st);
+        SP_CUDA(ctx, launch_draw(D, st), "draw launch");
+    }
+    NewtonLaunch L;
+    L.c = t->dc;
+    L.cfg = *cfg;
+    L.dv = SoA{s.derived, (size_t)count};
+    L.count = count;
+    L.x0 = d_x0;
+    L.x = d_x;
+    L.iters = d_iters;
+    L.status = d_status;
+    L.resid = d_resid;
+    L.fail_list = s.fail_list;
+    L.fail_count = s.counters;
+    const int kprec = prec == SP_PREC_MIXED ? SP_PREC_MIXED : SP_PREC_FP64;
+    size_t per = kprec == SP_PREC_MIXED ? work_bytes_per_thread<SP_PREC_MIXED>(t->n)
+                                        : work_bytes_per_thread<SP_PREC_FP64>(t->n);
+    int block = pick_block(per, ctx->max_smem);
+    if (!block) return fail(ctx, SP_ERR_INVALID_DIMENSION, "MNA size %d does not fit shared memory", t->n);
+    size_t smem = per * block;
+    int grid = (int)((count + block - 1) / block);
+    static const char* kname[3] = {"newton_primary_fp64", "newton_primary_mixed", "newton_primary_fp64_exact"};
+    static const char* fname[3] = {"newton_fallback_fp64", "newton_fallback_mixed", "newton_fallback_fp64_exact"};
+    cudaError_t e;
+    {
+        ProfScope prof(ctx, kname[prec], st);
+        e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, false, grid, block, smem, st)
+                                       : launch_newton_fast(kprec, L, false, grid, block, smem, st);
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "newton launch");
+    const bool any_fallback = d_x0 || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE));
+    if (any_fallback) {
+        int fgrid = std::min(grid, std::max(1, ctx->num_sms * 2));
+        ProfScope prof(ctx, fname[prec], st);
+        e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, true, fgrid, block, smem, st)
+                                       : launch_newton_fast(kprec, L, true, fgrid, block, smem, st);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback launch");
+    }
+    if (d_moments) {
+        ProfScope prof(ctx, "moments", st);
+        e = launch_moments(d_x, count, (uint32_t)t->n, (uint32_t)t->n, d_status, s.partial, s.moment_blocks,
+                           d_moments, st);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "moments launch");
+    }
+    return SP_OK;
+}
+
+int sp_newton_dc_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_config* cfg, uint64_t seed,
+                        uint64_t first_index, uint64_t num_samples, const double* d_table, uint32_t table_cols,
+                        const double* d_x0, double* d_x, int32_t* d_iters, uint8_t* d_status, double* d_resid,
+                        double* d_params, sp_moments* d_moments, void* stream) {
+    if (!ctx || !topo || !cfg) return SP_ERR_INVALID_ARGUMENT;
+    if (topo->ctx != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "topology belongs to another context");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    return newton_dc_locked(ctx, topo, cfg, seed, first_index, num_samples, d_table, table_cols, d_x0, d_x,
+                            d_iters, d_status, d_resid, d_params, d_moments, (cudaStream_t)stream);
+}
+
+int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* cfg, uint64_t seed,
+                 uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
+                 const double* x0, double* x, int32_t* iters, uint8_t* status, double* resid, double* params,
+                 sp_moments* moments) {
+    if (!ctx || !circuit || !cfg) return SP_ERR_INVALID_ARGUMENT;
+    if (count == 0) return SP_OK;
+    if (!x) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null output x");
+    sp_topology* t = nullptr;
+    int rc = sp_topology_create(ctx, circuit, &t);
+    if (rc) return rc;
+    struct Guard {
+        sp_topology* t;
+        ~Guard() { sp_topology_destroy(t); }
+    } guard{t};
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    const int n = t->n;
+    // The device buffers of this call sit after the Newton scratch; size both.
+    NewtonScratch ns;
+    rc = newton_scratch(ctx, t, count, ns);
+    if (rc) return rc;
+    size_t inner = (char*)ns.partial - (char*)ctx->scratch +
+                   align256(sizeof(sp_moments) * ns.moment_blocks * (size_t)n);
+    size_t bx = align256(8 * count * n), bi = align256(4 * count), bs = align256(count), br = align256(8 * count);
+    size_t bpar = align256(8 * count * (size_t)t->num_params), bm = align256(sizeof(sp_moments) * n);
+    size_t btab = table ? align256(8 * count * (size_t)table_cols) : 0;
+    size_t bx0 = x0 ? bx : 0;
+    rc = ensure_scratch(ctx, inner + bx + bi + bs + br + bpar + bm + btab + bx0);
+    if (rc) return rc;
+    rc = newton_scratch(ctx, t, count, ns);  // pointers may have moved
+    if (rc) return rc;
+    char* b = (char*)ctx->scratch + inner;
+    double* d_x = (double*)b;
+    int32_t* d_it = (int32_t*)(b + bx);
+    uint8_t* d_st = (uint8_t*)(b + bx + bi);
+    double* d_res = (double*)(b + bx + bi + bs);
+    double* d_par = (double*)(b + bx + bi + bs + br);
+    sp_moments* d_mom = (sp_moments*)(b + bx + bi + bs + br + bpar);
+    double* d_tab = table ? (double*)(b + bx + bi + bs + br + bpar + bm) : nullptr;
+    double* d_x0 = x0 ? (double*)(b + bx + bi + bs + br + bpar + bm + btab) : nullptr;
+    cudaStream_t st = ctx->stream;
+    if (table) SP_CUDA(ctx, cudaMemcpyAsync(d_tab, table, 8 * count * table_cols, cudaMemcpyHostToDevice, st), "H2D table");
+    if (x0) SP_CUDA(ctx, cudaMemcpyAsync(d_x0, x0, 8 * count * n, cudaMemcpyHostToDevice, st), "H2D x0");
+    rc = newton_dc_locked(ctx, t, cfg, seed, first_index, count, d_tab, table_cols, d_x0, d_x, d_it, d_st,
+                          resid ? d_res : nullptr, params ? d_par : nullptr, moments ? d_mom : nullptr, st);
+    if (rc) return rc;
+    SP_CUDA(ctx, cudaMemcpyAsync(x, d_x, 8 * count * n, cudaMemcpyDeviceToHost, st), "D2H x");
+    if (iters) SP_CUDA(ctx, cudaMemcpyAsync(iters, d_it, 4 * count, cudaMemcpyDeviceToHost, st), "D2H iters");
+    if (status) SP_CUDA(ctx, cudaMemcpyAsync(status, d_st, count, cudaMemcpyDeviceToHost, st), "D2H status");
+    if (resid) SP_CUDA(ctx, cudaMemcpyAsync(resid, d_res, 8 * count, cudaMemcpyDeviceToHost, st), "D2H resid");
+    if (params)
+        SP_CUDA(ctx, cudaMemcpyAsync(params, d_par, 8 * count * t->num_params, cudaMemcpyDeviceToHost, st),
+                "D2H params");
+    if (moments) SP_CUDA(ctx, cudaMemcpyAsync(moments, d_mom, sizeof(sp_moments) * n, cudaMemcpyDeviceToHost, st),
+                         "D2H moments");
+    SP_CUDA(ctx, cudaStreamSynchronize(st), "newton_dc");
+    return SP_OK;
+}
+
+int sp_draw_params_device(sp_ctx* ctx, const sp_topology* t, uint64_t seed, uint64_t first_index,
+                          uint64_t num_samples, const double* d_table, uint32_t table_cols, double* d_params,
+                          void* stream) {
+    if (!ctx || !t || !d_params) return SP_ERR_INVALID_ARGUMENT;
+    if (t->has_table && !d_table) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "circuit needs a parameter table");
+    if (t->has_table && table_cols < t->min_table_cols)
+        return fail(ctx, SP_ERR_INVALID_DIMENSION, "table has %u columns, circuit reads %u", table_cols,
+                    t->min_table_cols);
+    if (num_samples == 0) return SP_OK;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    NewtonScratch s;
+    int rc = newton_scratch(ctx, t, num_samples, s);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    ScratchOrder order(ctx, st);
+    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 8, st), "clear counters");
+    DrawLaunch D{t->dc, seed, first_index, num_samples, d_table, table_cols, s.params, s.derived, d_params,
+                 s.counters + 1};
+    SP_CUDA(ctx, launch_draw(D, st), "draw launch");
+    return SP_OK;
+}
+
+int sp_rng_fill_device(sp_ctx* ctx, int kind, uint64_t seed, uint64_t first_index, uint32_t param_index,
+                       uint64_t count, double* d_out, void* stream) {
+    if (!ctx || !d_out) return SP_ERR_INVALID_ARGUMENT;
+    if (kind < 0 || kind > 3) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad rng kind %d", kind);
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ProfScope prof(ctx, "rng_fill", (cudaStream_t)stream);
+    SP_CUDA(ctx, launch_rng_fill(kind, seed, first_index, param_index, count, d_out, (cudaStream_t)stream),
+            "rng launch");
+    return SP_OK;
+}
+
+int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld, uint32_t cols,
+                      const uint8_t* d_status, sp_moments* d_out, void* stream) {
+    if (!ctx || !d_values || !d_out) return SP_ERR_INVALID_ARGUMENT;
+    if (cols > ld) return fail(ctx, SP_ERR_INVALID_DIMENSION, "cols > ld");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    uint32_t mb = (uint32_t)std::min<uint64_t>(256, std::max<uint64_t>(1, rows / 1024));
+    int rc = ensure_scratch(ctx, align256(sizeof(sp_moments) * mb * (size_t)cols));
+    if (rc) return rc;
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    SP_CUDA(ctx, launch_moments(d_values, rows, ld, cols, d_status, (sp_moments*)ctx->scratch, mb, d_out,
+                                (cudaStream_t)stream),
+            "moments launch");
+    return SP_OK;
+}
+
+int sp_profile_enable(sp_ctx* ctx, int on) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->profiling = on != 0;
+    return SP_OK;
+}
+
+int sp_profile_read(sp_ctx* ctx, sp_kernel_time* out, int cap, int* count) {
+    if (!ctx || !count || (cap > 0 && !out)) return SP_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    int k = 0;
+    for (auto& r : ctx->recs) {
+        cudaError_t e = cudaEventSynchronize(r.b);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "profile synchronise");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        int j = 0;
+        while (j < k && std::strncmp(out[j].name, r.name, sizeof out[j].name) != 0) ++j;
+        if (j == k) {
+            if (k >= cap) continue;
+            std::memset(&out[k], 0, sizeof out[k]);
+            std::strncpy(out[k].name, r.name, sizeof out[k].name - 1);
+            ++k;
+        }
+        out[j].launches += 1;
+        out[j].total_ms += ms;
+    }
+    for (auto& r : ctx->recs) {
+        ctx->event_pool.push_back(r.a);
+        ctx->event_pool.push_back(r.b);
+    }
+    ctx->recs.clear();
+    *count = k;
+    return SP_OK;
+}
+
+}  // extern "C"

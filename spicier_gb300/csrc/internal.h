@@ -1,0 +1,119 @@
+// Internal launchers shared by the translation units of libspicier_gb300.
+//
+// Kernels whose results must reproduce the reference's IEEE operation
+// sequence live in kernels_exact.cu, compiled with --fmad=false; kernels
+// free to contract a*b+c into FMA live in kernels_fast.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/spicier_gb300.h"
+#include "newton_dense.cuh"
+
+namespace sp {
+
+struct DrawLaunch {
+    DevCircuit c;
+    uint64_t seed;
+    uint64_t first_index;
+    uint64_t count;
+    const double* table;  // [count][table_cols] or nullptr
+    uint32_t table_cols;
+    double* params_soa;   // [num_params][count]
+    double* derived_soa;  // [num_derived][count]
+    double* params_out;   // [count][num_params] or nullptr
+    unsigned int* hard;   // count of draws whose rounding was undecided (or nullptr)
+};
+
+// kernels_exact.cu (no FMA contraction)
+cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st);
+cudaError_t launch_newton_exact(const NewtonLaunch& L, bool fallback, int grid, int block, size_t smem,
+                                cudaStream_t st);
+cudaError_t launch_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t param, uint64_t count,
+                            double* out, cudaStream_t st);
+cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, uint64_t batch,
+                                  double* sol, uint8_t* sing, cudaStream_t st);
+cudaError_t prepare_exact_kernels(int max_smem);
+
+// kernels_fast.cu (FMA allowed)
+cudaError_t launch_newton_fast(int prec, const NewtonLaunch& L, bool fallback, int grid, int block,
+                               size_t smem, cudaStream_t st);
+cudaError_t launch_lu_batch_mixed(const double* mats, const double* rhs, int n, uint64_t batch,
+                                  double* sol, uint8_t* sing, int refine_steps, cudaStream_t st);
+cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
+                           const uint8_t* status, sp_moments* partial, uint32_t nblocks,
+                           sp_moments* out, cudaStream_t st);
+cudaError_t prepare_fast_kernels(int max_smem);
+
+// Largest dense size of the thread-per-sample Newton kernels.
+constexpr int kMaxDenseN = 28;
+
+}  // namespace sp
+
+// The context: one per device per caller; a mutex serialises host calls.
+struct sp_ctx {
+    int device = 0;
+    sp_batch_config cfg{16, 1, 1ull << 26};
+    std::string last_error;
+    std::mutex mu;
+    cudaStream_t stream = nullptr;  // used by the host-buffer entry points
+    cudaEvent_t scratch_done = nullptr;  // last enqueued user of the scratch
+    int max_smem = 0;
+    int num_sms = 0;
+    // grow-only device scratch of the host-buffer entry points and of the
+    // Newton launches (parameters, derived constants, fallback list)
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    // kernel timing records (sp_profile_enable)
+    bool profiling = false;
+    struct Rec {
+        const char* name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> event_pool;
+};
+
+// Brackets one kernel launch with events when the context is profiling.
+struct ProfScope {
+    sp_ctx* ctx;
+    cudaStream_t st;
+    sp_ctx::Rec rec{};
+    ProfScope(sp_ctx* c, const char* name, cudaStream_t s) : ctx(c), st(s) {
+        if (!ctx->profiling) return;
+        rec.name = name;
+        rec.a = take();
+        rec.b = take();
+        cudaEventRecord(rec.a, st);
+    }
+    ~ProfScope() {
+        if (!ctx->profiling || !rec.a) return;
+        cudaEventRecord(rec.b, st);
+        ctx->recs.push_back(rec);
+    }
+    cudaEvent_t take() {
+        if (!ctx->event_pool.empty()) {
+            cudaEvent_t e = ctx->event_pool.back();
+            ctx->event_pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+};
+
+struct sp_topology {
+    sp_ctx* ctx = nullptr;
+    int n = 0;
+    int num_nodes = 0, num_branches = 0, num_elements = 0, num_params = 0, num_derived = 0;
+    int num_pulses = 0;
+    bool has_table = false;
+    uint32_t min_table_cols = 0;  // 1 + largest table column any parameter reads
+    void* dev = nullptr;  // one allocation: elements, params, pulses, doff, nodeset
+    sp::DevCircuit dc{};
+};

@@ -1,0 +1,165 @@
+// Kernels that reproduce the reference's IEEE operation sequence.
+// Compiled with --fmad=false: no a*b+c is fused, as in the Rust reference.
+#define SP_KERNEL_NS kexact
+#include "internal.h"
+#include <math_constants.h>
+
+#include "rng.cuh"
+
+namespace sp {
+
+// Per-sample parameter draw (sp_draw_kind) and derived constants.
+// gaussian_scaled = mean + z * sigma (rng.rs:148-150), two roundings.
+__device__ inline double draw_one(const sp_param& p, uint64_t seed, uint32_t sweep,
+                                  const double* row, unsigned* hard) {
+    switch (p.kind) {
+        case SP_DRAW_FIXED: return p.a;
+        case SP_DRAW_GAUSS: return p.a + rng_gaussian(seed, sweep, p.rng_index, hard) * p.b;
+        case SP_DRAW_UNIFORM: return p.a + rng_uniform(seed, sweep, p.rng_index) * (p.b - p.a);
+        case SP_DRAW_LOGUNIFORM:
+            return p.a * exp(rng_uniform(seed, sweep, p.rng_index) * log(p.b / p.a));
+        case SP_DRAW_TABLE: return row ? row[p.rng_index] : CUDART_NAN;
+    }
+    return CUDART_NAN;
+}
+
+__global__ void draw_kernel(DrawLaunch L) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.count) return;
+    const DevCircuit& c = L.c;
+    const uint32_t sweep = (uint32_t)(L.first_index + s);
+    const double* row = L.table ? L.table + s * L.table_cols : nullptr;
+    unsigned hard = 0;
+    for (int k = 0; k < c.num_params; ++k) {
+        double v = draw_one(c.par[k], L.seed, sweep, row, &hard);
+        L.params_soa[(size_t)k * L.count + s] = v;
+        if (L.params_out) L.params_out[s * c.num_params + k] = v;
+    }
+    if (hard && L.hard) atomicAdd(L.hard, hard);
+    auto P = [&](int slot) { return L.params_soa[(size_t)slot * L.count + s]; };
+    const double vt = thermal_voltage_300();
+    for (int e = 0; e < c.num_elements; ++e) {
+        const sp_element el = c.el[e];
+        double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
+        const size_t st = L.count;
+        switch (el.kind) {
+            case SP_EL_R: out[0] = 1.0 / P(el.field[0]); break;  // passive.rs:48-50
+            case SP_EL_D: {
+                double nvt = P(el.field[1]) * vt;
+                out[0] = P(el.field[0]);
+                out[st] = nvt;
+                out[2 * st] = diode_vcrit(nvt);
+                break;
+            }
+            case SP_EL_NMOS:
+            case SP_EL_PMOS: {
+                // vth = |VTO| (level1.rs:164); beta = kp * nf * w / l (level1.rs:68-70)
+                double kp = P(el.field[1]), w = P(el.field[3]), l = P(el.field[4]), nf = P(el.field[5]);
+                out[0] = fabs(P(el.field[0]));
+                out[st] = kp * nf * w / l;
+                out[2 * st] = P(el.field[2]);
+                break;
+            }
+            case SP_EL_NPN:
+            case SP_EL_PNP: {
+                double nf_vt = P(el.field[3]) * vt, nr_vt = P(el.field[4]) * vt;
+                out[0] = P(el.field[0]);
+                out[st] = P(el.field[1]);
+                out[2 * st] = P(el.field[2]);
+                out[3 * st] = nf_vt;
+                out[4 * st] = nr_vt;
+                out[5 * st] = P(el.field[5]);
+                out[6 * st] = diode_vcrit(nf_vt);
+                out[7 * st] = diode_vcrit(nr_vt);
+                break;
+            }
+            default: out[0] = P(el.field[0]); break;  // C, L, V, I
+        }
+    }
+}
+
+cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st) {
+    if (L.count == 0) return cudaSuccess;
+    const int block = 128;
+    const uint64_t grid = (L.count + block - 1) / block;
+    draw_kernel<<<(unsigned)grid, block, 0, st>>>(L);
+    return cudaGetLastError();
+}
+
+__global__ void rng_fill_kernel(int kind, uint64_t seed, uint64_t first, uint32_t param, uint64_t count,
+                                double* out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t s = (uint32_t)(first + i);
+    unsigned hard = 0;
+    switch (kind) {
+        case 0: out[i] = rng_uniform(seed, s, param); break;
+        case 1: out[i] = rng_gaussian(seed, s, param, &hard); break;
+        case 2: out[i] = (double)rng_uniform_f32(seed, s, param); break;
+        default: out[i] = (double)rng_gaussian_f32(seed, s, param); break;
+    }
+}
+
+cudaError_t launch_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t param, uint64_t count,
+                            double* out, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    const int block = 256;
+    rng_fill_kernel<<<(unsigned)((count + block - 1) / block), block, 0, st>>>(kind, seed, first, param,
+                                                                              count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_newton_exact(const NewtonLaunch& L, bool fallback, int grid, int block, size_t smem,
+                                cudaStream_t st) {
+    if (fallback)
+        SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
+    else
+        SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
+    return cudaGetLastError();
+}
+
+// BatchedLuSolver::solve_batch in FP64 with the reference's LU
+// (CpuBatchedSolver, solver.rs:326-384): one thread per system, column-major
+// input copied into interleaved shared memory; singular -> zero solution.
+__global__ void lu_batch_fp64_kernel(const double* __restrict__ mats, const double* __restrict__ rhs,
+                                     int n, uint64_t batch, double* __restrict__ sol,
+                                     uint8_t* __restrict__ sing) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= batch) return;
+    double* base = reinterpret_cast<double*>(smem);
+    Il<double> A{base + threadIdx.x, (int)blockDim.x};
+    Il<double> b{base + (size_t)n * n * blockDim.x + threadIdx.x, (int)blockDim.x};
+    const double* m = mats + s * n * n;
+    for (int i = 0; i < n * n; ++i) A[i] = m[i];
+    for (int i = 0; i < n; ++i) b[i] = rhs[s * n + i];
+    bool ok = lu_solve_fp64(n, A, b);
+    for (int i = 0; i < n; ++i) sol[s * n + i] = ok ? b[i] : 0.0;
+    sing[s] = ok ? 0 : 1;
+}
+
+cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, uint64_t batch,
+                                  double* sol, uint8_t* sing, cudaStream_t st) {
+    if (batch == 0) return cudaSuccess;
+    size_t per = (size_t)(n * n + n) * 8;
+    int block = 128;
+    while (block > 32 && per * block > 110 * 1024) block -= 32;
+    size_t smem = per * block;
+    lu_batch_fp64_kernel<<<(unsigned)((batch + block - 1) / block), block, smem, st>>>(mats, rhs, n, batch,
+                                                                                     sol, sing);
+    return cudaGetLastError();
+}
+
+cudaError_t prepare_exact_kernels(int max_smem) {
+    cudaError_t e;
+    e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(lu_batch_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                max_smem);
+}
+
+}  // namespace sp

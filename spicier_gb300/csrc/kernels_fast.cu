@@ -1,0 +1,245 @@
+// Kernels free to use FMA: the mixed-precision Newton path, the FMA build
+// of the FP64 Newton path (the fastest plain-FP64 form), the mixed-precision
+// batched LU and the statistics reductions.
+#include <math_constants.h>
+
+#include <cfloat>
+
+#define SP_KERNEL_NS kfast
+#include "internal.h"
+
+namespace sp {
+
+cudaError_t launch_newton_fast(int prec, const NewtonLaunch& L, bool fallback, int grid, int block,
+                               size_t smem, cudaStream_t st) {
+    if (prec == SP_PREC_MIXED) {
+        if (fallback)
+            SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_MIXED><<<grid, block, smem, st>>>(L);
+        else
+            SP_KERNEL_NS::newton_primary_kernel<SP_PREC_MIXED><<<grid, block, smem, st>>>(L);
+    } else {
+        if (fallback)
+            SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
+        else
+            SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
+    }
+    return cudaGetLastError();
+}
+
+// Mixed-precision BatchedLuSolver::solve_batch: FP32 partial-pivot LU in
+// shared memory, then refine_steps sweeps of FP64 iterative refinement
+// (r = b - A x from the FP64 matrix in HBM, d = LU32 \ r, x += d).  A system
+// whose final FP64 residual is not at FP64 level (||r|| > 64 eps ||A|| ||x||)
+// is refactorised in FP64 with the reference's algorithm.
+__global__ void lu_batch_mixed_kernel(const double* __restrict__ mats, const double* __restrict__ rhs,
+                                      int n, uint64_t batch, double* __restrict__ sol,
+                                      uint8_t* __restrict__ sing, int refine_steps) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= batch) return;
+    const int bs = blockDim.x;
+    double* dbase = reinterpret_cast<double*>(smem);
+    Il<double> x{dbase + threadIdx.x, bs};
+    Il<double> r{dbase + (size_t)n * bs + threadIdx.x, bs};
+    float* fbase = reinterpret_cast<float*>(dbase + (size_t)2 * n * bs);
+    Il<float> A{fbase + threadIdx.x, bs};
+    Il<float> d{fbase + (size_t)n * n * bs + threadIdx.x, bs};
+    int* ibase = reinterpret_cast<int*>(fbase + (size_t)(n * n + n) * bs);
+    Il<int> perm{ibase + threadIdx.x, bs};
+    const double* M = mats + s * n * n;
+    const double* b = rhs + s * n;
+    double anorm = 0.0;
+    for (int i = 0; i < n * n; ++i) {
+        double v = M[i];
+        A[i] = (float)v;
+        anorm = fmax(anorm, fabs(v));
+    }
+    bool ok = true;
+    for (int i = 0; i < n && ok; ++i) {
+        int piv = i;
+        float best = fabsf(A[i * n + i]);
+        for (int q = i + 1; q < n; ++q) {
+            float v = fabsf(A[i * n + q]);
+            if (v > best) {
+                best = v;
+                piv = q;
+            }
+        }
+        perm[i] = piv;
+        float diag = A[i * n + piv];
+        if (diag == 0.0f) {
+            ok = false;
+            break;
+        }
+        if (piv != i)
+            for (int c = 0; c < n; ++c) {
+                float t = A[c * n + i];
+                A[c * n + i] = A[c * n + piv];
+                A[c * n + piv] = t;
+            }
+        float inv = 1.0f / diag;
+        for (int q = i + 1; q < n; ++q) A[i * n + q] *= inv;
+        for (int c = i + 1; c < n; ++c) {
+            float p = A[c * n + i];
+            for (int q = i + 1; q < n; ++q) A[c * n + q] = fmaf(-p, A[i * n + q], A[c * n + q]);
+        }
+    }
+    double xnorm = 0.0, rnorm = 0.0;
+    if (ok) {
+        for (int i = 0; i < n; ++i) {
+            x[i] = 0.0;
+            r[i] = b[i];
+        }
+        for (int sweep = 0; sweep <= refine_steps; ++sweep) {
+            for (int i = 0; i < n; ++i) d[i] = (float)r[i];
+            for (int i = 0; i < n; ++i) {
+                int p = perm[i];
+                if (p != i) {
+                    float t = d[i];
+                    d[i] = d[p];
+                    d[p] = t;
+                }
+            }
+            for (int i = 0; i < n; ++i) {
+                float cf = d[i];
+                for (int q = i + 1; q < n; ++q) d[q] = fmaf(-cf, A[i * n + q], d[q]);
+            }
+            for (int i = n - 1; i >= 0; --i) {
+                float cf = d[i] / A[i * n + i];
+                d[i] = cf;
+                for (int q = 0; q < i; ++q) d[q] = fmaf(-cf, A[i * n + q], d[q]);
+            }
+            xnorm = 0.0;
+            for (int i = 0; i < n; ++i) {
+                x[i] = x[i] + (double)d[i];
+                xnorm = fmax(xnorm, fabs(x[i]));
+            }
+            for (int i = 0; i < n; ++i) r[i] = b[i];
+            for (int c = 0; c < n; ++c) {
+                double xc = x[c];
+                for (int q = 0; q < n; ++q) r[q] = fma(-M[c * n + q], xc, r[q]);
+            }
+            rnorm = 0.0;
+            for (int i = 0; i < n; ++i) rnorm = fmax(rnorm, fabs(r[i]));
+        }
+        if (!(rnorm <= 64.0 * DBL_EPSILON * anorm * xnorm * n) || !isfinite(rnorm)) ok = false;
+    }
+    if (!ok) {
+        // FP32 pivot breakdown or refinement short of FP64 accuracy: mark the
+        // system for lu_batch_escalate_kernel (FP64 factorisation).
+        sing[s] = 2;
+        return;
+    }
+    for (int i = 0; i < n; ++i) sol[s * n + i] = x[i];
+    sing[s] = 0;
+}
+
+// Re-solve the systems flagged 2 by the mixed kernel in FP64.
+__global__ void lu_batch_escalate_kernel(const double* __restrict__ mats, const double* __restrict__ rhs,
+                                         int n, uint64_t batch, double* __restrict__ sol,
+                                         uint8_t* __restrict__ sing) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= batch) return;
+    if (sing[s] != 2) return;
+    double* base = reinterpret_cast<double*>(smem);
+    Il<double> A{base + threadIdx.x, (int)blockDim.x};
+    Il<double> b{base + (size_t)n * n * blockDim.x + threadIdx.x, (int)blockDim.x};
+    for (int i = 0; i < n * n; ++i) A[i] = mats[s * n * n + i];
+    for (int i = 0; i < n; ++i) b[i] = rhs[s * n + i];
+    bool ok = lu_solve_fp64(n, A, b);
+    for (int i = 0; i < n; ++i) sol[s * n + i] = ok ? b[i] : 0.0;
+    sing[s] = ok ? 0 : 1;
+}
+
+cudaError_t launch_lu_batch_mixed(const double* mats, const double* rhs, int n, uint64_t batch,
+                                  double* sol, uint8_t* sing, int refine_steps, cudaStream_t st) {
+    if (batch == 0) return cudaSuccess;
+    size_t per = (size_t)2 * n * 8 + (size_t)(n * n + n) * 4 + (size_t)n * 4;
+    int block = 128;
+    while (block > 32 && per * block > 110 * 1024) block -= 32;
+    lu_batch_mixed_kernel<<<(unsigned)((batch + block - 1) / block), block, per * block, st>>>(
+        mats, rhs, n, batch, sol, sing, refine_steps);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    size_t per64 = (size_t)(n * n + n) * 8;
+    int b64 = 128;
+    while (b64 > 32 && per64 * b64 > 110 * 1024) b64 -= 32;
+    lu_batch_escalate_kernel<<<(unsigned)((batch + b64 - 1) / b64), b64, per64 * b64, st>>>(mats, rhs, n,
+                                                                                          batch, sol, sing);
+    return cudaGetLastError();
+}
+
+// Moments of `cols` columns over rows (StatisticsAccumulator::add/merge,
+// statistics.rs:127-155).  Pass 1: each block reduces a contiguous row range
+// per column in a fixed tree order; pass 2: one block merges the partials in
+// block order.  The order is fixed, so reruns are bit-identical.
+__device__ inline void mom_merge(sp_moments& a, const sp_moments& b) {
+    a.count += b.count;
+    a.sum += b.sum;
+    a.sum_sq += b.sum_sq;
+    a.min = fmin(a.min, b.min);
+    a.max = fmax(a.max, b.max);
+}
+
+__global__ void moments_partial_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
+                                       uint32_t cols, const uint8_t* __restrict__ status,
+                                       sp_moments* __restrict__ partial) {
+    __shared__ sp_moments sh[256];
+    const uint32_t col = blockIdx.y;
+    const uint64_t per_block = (rows + gridDim.x - 1) / gridDim.x;
+    const uint64_t lo = (uint64_t)blockIdx.x * per_block;
+    const uint64_t hi = min(rows, lo + per_block);
+    sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+        double x = v[i * ld + col];
+        m.count += 1;
+        m.sum += x;
+        m.sum_sq += x * x;
+        m.min = fmin(m.min, x);
+        m.max = fmax(m.max, x);
+    }
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[(size_t)col * gridDim.x + blockIdx.x] = sh[0];
+}
+
+__global__ void moments_final_kernel(const sp_moments* __restrict__ partial, uint32_t nblocks,
+                                     uint32_t cols, sp_moments* __restrict__ out) {
+    const uint32_t col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= cols) return;
+    sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+    for (uint32_t b = 0; b < nblocks; ++b) mom_merge(m, partial[(size_t)col * nblocks + b]);
+    out[col] = m;
+}
+
+cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
+                           const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
+                           cudaStream_t st) {
+    if (cols == 0) return cudaSuccess;
+    dim3 grid(nblocks, cols);
+    moments_partial_kernel<<<grid, 256, 0, st>>>(values, rows, ld, cols, status, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    moments_final_kernel<<<(cols + 127) / 128, 128, 0, st>>>(partial, nblocks, cols, out);
+    return cudaGetLastError();
+}
+
+cudaError_t prepare_fast_kernels(int max_smem) {
+    const void* fns[] = {
+        (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_MIXED>,
+        (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
+        (const void*)lu_batch_mixed_kernel, (const void*)lu_batch_escalate_kernel};
+    for (const void* f : fns) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace sp
