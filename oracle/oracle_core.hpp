@@ -570,6 +570,9 @@ inline bool all_finite(const double* x, int n) {
 // zero); on a miss, Newton from zero when a guess was used; then gmin
 // stepping, then source stepping, as enabled by cfg.fallback.  Returns the
 // sp_sample_status byte; *iters is the total Newton iteration count.
+// A stage succeeds only if it converged with a finite iterate: the
+// reference's check_convergence passes a NaN iterate (every comparison with
+// NaN is false), which would otherwise end the chain on a NaN "solution".
 inline uint8_t dc_pipeline(const sp_circuit& c, const double* P, const sp_newton_config& cfg,
                            const double* x0, double* x, int* iters, Mna& m) {
     int n = c.num_nodes + c.num_branches;
@@ -590,28 +593,28 @@ inline uint8_t dc_pipeline(const sp_circuit& c, const double* P, const sp_newton
     NrOutcome r = newton(c, P, cfg, StampMode::Plain, 0.0, x, m);
     total += r.iterations;
     last_singular = r.singular;
-    bool ok = r.converged;
+    bool ok = r.converged && all_finite(x, n);
     if (!ok && x0) {
         flags |= SP_ST_FLAG_COLD;
         cold_start();
         r = newton(c, P, cfg, StampMode::Plain, 0.0, x, m);
         total += r.iterations;
         last_singular = r.singular;
-        ok = r.converged;
+        ok = r.converged && all_finite(x, n);
     }
     if (!ok && (cfg.fallback & SP_FALLBACK_GMIN)) {
         flags |= SP_ST_FLAG_GMIN;
         SteppingOutcome s = gmin_stepping(c, P, cfg, x, m);
         total += s.total_iterations;
         last_singular = s.singular;
-        ok = s.converged;
+        ok = s.converged && all_finite(x, n);
     }
     if (!ok && (cfg.fallback & SP_FALLBACK_SOURCE)) {
         flags |= SP_ST_FLAG_SOURCE;
         SteppingOutcome s = source_stepping(c, P, cfg, x, m);
         total += s.total_iterations;
         last_singular = s.singular;
-        ok = s.converged;
+        ok = s.converged && all_finite(x, n);
     }
     *iters = total;
     uint8_t st;

@@ -419,6 +419,14 @@ __global__ void newton_fallback_kernel(NewtonLaunch L) {
         const size_t s = L.fail_list[j];
         int total = L.iters ? L.iters[s] : 0;
         uint8_t flags = warm ? SP_ST_FLAG_WARM : 0;
+        // A stage succeeds only if it converged with a finite iterate (the
+        // reference's convergence test passes NaN iterates).
+        auto ok = [&](int code) {
+            if (code != NR_CONVERGED) return false;
+            for (int i = 0; i < n; ++i)
+                if (!isfinite(L.x[s * n + i])) return false;
+            return true;
+        };
         int code = NR_MAXITER;
         if (warm) {
             flags |= SP_ST_FLAG_COLD;
@@ -428,11 +436,11 @@ __global__ void newton_fallback_kernel(NewtonLaunch L) {
             total += it;
             for (int i = 0; i < n; ++i) L.x[s * n + i] = w.x[i];
         }
-        if (code != NR_CONVERGED && (L.cfg.fallback & SP_FALLBACK_GMIN)) {
+        if (!ok(code) && (L.cfg.fallback & SP_FALLBACK_GMIN)) {
             flags |= SP_ST_FLAG_GMIN;
             code = gmin_stepping<PREC>(L, s, w, total);
         }
-        if (code != NR_CONVERGED && (L.cfg.fallback & SP_FALLBACK_SOURCE)) {
+        if (!ok(code) && (L.cfg.fallback & SP_FALLBACK_SOURCE)) {
             flags |= SP_ST_FLAG_SOURCE;
             code = source_stepping<PREC>(L, s, w, total);
         }
