@@ -29,6 +29,12 @@ def tabled(circuit: Circuit, params: np.ndarray) -> Circuit:
     return c
 
 
+def same_bits(a, b):
+    """Bitwise equality, NaN == NaN (payload bits of a NaN are not portable)."""
+    eq = a.view(np.uint64) == b.view(np.uint64)
+    return bool(np.all(eq | (np.isnan(a) & np.isnan(b))))
+
+
 def spice_close(x, ref, num_nodes, reltol=1e-3, vntol=1e-6, abstol=1e-12):
     tol = np.empty_like(ref)
     tol[:, :num_nodes] = reltol * np.abs(ref[:, :num_nodes]) + vntol
@@ -56,7 +62,7 @@ def test_exact_mode_bitwise_with_shared_params(ctx, name, make, N):
     xo, io, so, _ = oracle.newton_dc(circ, abi.newton_config(), seed=1, count=N, table=P)
     assert np.array_equal(r.status, so)
     assert np.array_equal(r.iters, io)
-    assert np.array_equal(r.x.view(np.uint64), xo.view(np.uint64)), "FP64_EXACT must be bit-identical"
+    assert same_bits(r.x, xo), "FP64_EXACT must be bit-identical"
 
 
 @pytest.mark.parametrize("prec", [FAST, EXACT])
@@ -139,7 +145,7 @@ def test_warm_start_and_cold_fallback(ctx):
     r2 = ctx.newton_dc(tc, abi.newton_config(precision=EXACT), seed=2, count=N, x0=bad, table=P)
     xo2, io2, so2, _ = oracle.newton_dc(tc, abi.newton_config(), seed=2, count=N, x0=bad, table=P)
     assert np.array_equal(r2.status, so2) and np.array_equal(r2.iters, io2)
-    assert np.array_equal(r2.x.view(np.uint64), xo2.view(np.uint64))
+    assert same_bits(r2.x, xo2)
     assert (r2.status & abi.SP_ST_FLAG_WARM).all()
 
 

@@ -32,13 +32,15 @@ def test_uniform_bit_exact(ctx, seed, param):
     assert np.array_equal(g.view(np.uint64), c.view(np.uint64))
 
 
-def test_gaussian_within_two_ulp(ctx):
+def test_gaussian_close_to_host_libm(ctx):
+    # sqrt(-2 ln u1) * cos(2 pi u2): an ulp of ln or cos is an absolute error
+    # on the scale of the radius, so compare against the radius' spacing.
     n = 1 << 20
     g = rng_gpu(ctx, 1, 1, 0, 3, n)
     c = rng_cpu(1, 1, 0, 3, n)
-    ulp = np.abs(g.view(np.int64) - c.view(np.int64))
-    assert ulp.max() <= 2
-    assert np.mean(ulp == 0) > 0.99
+    scale = np.spacing(np.maximum(np.abs(c), 1.0))
+    assert np.all(np.abs(g - c) <= 8 * scale)
+    assert np.mean(g == c) > 0.99
 
 
 def test_f32_variants(ctx):
@@ -87,7 +89,8 @@ def test_solve_batch_mixed_refined(ctx):
     assert f[7] == 1 and np.all(x[7] == 0.0) and f.sum() == 1
     ok = np.arange(batch) != 7
     ref = np.linalg.solve(A[ok], b[ok][..., None])[..., 0]
-    assert np.max(np.abs(x[ok] - ref) / (np.abs(ref) + 1e-12)) < 1e-12
+    normwise = np.max(np.abs(x[ok] - ref), axis=1) / np.max(np.abs(ref), axis=1)
+    assert normwise.max() < 1e-13
 
 
 def test_solve_batch_errors(ctx):
