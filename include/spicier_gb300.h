@@ -312,6 +312,27 @@ int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit,
                  uint8_t* status, double* resid, double* params,
                  sp_moments* moments);
 
+/* sp_newton_dc_device without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot let a library call cudaMalloc — a host
+ * application whose device memory belongs to its own pool, a process under a
+ * hard device-memory cap, a loop that cannot take cudaMalloc's implicit
+ * device synchronisation.  No context, no topology: the circuit is copied
+ * from host memory into a fixed 16 MiB file-scope device array that also
+ * holds the drawn parameters, derived constants and fallback miss list
+ * (every GPU that loads the library holds it until exit); sweeps needing more
+ * are rejected with SP_ERR_BATCH_TOO_LARGE.  Runs on the current device.  The
+ * first call on a device does a one-time set-up (it looks up the array's
+ * address with cudaGetSymbolAddress): make it before any stream capture.
+ * All calls on a device share the array, so calls that overlap on the GPU
+ * race; order them.  Outputs as for sp_newton_dc_device (no moments); err
+ * (optional, err_len bytes) receives a message on failure. */
+int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_config* cfg,
+                        uint64_t seed, uint64_t first_index, uint64_t num_samples,
+                        const double* d_table, uint32_t table_cols,
+                        const double* d_x0, double* d_x, int32_t* d_iters,
+                        uint8_t* d_status, double* d_resid, void* stream,
+                        char* err, size_t err_len);
+
 /* Draw the per-sample parameter vectors only ([num_samples][num_params]). */
 int sp_draw_params_device(sp_ctx* ctx, const sp_topology* topo, uint64_t seed,
                           uint64_t first_index, uint64_t num_samples,

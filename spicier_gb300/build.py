@@ -21,6 +21,7 @@ UNITS = {
     "api.cu": [],
     "kernels_exact.cu": ["--fmad=false"],
     "kernels_fast.cu": [],
+    "newton_static.cu": [],
 }
 EXTRA_UNITS: dict = {}
 

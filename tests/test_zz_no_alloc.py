@@ -1,0 +1,80 @@
+"""sp_newton_dc_static — the allocation-free sweep — against the allocating
+entry point sp_newton_dc_device, through the C ABI.
+
+The static entry point exists for callers that cannot let a library allocate
+device memory (their device memory belongs to a pool they manage, or a hard
+cap forbids growth, or cudaMalloc's implicit synchronisation is not allowed
+where they call from).  It keeps all scratch in one fixed file-scope device
+array.  This file is collected last so that a run stopping at the first
+failure has already run every other test; it must pass on its own in a fresh
+process as well.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+import spicier_gb300 as sg
+from spicier_gb300 import abi, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def _bind(lib):
+    f = lib.sp_newton_dc_static
+    vp, u64 = C.c_void_p, C.c_uint64
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(abi.SpCircuit), C.POINTER(abi.SpNewtonConfig), u64, u64, u64, vp, C.c_uint32, vp,
+                  vp, vp, vp, vp, vp, C.c_char_p, C.c_size_t]
+    return f
+
+
+def _bits_equal(a, b):
+    eq = a.view(np.uint64) == b.view(np.uint64)
+    return bool(np.all(eq | (np.isnan(a) & np.isnan(b))))
+
+
+@pytest.mark.parametrize("prec", [abi.SP_PREC_MIXED, abi.SP_PREC_FP64_EXACT])
+def test_static_entry_matches_allocating_entry(product_lib, prec):
+    static = _bind(product_lib)
+    ctx = sg.Context(0)
+    circ = configs.miller_opamp()
+    topo = ctx.topology(circ)
+    cfg = abi.newton_config(precision=prec)
+    N, n = 4096, circ.n
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream().cuda_stream
+    errbuf = C.create_string_buffer(256)
+    for call, first in enumerate((0, 50000)):  # two calls in a row, different sweep ranges
+        ref = [torch.full((N, n), -1.0, dtype=torch.float64, device=dev), torch.zeros(N, dtype=torch.int32, device=dev),
+               torch.zeros(N, dtype=torch.uint8, device=dev), torch.zeros(N, dtype=torch.float64, device=dev)]
+        new = [torch.full((N, n), -2.0, dtype=torch.float64, device=dev), torch.zeros(N, dtype=torch.int32, device=dev),
+               torch.zeros(N, dtype=torch.uint8, device=dev), torch.zeros(N, dtype=torch.float64, device=dev)]
+        ctx.newton_dc_device(topo, cfg, 1, N, ref[0], first=first, iters=ref[1], status=ref[2], resid=ref[3],
+                             stream=stream)
+        rc = static(C.byref(circ.to_c()), C.byref(cfg), 1, first, N, None, 0, None, new[0].data_ptr(),
+                    new[1].data_ptr(), new[2].data_ptr(), new[3].data_ptr(), stream, errbuf, 256)
+        assert rc == 0, errbuf.value.decode()
+        torch.cuda.synchronize()
+        a = [t.cpu().numpy() for t in ref]
+        b = [t.cpu().numpy() for t in new]
+        # same kernels and inputs: identical results (the tests' FP64 bar)
+        assert _bits_equal(a[0], b[0]), f"call {call}: solutions differ"
+        assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+        assert _bits_equal(a[3], b[3])
+        assert ((b[2] & abi.SP_ST_MASK) == 0).all()
+    topo.close()
+    ctx.close()
+
+
+def test_static_entry_rejects_oversized_sweeps(product_lib):
+    static = _bind(product_lib)
+    circ = configs.miller_opamp()
+    cfg = abi.newton_config(precision=abi.SP_PREC_MIXED)
+    errbuf = C.create_string_buffer(256)
+    x = torch.empty((1, circ.n), dtype=torch.float64, device="cuda")
+    rc = static(C.byref(circ.to_c()), C.byref(cfg), 1, 0, 10_000_000, None, 0, None, x.data_ptr(), None, None,
+                None, None, errbuf, 256)
+    assert rc == abi.SP_ERR_BATCH_TOO_LARGE
+    assert b"exceeds maximum" in errbuf.value
