@@ -333,6 +333,57 @@ int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_config* cfg,
                         uint8_t* d_status, double* d_resid, void* stream,
                         char* err, size_t err_len);
 
+/* ---------------------------------------------------------------------- */
+/* Learned Newton warm start (no counterpart in the reference).            */
+/* A BF16 MLP n_in -> n_layers x n_hidden (GELU) -> n_out, trained and run */
+/* on the tensor cores with FP32 accumulation; FP32 master weights + Adam. */
+/* ---------------------------------------------------------------------- */
+typedef struct sp_mlp sp_mlp;
+typedef struct sp_mlp_desc {
+    int32_t n_in;       /* <= 64 */
+    int32_t n_hidden;   /* multiple of 32, <= 1024 */
+    int32_t n_layers;   /* hidden layers, 1..8 */
+    int32_t n_out;      /* <= 64 */
+    uint64_t init_seed; /* He-uniform initialisation from the hash RNG */
+} sp_mlp_desc;
+
+int sp_mlp_create(sp_ctx* ctx, const sp_mlp_desc* desc, sp_mlp** out);
+int sp_mlp_destroy(sp_mlp* mlp);
+/* Flat FP32 parameters: per layer Wt[out_pad][in_pad] then b[out_pad], where
+ * in/out of the first/last layer are padded to multiples of 32. */
+int sp_mlp_num_params(const sp_mlp* mlp);
+int sp_mlp_get_params(sp_mlp* mlp, float* host_params);
+int sp_mlp_set_params(sp_mlp* mlp, const float* host_params);
+/* Warm-start wiring: input j is circuit parameter slot in_slots[j],
+ * normalised as (p - in_mean[j]) / in_scale[j]; output k is MNA unknown k,
+ * x0[k] = out_mean[k] + out_scale[k] * y[k] (n_out must equal the MNA size). */
+int sp_mlp_set_io(sp_mlp* mlp, const int32_t* in_slots, const float* in_mean,
+                  const float* in_scale, const float* out_mean, const float* out_scale);
+/* y[rows][n_out] = net(x[rows][n_in]) on normalised FP32 data. */
+int sp_mlp_forward_device(sp_mlp* mlp, const float* d_x, uint64_t rows, float* d_y,
+                          void* stream);
+/* Mean-squared-error gradients of one batch (rows a multiple of 64) into
+ * d_grads[num_params] (flat layout above); *d_loss = the batch loss. */
+int sp_mlp_gradients_device(sp_mlp* mlp, const float* d_x, const float* d_t, uint64_t rows,
+                            float* d_grads, float* d_loss, void* stream);
+/* Adam training over rows/batch contiguous batches per epoch, cosine learning
+ * rate decay from lr to lr/100; d_epoch_loss[e] (optional) = sum over the
+ * epoch's batches of the batch loss. */
+int sp_mlp_train_device(sp_mlp* mlp, const float* d_x, const float* d_t, uint64_t rows,
+                        int batch, int epochs, float lr, float* d_epoch_loss, void* stream);
+
+/* Batched DC operating points started from the network's prediction:
+ * parameters are drawn once, the network maps them to an FP64 warm start, and
+ * Newton runs from there; a miss restarts from the circuit's nodeset and then
+ * the gmin/source-stepping chain (cfg.fallback).  Outputs as for
+ * sp_newton_dc_device. */
+int sp_newton_dc_learned_device(sp_ctx* ctx, const sp_topology* topo, sp_mlp* mlp,
+                                const sp_newton_config* cfg, uint64_t seed,
+                                uint64_t first_index, uint64_t num_samples,
+                                const double* d_table, uint32_t table_cols, double* d_x,
+                                int32_t* d_iters, uint8_t* d_status, double* d_resid,
+                                sp_moments* d_moments, void* stream);
+
 /* Draw the per-sample parameter vectors only ([num_samples][num_params]). */
 int sp_draw_params_device(sp_ctx* ctx, const sp_topology* topo, uint64_t seed,
                           uint64_t first_index, uint64_t num_samples,

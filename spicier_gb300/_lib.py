@@ -24,6 +24,11 @@ class SpKernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint64), ("total_ms", C.c_double)]
 
 
+class SpMlpDesc(C.Structure):
+    _fields_ = [("n_in", C.c_int32), ("n_hidden", C.c_int32), ("n_layers", C.c_int32), ("n_out", C.c_int32),
+                ("init_seed", C.c_uint64)]
+
+
 class SpicierError(RuntimeError):
     """A negative sp_status from the library (BatchedSweepError mirror)."""
 
@@ -80,6 +85,17 @@ def _bind(L):
         "sp_draw_params_device": (i32, [vp, vp, u64, u64, u64, vp, u32, vp, vp]),
         "sp_rng_fill_device": (i32, [vp, i32, u64, u64, u32, u64, vp, vp]),
         "sp_moments_device": (i32, [vp, vp, u64, u32, u32, vp, vp, vp]),
+        "sp_mlp_create": (i32, [vp, P(SpMlpDesc), P(vp)]),
+        "sp_mlp_destroy": (i32, [vp]),
+        "sp_mlp_num_params": (i32, [vp]),
+        "sp_mlp_get_params": (i32, [vp, vp]),
+        "sp_mlp_set_params": (i32, [vp, vp]),
+        "sp_mlp_set_io": (i32, [vp, vp, vp, vp, vp, vp]),
+        "sp_mlp_forward_device": (i32, [vp, vp, u64, vp, vp]),
+        "sp_mlp_gradients_device": (i32, [vp, vp, vp, u64, vp, vp, vp]),
+        "sp_mlp_train_device": (i32, [vp, vp, vp, u64, i32, i32, C.c_float, vp, vp]),
+        "sp_newton_dc_learned_device": (i32, [vp, vp, vp, P(abi.SpNewtonConfig), u64, u64, u64, vp, u32, vp, vp,
+                                              vp, vp, vp, vp]),
         "sp_profile_enable": (i32, [vp, i32]),
         "sp_profile_read": (i32, [vp, P(SpKernelTime), i32, P(i32)]),
     }

@@ -238,6 +238,85 @@ class Context:
                                                   stream))
 
 
+class Mlp:
+    """The BF16 warm-start network (sp_mlp)."""
+
+    def __init__(self, ctx: Context, n_in: int, n_out: int, n_hidden: int = 256, n_layers: int = 3,
+                 seed: int = 0):
+        from ._lib import SpMlpDesc
+        self.ctx = ctx
+        self.n_in, self.n_out, self.n_hidden, self.n_layers = n_in, n_out, n_hidden, n_layers
+        self._ptr = C.c_void_p()
+        d = SpMlpDesc(n_in, n_hidden, n_layers, n_out, seed)
+        check(ctx._ptr, load().sp_mlp_create(ctx._ptr, C.byref(d), C.byref(self._ptr)))
+
+    def close(self):
+        if self._ptr:
+            load().sp_mlp_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self) -> int:
+        return load().sp_mlp_num_params(self._ptr)
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(self.ctx._ptr, load().sp_mlp_get_params(self._ptr, _vp(out)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(self.ctx._ptr, load().sp_mlp_set_params(self._ptr, _vp(p)))
+
+    def set_io(self, in_slots, in_mean, in_scale, out_mean, out_scale):
+        arrs = [np.ascontiguousarray(in_slots, dtype=np.int32)] + [
+            np.ascontiguousarray(a, dtype=np.float32) for a in (in_mean, in_scale, out_mean, out_scale)]
+        check(self.ctx._ptr, load().sp_mlp_set_io(self._ptr, *[_vp(a) for a in arrs]))
+
+    def forward_device(self, x, rows, y, stream=0):
+        check(self.ctx._ptr, load().sp_mlp_forward_device(self._ptr, _vp(x), rows, _vp(y), stream))
+
+    def gradients_device(self, x, t, rows, grads, loss=None, stream=0):
+        check(self.ctx._ptr, load().sp_mlp_gradients_device(self._ptr, _vp(x), _vp(t), rows, _vp(grads),
+                                                            _vp(loss), stream))
+
+    def train_device(self, x, t, rows, batch, epochs, lr, epoch_loss=None, stream=0):
+        check(self.ctx._ptr, load().sp_mlp_train_device(self._ptr, _vp(x), _vp(t), rows, batch, epochs,
+                                                        C.c_float(lr), _vp(epoch_loss), stream))
+
+    def layer_shapes(self):
+        """[(out_pad, in_pad)] per layer of the flat parameter vector."""
+        kin = (self.n_in + 31) // 32 * 32
+        kout = (self.n_out + 31) // 32 * 32
+        dims = [kin] + [self.n_hidden] * self.n_layers + [kout]
+        return [(dims[i + 1], dims[i]) for i in range(len(dims) - 1)]
+
+    def unflatten(self, flat):
+        """[(Wt, b)] views of a flat parameter vector."""
+        out, o = [], 0
+        for (r, c) in self.layer_shapes():
+            W = flat[o:o + r * c].reshape(r, c)
+            o += r * c
+            b = flat[o:o + r]
+            o += r
+            out.append((W, b))
+        return out
+
+
+def newton_dc_learned_device(ctx: Context, topo: Topology, mlp: Mlp, cfg, seed, count, x, first=0, table=None,
+                             iters=None, status=None, resid=None, moments=None, stream=0):
+    cols = 0 if table is None else int(table.shape[1])
+    check(ctx._ptr, load().sp_newton_dc_learned_device(ctx._ptr, topo._ptr, mlp._ptr, C.byref(cfg), seed, first,
+                                                       count, _vp(table), cols, _vp(x), _vp(iters), _vp(status),
+                                                       _vp(resid), _vp(moments), stream))
+
+
 # ---------------------------------------------------------------------------
 # BatchedLuSolver mirror and the sweep API
 # ---------------------------------------------------------------------------

@@ -22,6 +22,7 @@ UNITS = {
     "kernels_exact.cu": ["--fmad=false"],
     "kernels_fast.cu": [],
     "newton_static.cu": [],
+    "mlp.cu": [],
 }
 EXTRA_UNITS: dict = {}
 

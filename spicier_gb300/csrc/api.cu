@@ -360,16 +360,20 @@ struct NewtonScratch {
     unsigned int* counters;  // [0] fail count, [1] undecided roundings
     sp_moments* partial;
     uint32_t moment_blocks;
+    double* x0;   // learned warm starts [count][n] (when requested)
+    size_t used;  // bytes of the context scratch this layout occupies
 };
 
-static int newton_scratch(sp_ctx* ctx, const sp_topology* t, uint64_t count, NewtonScratch& s) {
+static int newton_scratch(sp_ctx* ctx, const sp_topology* t, uint64_t count, NewtonScratch& s,
+                          bool want_x0 = false) {
     size_t bp = align256(8 * (size_t)t->num_params * count);
     size_t bd = align256(8 * (size_t)t->num_derived * count);
     size_t bl = align256(4 * count);
     size_t bc = 256;
     uint32_t mb = (uint32_t)std::min<uint64_t>(256, std::max<uint64_t>(1, count / 1024));
     size_t bm = align256(sizeof(sp_moments) * mb * (size_t)t->n);
-    int rc = ensure_scratch(ctx, bp + bd + bl + bc + bm);
+    size_t bx = want_x0 ? align256(8 * (size_t)t->n * count) : 0;
+    int rc = ensure_scratch(ctx, bp + bd + bl + bc + bm + bx);
     if (rc) return rc;
     char* b = (char*)ctx->scratch;
     s.params = (double*)b;
@@ -378,13 +382,16 @@ static int newton_scratch(sp_ctx* ctx, const sp_topology* t, uint64_t count, New
     s.counters = (unsigned int*)(b + bp + bd + bl);
     s.partial = (sp_moments*)(b + bp + bd + bl + bc);
     s.moment_blocks = mb;
+    s.x0 = want_x0 ? (double*)(b + bp + bd + bl + bc + bm) : nullptr;
+    s.used = bp + bd + bl + bc + bm + bx;
     return SP_OK;
 }
 
 static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_config* cfg, uint64_t seed,
                             uint64_t first_index, uint64_t count, const double* d_table, uint32_t table_cols,
                             const double* d_x0, double* d_x, int32_t* d_iters, uint8_t* d_status,
-                            double* d_resid, double* d_params, sp_moments* d_moments, cudaStream_t st) {
+                            double* d_resid, double* d_params, sp_moments* d_moments, cudaStream_t st,
+                            sp_mlp* warm = nullptr) {
     if (count == 0) return SP_OK;
     if (!d_x) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null output x");
     if (count > ctx->cfg.max_batch_per_launch)
@@ -405,8 +412,21 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (prec != SP_PREC_FP64 && prec != SP_PREC_MIXED && prec != SP_PREC_FP64_EXACT)
         return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad precision %d", prec);
     if (cfg->max_iterations <= 0) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "max_iterations <= 0");
+    if (warm) {
+        if (mlp_ctx(warm) != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "network belongs to another context");
+        if (!mlp_io_ready(warm)) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "network inputs/outputs not set");
+        if (mlp_outputs(warm) != t->n)
+            return fail(ctx, SP_ERR_INVALID_DIMENSION, "network has %d outputs, circuit %d unknowns",
+                        mlp_outputs(warm), t->n);
+        if (mlp_max_slot(warm) >= t->num_params)
+            return fail(ctx, SP_ERR_INVALID_DIMENSION, "network input slot %d beyond the circuit's %d parameters",
+                        mlp_max_slot(warm), t->num_params);
+        if (count > mlp_max_rows())
+            return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "learned sweeps take at most %llu samples per call",
+                        (unsigned long long)mlp_max_rows());
+    }
     NewtonScratch s;
-    int rc = newton_scratch(ctx, t, count, s);
+    int rc = newton_scratch(ctx, t, count, s, warm != nullptr);
     if (rc) return rc;
     SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 8, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
@@ -414,6 +434,11 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     {
         ProfScope prof(ctx, "draw_params", st);
         SP_CUDA(ctx, launch_draw(D, st), "draw launch");
+    }
+    if (warm) {
+        ProfScope prof(ctx, "mlp_warm_start", st);
+        SP_CUDA(ctx, mlp_warm_start(warm, s.params, (size_t)count, (int)count, s.x0, st), "network warm start");
+        d_x0 = s.x0;
     }
     NewtonLaunch L;
     L.c = t->dc;
@@ -473,6 +498,19 @@ int sp_newton_dc_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_co
                             d_iters, d_status, d_resid, d_params, d_moments, (cudaStream_t)stream);
 }
 
+int sp_newton_dc_learned_device(sp_ctx* ctx, const sp_topology* topo, sp_mlp* mlp, const sp_newton_config* cfg,
+                                uint64_t seed, uint64_t first_index, uint64_t num_samples, const double* d_table,
+                                uint32_t table_cols, double* d_x, int32_t* d_iters, uint8_t* d_status,
+                                double* d_resid, sp_moments* d_moments, void* stream) {
+    if (!ctx || !topo || !cfg || !mlp) return SP_ERR_INVALID_ARGUMENT;
+    if (topo->ctx != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "topology belongs to another context");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    return newton_dc_locked(ctx, topo, cfg, seed, first_index, num_samples, d_table, table_cols, nullptr, d_x,
+                            d_iters, d_status, d_resid, nullptr, d_moments, (cudaStream_t)stream, mlp);
+}
+
 int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* cfg, uint64_t seed,
                  uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
                  const double* x0, double* x, int32_t* iters, uint8_t* status, double* resid, double* params,
@@ -494,8 +532,7 @@ int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
     NewtonScratch ns;
     rc = newton_scratch(ctx, t, count, ns);
     if (rc) return rc;
-    size_t inner = (char*)ns.partial - (char*)ctx->scratch +
-                   align256(sizeof(sp_moments) * ns.moment_blocks * (size_t)n);
+    size_t inner = ns.used;
     size_t bx = align256(8 * count * n), bi = align256(4 * count), bs = align256(count), br = align256(8 * count);
     size_t bpar = align256(8 * count * (size_t)t->num_params), bm = align256(sizeof(sp_moments) * n);
     size_t btab = table ? align256(8 * count * (size_t)table_cols) : 0;

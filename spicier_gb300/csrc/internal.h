@@ -52,6 +52,15 @@ cudaError_t prepare_fast_kernels(int max_smem);
 // Largest dense size of the thread-per-sample Newton kernels.
 constexpr int kMaxDenseN = 28;
 
+// mlp.cu: warm start x0[rows][n_out] from parameters in SoA layout.
+cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, int rows, double* x0,
+                           cudaStream_t st);
+int mlp_outputs(const sp_mlp* m);
+int mlp_max_slot(const sp_mlp* m);
+uint64_t mlp_max_rows();
+bool mlp_io_ready(const sp_mlp* m);
+sp_ctx* mlp_ctx(const sp_mlp* m);
+
 }  // namespace sp
 
 // The context: one per device per caller; a mutex serialises host calls.

@@ -1,0 +1,102 @@
+"""The BF16 tensor-core MLP (forward, gradients, training) against the CPU
+oracle, and the learned Newton warm start against the nodeset start."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from oracle import mlp_oracle as mo
+import spicier_gb300 as sg
+from spicier_gb300 import abi, configs
+from spicier_gb300.api import Mlp
+from spicier_gb300.learned import WarmStart
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(np.ravel(a - b)) / max(np.linalg.norm(np.ravel(b)), 1e-30)
+
+
+@pytest.fixture(scope="module")
+def net(ctx):
+    m = Mlp(ctx, n_in=10, n_out=12, n_hidden=256, n_layers=3, seed=11)
+    yield m
+    m.close()
+
+
+def test_forward_matches_oracle(ctx, net):
+    rng = np.random.default_rng(0)
+    rows = 200
+    X = rng.standard_normal((rows, 10)).astype(np.float32)
+    y = torch.empty((rows, 12), dtype=torch.float32, device="cuda")
+    net.forward_device(torch.tensor(X, device="cuda"), rows, y)
+    torch.cuda.synchronize()
+    layers = net.unflatten(net.get_params())
+    Yo, _, _ = mo.forward_backward(layers, X, np.zeros((rows, 12), np.float32), 12)
+    assert rel(y.cpu().numpy(), Yo[:, :12]) < 1e-2
+
+
+def test_gradients_match_oracle(ctx, net):
+    rng = np.random.default_rng(1)
+    rows = 512
+    X = rng.standard_normal((rows, 10)).astype(np.float32)
+    T = rng.standard_normal((rows, 12)).astype(np.float32)
+    g = torch.empty(net.num_params, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    net.gradients_device(torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda"), rows, g, loss)
+    torch.cuda.synchronize()
+    layers = net.unflatten(net.get_params())
+    _, lo, go = mo.forward_backward(layers, X, T, 12)
+    gpu = net.unflatten(g.cpu().numpy())
+    assert abs(loss.item() - lo) <= 1e-2 * lo
+    for l, ((dW, db), (oW, ob)) in enumerate(zip(gpu, go)):
+        assert rel(dW, oW) < 3e-2, f"layer {l} weight gradient"
+        assert rel(db, ob) < 3e-2, f"layer {l} bias gradient"
+
+
+def test_training_is_deterministic_and_learns(ctx):
+    rng = np.random.default_rng(2)
+    rows = 8192
+    X = rng.standard_normal((rows, 10)).astype(np.float32)
+    W = rng.standard_normal((10, 12)).astype(np.float32) * 0.5
+    T = np.tanh(X @ W).astype(np.float32)
+    xs, ts = torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda")
+    finals = []
+    for _ in range(2):
+        m = Mlp(ctx, 10, 12, 256, 3, seed=5)
+        ep = torch.zeros(6, dtype=torch.float32, device="cuda")
+        m.train_device(xs, ts, rows, 1024, 6, 2e-3, ep)
+        torch.cuda.synchronize()
+        e = ep.cpu().numpy() / (rows // 1024)
+        assert e[-1] < 0.2 * e[0]
+        finals.append(m.get_params())
+        m.close()
+    assert np.array_equal(finals[0], finals[1])
+
+
+def test_learned_warm_start_cuts_iterations(ctx):
+    circ = configs.miller_opamp()
+    topo = ctx.topology(circ)
+    ws = WarmStart(ctx, circ, n_inputs=10, seed=3)
+    rep = ws.train(topo, seed=7, samples=1 << 17, epochs=12, batch=2048)
+    assert len(rep.inputs) == 10 and rep.epoch_loss[-1] < rep.epoch_loss[0]
+    N = 8192
+    dev = torch.device("cuda")
+    x = torch.empty((N, circ.n), dtype=torch.float64, device=dev)
+    it = torch.empty(N, dtype=torch.int32, device=dev)
+    st = torch.empty(N, dtype=torch.uint8, device=dev)
+    cfg = abi.newton_config(precision=abi.SP_PREC_MIXED)
+    ws.sweep_device(topo, cfg, 1, N, x, iters=it, status=st)
+    torch.cuda.synchronize()
+    xl, il, sl = x.cpu().numpy(), it.cpu().numpy(), st.cpu().numpy()
+    base = ctx.newton_dc(circ, cfg, 1, N)
+    assert ((sl & abi.SP_ST_MASK) == 0).all()
+    assert (sl & abi.SP_ST_FLAG_WARM).all()
+    assert il.mean() < base.iters.mean() - 0.5, (il.mean(), base.iters.mean())
+    xo, _io, _so, _ = oracle.newton_dc(circ, abi.newton_config(), 1, N)
+    tol = np.empty_like(xo)
+    nn = circ.num_nodes
+    tol[:, :nn] = 1e-3 * np.abs(xo[:, :nn]) + 1e-6
+    tol[:, nn:] = 1e-3 * np.abs(xo[:, nn:]) + 1e-12
+    assert np.all(np.abs(xl - xo) <= tol)
