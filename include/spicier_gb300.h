@@ -278,6 +278,26 @@ int sp_topology_destroy(sp_topology* topo);
 /* Number of MNA unknowns (nodes + branches). */
 int sp_topology_size(const sp_topology* topo);
 
+/* Topology-specialised Newton kernel for `precision` (SP_PREC_MIXED or
+ * SP_PREC_FP64): the element list, the sparsity pattern and a static pivot
+ * order (partial pivoting of the Jacobian at the nominal operating point)
+ * with its symbolic fill are compiled into straight-line register code with
+ * NVRTC (the cached symbolic factorisation of CachedSparseLu,
+ * crates/spicier-solver/src/linear.rs:334-410, fixed at compile time).
+ * enable != 0 builds it (once) and uses it for later sweeps of that
+ * precision; enable == 0 returns to the generic kernels.  SP_PREC_MIXED is
+ * specialised automatically on first use unless disabled here.  log (optional)
+ * receives the compiler log or the reason for a failure. */
+int sp_topology_specialize(sp_ctx* ctx, sp_topology* topo, int precision, int enable,
+                           char* log, size_t log_len);
+
+/* The CUDA source of a circuit's specialised kernel, without a device: fills
+ * src (capacity src_len, truncated) and, when compile != 0, compiles it with
+ * NVRTC for sm_103a (the compiler log goes to src on failure).  *nnz (optional)
+ * receives the number of Jacobian slots (structural nonzeros + fill). */
+int sp_specialize_source(const sp_circuit* circuit, int precision, int compile, char* src,
+                         size_t src_len, int* nnz);
+
 /* Batched DC operating points on device buffers.
  *   Samples are sweep indices first_index .. first_index + num_samples - 1;
  *   draws are keyed by (seed, sweep index, rng_index) so any split of a sweep

@@ -222,6 +222,13 @@ class Context:
     def rng_fill_device(self, kind: int, seed: int, first: int, param: int, count: int, out, stream: int = 0):
         check(self._ptr, load().sp_rng_fill_device(self._ptr, kind, seed, first, param, count, _vp(out), stream))
 
+    def specialize(self, topo: Topology, precision: int = abi.SP_PREC_MIXED, enable: bool = True) -> str:
+        """Build (NVRTC) and enable / disable the topology-specialised kernel."""
+        log = C.create_string_buffer(1 << 16)
+        check(self._ptr, load().sp_topology_specialize(self._ptr, topo._ptr, precision, 1 if enable else 0, log,
+                                                       len(log)))
+        return log.value.decode(errors="replace")
+
     def profile_enable(self, on: bool = True):
         check(self._ptr, load().sp_profile_enable(self._ptr, 1 if on else 0))
 
@@ -307,6 +314,18 @@ class Mlp:
             o += r
             out.append((W, b))
         return out
+
+
+def specialized_source(circuit: Circuit, precision: int = abi.SP_PREC_MIXED, compile: bool = False):
+    """(source, jacobian_slots) of a circuit's specialised kernel; compiles it
+    with NVRTC when asked (no device needed).  Raises on failure."""
+    buf = C.create_string_buffer(1 << 21)
+    nnz = C.c_int(0)
+    rc = load().sp_specialize_source(C.byref(circuit.to_c()), precision, 1 if compile else 0, buf, len(buf),
+                                     C.byref(nnz))
+    if rc != 0:
+        raise SpicierError(rc, buf.value.decode(errors="replace")[:2000])
+    return buf.value.decode(errors="replace"), nnz.value
 
 
 def newton_dc_learned_device(ctx: Context, topo: Topology, mlp: Mlp, cfg, seed, count, x, first=0, table=None,

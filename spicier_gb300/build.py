@@ -23,6 +23,7 @@ UNITS = {
     "kernels_fast.cu": [],
     "newton_static.cu": [],
     "mlp.cu": [],
+    "spec.cu": [],
 }
 EXTRA_UNITS: dict = {}
 
@@ -68,7 +69,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), units.items()))
     tmp = LIB + ".tmp"
-    cmd = [_nvcc(), "-shared", "-o", tmp, *objs, *ARCH]
+    cuda_lib = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64")
+    cmd = [_nvcc(), "-shared", "-o", tmp, *objs, *ARCH, "-lnvrtc", f"-L{cuda_lib}", "-Xlinker", f"-rpath={cuda_lib}"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

@@ -36,6 +36,21 @@ def cs_nmos_amp() -> Circuit:
     return c
 
 
+def bjt_diode_bias() -> Circuit:
+    """NPN common-emitter stage (RB 430k, RC ~ N(2k, 100 ohm) at rng index 0,
+    RE 200, IS 1e-15, BF 120, VAF 80) plus a 1k-fed diode from a 5 V rail:
+    the exponential device models of the Newton path (diode.rs, bjt.rs)."""
+    c = Circuit("bjt_diode_bias")
+    c.V("VCC", "vcc", "0", 5.0)
+    c.R("RB", "vcc", "b", 430e3)
+    c.R("RC", "vcc", "c", Gauss(2e3, 100.0, 0))
+    c.Q("Q1", "c", "b", "e", is_=1e-15, bf=120.0, vaf=80.0)
+    c.R("RE", "e", "0", 200.0)
+    c.R("RD", "vcc", "d", 1e3)
+    c.D("D1", "d", "0", is_=1e-14, n=1.0)
+    return c
+
+
 # (name, drain, gate, source, pmos, W) of the two-stage Miller op-amp, netlist order.
 OPAMP_DEVICES = (
     ("M1", "n1", "out", "tail", False, 20e-6),   # diff pair, inverting input (feedback)

@@ -3,6 +3,7 @@
 // the device copy of a circuit, scratch management and kernel launches.
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -126,6 +127,7 @@ int sp_ctx_destroy(sp_ctx* ctx) {
         cudaEventDestroy(r.b);
     }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    spec_release_all(ctx);
     delete ctx;
     return SP_OK;
 }
@@ -335,7 +337,34 @@ int sp_topology_create(sp_ctx* ctx, const sp_circuit* c, sp_topology** out) {
     }
     t->dc = DevCircuit{c->num_nodes, c->num_branches, t->n, c->num_elements, c->num_params, nd,
                        del, dpar, dpul, ddoff, c->nodeset ? dns : nullptr};
+    t->h_elements.assign(c->elements, c->elements + c->num_elements);
+    t->h_params.assign(c->params, c->params + c->num_params);
+    if (c->nodeset) t->h_nodeset.assign(c->nodeset, c->nodeset + t->n);
     *out = t;
+    return SP_OK;
+}
+
+int sp_topology_specialize(sp_ctx* ctx, sp_topology* t, int precision, int enable, char* log, size_t log_len) {
+    if (!ctx || !t) return SP_ERR_INVALID_ARGUMENT;
+    if (t->ctx != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "topology belongs to another context");
+    if (precision != SP_PREC_MIXED && precision != SP_PREC_FP64)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "specialisation exists for SP_PREC_MIXED and SP_PREC_FP64");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    const int sidx = precision == SP_PREC_MIXED ? 0 : 1;
+    if (!enable) {
+        t->spec_enabled[sidx] = false;
+        return SP_OK;
+    }
+    std::string why;
+    int rc = spec_prepare(t, precision, why);
+    const std::string& msg = rc == SP_OK ? t->spec_log[sidx] : why;
+    if (log && log_len) {
+        std::strncpy(log, msg.c_str(), log_len - 1);
+        log[log_len - 1] = '\0';
+    }
+    if (rc != SP_OK) return fail(ctx, rc, "specialisation failed: %s", why.c_str());
+    t->spec_enabled[sidx] = true;
     return SP_OK;
 }
 
@@ -461,11 +490,22 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     int grid = (int)((count + block - 1) / block);
     static const char* kname[3] = {"newton_primary_fp64", "newton_primary_mixed", "newton_primary_fp64_exact"};
     static const char* fname[3] = {"newton_fallback_fp64", "newton_fallback_mixed", "newton_fallback_fp64_exact"};
+    static const char* sname[2] = {"newton_primary_mixed_spec", "newton_primary_fp64_spec"};
+    // topology-specialised primary kernel when enabled and buildable
+    const int sidx = prec == SP_PREC_MIXED ? 0 : (prec == SP_PREC_FP64 ? 1 : -1);
+    bool use_spec = false;
+    if (sidx >= 0 && t->spec_enabled[sidx] && !std::getenv("SPICIER_GB300_GENERIC")) {
+        std::string why;
+        use_spec = spec_prepare(const_cast<sp_topology*>(t), prec, why) == SP_OK;
+    }
     cudaError_t e;
     {
-        ProfScope prof(ctx, kname[prec], st);
-        e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, false, grid, block, smem, st)
-                                       : launch_newton_fast(kprec, L, false, grid, block, smem, st);
+        ProfScope prof(ctx, use_spec ? sname[sidx] : kname[prec], st);
+        if (use_spec)
+            e = spec_launch(t, prec, L, st);
+        else
+            e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, false, grid, block, smem, st)
+                                           : launch_newton_fast(kprec, L, false, grid, block, smem, st);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "newton launch");
     const bool any_fallback = d_x0 || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE));

@@ -49,11 +49,11 @@ __host__ __device__ inline double thermal_voltage_300() {
 
 // nvt * ln(nvt / (sqrt(2) * 1e-14)) — the critical voltage of the diode
 // limiter (diode.rs:139).  The saturation current in it is the literal 1e-14.
-__device__ inline double diode_vcrit(double nvt) { return nvt * log(nvt / (1.4142135623730951 * 1e-14)); }
+__host__ __device__ inline double diode_vcrit(double nvt) { return nvt * log(nvt / (1.4142135623730951 * 1e-14)); }
 
 // diode.rs:138-148 with vcrit precomputed (the same value the reference
 // recomputes on every call).
-__device__ inline double limit_voltage(double vd, double nvt, double vcrit) {
+__host__ __device__ inline double limit_voltage(double vd, double nvt, double vcrit) {
     if (vd > vcrit) {
         double arg = (vd - vcrit) / nvt;
         return vcrit + nvt * (1.0 + log1p(arg));
@@ -62,7 +62,7 @@ __device__ inline double limit_voltage(double vd, double nvt, double vcrit) {
 }
 
 // Level-1 evaluate (level1.rs:154-191); vth = |VTO|, beta = KP*NF*W/L.
-__device__ inline void mos_eval(bool pmos, double vth, double beta, double lambda, double vgs,
+__host__ __device__ inline void mos_eval(bool pmos, double vth, double beta, double lambda, double vgs,
                                 double vds, double& ids, double& gds, double& gm) {
     if (pmos) {
         vgs = -vgs;
@@ -92,11 +92,58 @@ __device__ inline void mos_eval(bool pmos, double vth, double beta, double lambd
     }
 }
 
+// Derived per-sample constants of one element from its parameters
+// (P(slot) -> value; out(k, value) stores derived constant k).  The same
+// operation order as the reference's per-call computations, done once.
+template <class PF, class OF>
+__host__ __device__ inline void derive_element(const sp_element& el, PF P, OF out) {
+    const double vt = thermal_voltage_300();
+    switch (el.kind) {
+        case SP_EL_R: out(0, 1.0 / P(el.field[0])); break;  // passive.rs:48-50
+        case SP_EL_D: {
+            double nvt = P(el.field[1]) * vt;
+            out(0, P(el.field[0]));
+            out(1, nvt);
+            out(2, diode_vcrit(nvt));
+            break;
+        }
+        case SP_EL_NMOS:
+        case SP_EL_PMOS: {
+            // vth = |VTO| (level1.rs:164); beta = kp * nf * w / l (level1.rs:68-70)
+            double kp = P(el.field[1]), w = P(el.field[3]), l = P(el.field[4]), nf = P(el.field[5]);
+            out(0, fabs(P(el.field[0])));
+            out(1, kp * nf * w / l);
+            out(2, P(el.field[2]));
+            break;
+        }
+        case SP_EL_NPN:
+        case SP_EL_PNP: {
+            double nf_vt = P(el.field[3]) * vt, nr_vt = P(el.field[4]) * vt;
+            out(0, P(el.field[0]));
+            out(1, P(el.field[1]));
+            out(2, P(el.field[2]));
+            out(3, nf_vt);
+            out(4, nr_vt);
+            out(5, P(el.field[5]));
+            out(6, diode_vcrit(nf_vt));
+            out(7, diode_vcrit(nr_vt));
+            break;
+        }
+        default: out(0, P(el.field[0])); break;  // C, L, V, I
+    }
+}
+
 // Reader of per-sample SoA arrays.
 struct SoA {
     const double* __restrict__ p;
     size_t stride;  // number of samples
-    __device__ double operator()(int slot, size_t s) const { return __ldg(p + (size_t)slot * stride + s); }
+    __host__ __device__ double operator()(int slot, size_t s) const {
+#ifdef __CUDA_ARCH__
+        return __ldg(p + (size_t)slot * stride + s);
+#else
+        return p[(size_t)slot * stride + s];
+#endif
+    }
 };
 
 // Mode of a stamping pass (Netlist::stamp_nonlinear_into, _scaled, + gmin).
@@ -106,7 +153,7 @@ enum StampMode { STAMP_PLAIN = 0, STAMP_GMIN = 1, STAMP_SCALED = 2 };
 // Sink API: double x(int i); void add(int r, int c, double v);
 //           void rhs_add(int r, double v); void rhs_set(int r, double v).
 template <class Sink>
-__device__ inline void stamp_all(const DevCircuit& c, const SoA& dv, size_t s, Sink& k, int mode,
+__host__ __device__ inline void stamp_all(const DevCircuit& c, const SoA& dv, size_t s, Sink& k, int mode,
                                  double aux) {
     const bool scaled = (mode == STAMP_SCALED);
     for (int e = 0; e < c.num_elements; ++e) {

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -85,6 +86,14 @@ struct sp_ctx {
     };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> event_pool;
+    // topology-specialised kernels, keyed by circuit structure + nominal values
+    struct Spec {
+        cudaLibrary_t lib = nullptr;
+        cudaKernel_t kernel = nullptr;
+        std::string log;
+        int nnz = 0;
+    };
+    std::map<std::string, Spec> spec_cache;
 };
 
 // Brackets one kernel launch with events when the context is profiling.
@@ -125,4 +134,20 @@ struct sp_topology {
     uint32_t min_table_cols = 0;  // 1 + largest table column any parameter reads
     void* dev = nullptr;  // one allocation: elements, params, pulses, doff, nodeset
     sp::DevCircuit dc{};
+    // host copy of the description (for the specialiser)
+    std::vector<sp_element> h_elements;
+    std::vector<sp_param> h_params;
+    std::vector<double> h_nodeset;
+    // topology-specialised kernels: [0] SP_PREC_MIXED, [1] SP_PREC_FP64
+    bool spec_tried[2] = {false, false};
+    bool spec_enabled[2] = {true, false};
+    cudaKernel_t spec_kernel[2] = {nullptr, nullptr};  // owned by the context's cache
+    std::string spec_log[2];
+    int spec_nnz[2] = {0, 0};
 };
+
+namespace sp {
+int spec_prepare(sp_topology* t, int prec, std::string& err);
+cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, cudaStream_t st);
+void spec_release_all(sp_ctx* ctx);
+}  // namespace sp

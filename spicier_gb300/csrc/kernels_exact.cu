@@ -37,44 +37,11 @@ __global__ void draw_kernel(DrawLaunch L) {
     }
     if (hard && L.hard) atomicAdd(L.hard, hard);
     auto P = [&](int slot) { return L.params_soa[(size_t)slot * L.count + s]; };
-    const double vt = thermal_voltage_300();
     for (int e = 0; e < c.num_elements; ++e) {
         const sp_element el = c.el[e];
         double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
         const size_t st = L.count;
-        switch (el.kind) {
-            case SP_EL_R: out[0] = 1.0 / P(el.field[0]); break;  // passive.rs:48-50
-            case SP_EL_D: {
-                double nvt = P(el.field[1]) * vt;
-                out[0] = P(el.field[0]);
-                out[st] = nvt;
-                out[2 * st] = diode_vcrit(nvt);
-                break;
-            }
-            case SP_EL_NMOS:
-            case SP_EL_PMOS: {
-                // vth = |VTO| (level1.rs:164); beta = kp * nf * w / l (level1.rs:68-70)
-                double kp = P(el.field[1]), w = P(el.field[3]), l = P(el.field[4]), nf = P(el.field[5]);
-                out[0] = fabs(P(el.field[0]));
-                out[st] = kp * nf * w / l;
-                out[2 * st] = P(el.field[2]);
-                break;
-            }
-            case SP_EL_NPN:
-            case SP_EL_PNP: {
-                double nf_vt = P(el.field[3]) * vt, nr_vt = P(el.field[4]) * vt;
-                out[0] = P(el.field[0]);
-                out[st] = P(el.field[1]);
-                out[2 * st] = P(el.field[2]);
-                out[3 * st] = nf_vt;
-                out[4 * st] = nr_vt;
-                out[5 * st] = P(el.field[5]);
-                out[6 * st] = diode_vcrit(nf_vt);
-                out[7 * st] = diode_vcrit(nr_vt);
-                break;
-            }
-            default: out[0] = P(el.field[0]); break;  // C, L, V, I
-        }
+        derive_element(el, P, [&](int k, double v) { out[k * st] = v; });
     }
 }
 

@@ -1,0 +1,591 @@
+// Topology-specialised Newton kernels, generated and compiled at run time.
+//
+// For one circuit the generic kernels interpret the element list and keep the
+// dense Jacobian in shared memory.  Here the element list, the MNA sparsity
+// pattern and the elimination order are constants: the host generates CUDA
+// source in which every stamp is a named register update, the factorisation
+// is straight-line code over the structural nonzeros plus their fill, and the
+// whole Newton iteration of one sample stays in registers.  The pivot order
+// is the partial-pivoting order of the Jacobian at the circuit's nominal
+// operating point (parameters at their distribution centres, x at the
+// nodeset), chosen once and cached with the symbolic fill pattern — the
+// numeric factorisation of every iteration of every sample reuses it (the
+// cached symbolic factorisation of CachedSparseLu, linear.rs:334-410, taken
+// to compile time).  A zero or non-finite pivot marks the sample singular, and
+// it goes to the generic fallback chain.
+//
+// The iteration is the correction form of the mixed-precision kernel: FP64
+// device currents and KCL residual F(x) (current form: each element adds
+// its current, not G*x - b), FP32 Jacobian and LU for the step, FP64 update
+// and convergence test (check_convergence, newton.rs:134-159).  With
+// precision SP_PREC_FP64 the Jacobian and LU are FP64 instead.
+#include <nvrtc.h>
+
+#include <cmath>
+#include <cstring>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace sp {
+
+namespace {
+
+struct Pattern {
+    int n = 0;
+    std::vector<int> perm, iperm;  // permuted row k holds original row perm[k]
+    std::vector<int> slot;         // [k*n + j] -> J slot or -1 (permuted rows)
+    int nnz = 0;
+    bool has(int k, int j) const { return slot[k * n + j] >= 0; }
+    int at(int orig_row, int col) const { return slot[iperm[orig_row] * n + col]; }
+};
+
+double nominal_value(const sp_param& p) {
+    switch (p.kind) {
+        case SP_DRAW_FIXED: return p.a;
+        case SP_DRAW_GAUSS: return p.a;
+        case SP_DRAW_UNIFORM: return 0.5 * (p.a + p.b);
+        case SP_DRAW_LOGUNIFORM: return std::sqrt(p.a * p.b);
+        default: return 1.0;
+    }
+}
+
+struct HostSink {
+    std::vector<double>& A;
+    std::vector<double>& b;
+    const std::vector<double>& xs;
+    int n;
+    double x(int i) const { return xs[i]; }
+    void add(int r, int c, double v) { A[(size_t)c * n + r] += v; }
+    void rhs_add(int r, double v) { b[r] += v; }
+    void rhs_set(int r, double v) { b[r] = v; }
+};
+
+// Structural nonzeros of the MNA Jacobian of the element list.
+std::vector<char> structure(const std::vector<sp_element>& els, int nn, int n) {
+    std::vector<char> S((size_t)n * n, 0);
+    auto put = [&](int r, int c) {
+        if (r >= 0 && c >= 0) S[(size_t)r * n + c] = 1;
+    };
+    for (const sp_element& e : els) {
+        const int a = e.node[0], b = e.node[1], c = e.node[2];
+        switch (e.kind) {
+            case SP_EL_R:
+            case SP_EL_D:
+                put(a, a), put(b, b), put(a, b), put(b, a);
+                break;
+            case SP_EL_V:
+            case SP_EL_L: {
+                const int br = nn + e.branch;
+                put(a, br), put(br, a), put(b, br), put(br, b);
+                break;
+            }
+            case SP_EL_NMOS:
+            case SP_EL_PMOS:  // d = a, g = b, s = c
+                put(a, a), put(c, c), put(a, c), put(c, a), put(a, b), put(c, b);
+                break;
+            case SP_EL_NPN:
+            case SP_EL_PNP:  // c = a, b = b, e = c
+                put(b, b), put(c, c), put(b, c), put(c, b), put(a, a), put(a, c), put(c, a), put(a, b);
+                break;
+            default:
+                break;
+        }
+    }
+    return S;
+}
+
+// Partial pivoting (column icamax over structural candidates) at the
+// nominal Jacobian, then the symbolic fill of the permuted pattern.
+bool plan(const sp_topology* t, Pattern& P, std::string& why) {
+    const int n = t->n, nn = t->num_nodes;
+    // nominal parameters and derived constants
+    std::vector<double> prm(t->num_params);
+    for (int k = 0; k < t->num_params; ++k) prm[k] = nominal_value(t->h_params[k]);
+    std::vector<double> der(t->num_derived, 0.0);
+    std::vector<int> doff(t->num_elements);
+    for (int e = 0, o = 0; e < t->num_elements; ++e) {
+        doff[e] = o;
+        const sp_element& el = t->h_elements[e];
+        derive_element(el, [&](int s) { return prm[s]; }, [&](int k, double v) { der[o + k] = v; });
+        o += derived_count(el.kind);
+    }
+    DevCircuit hc{nn, t->num_branches, n, t->num_elements, t->num_params, t->num_derived,
+                  t->h_elements.data(), t->h_params.data(), nullptr, doff.data(), nullptr};
+    std::vector<double> x(n, 0.0);
+    if (!t->h_nodeset.empty()) x = t->h_nodeset;
+    std::vector<double> A((size_t)n * n, 0.0), b(n, 0.0);
+    HostSink sink{A, b, x, n};
+    stamp_all(hc, SoA{der.data(), 1}, 0, sink, STAMP_PLAIN, 0.0);
+    std::vector<char> S = structure(t->h_elements, nn, n);
+    // work on a row-major copy with row swaps tracked in perm
+    std::vector<double> M((size_t)n * n);
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) M[(size_t)r * n + c] = A[(size_t)c * n + r];
+    std::vector<char> Sp = S;
+    P.n = n;
+    P.perm.resize(n);
+    for (int i = 0; i < n; ++i) P.perm[i] = i;
+    for (int k = 0; k < n; ++k) {
+        int piv = -1;
+        double best = -1.0;
+        for (int r = k; r < n; ++r) {
+            if (!Sp[(size_t)r * n + k]) continue;
+            double v = std::fabs(M[(size_t)r * n + k]);
+            if (v > best) {
+                best = v;
+                piv = r;
+            }
+        }
+        if (piv < 0) {
+            why = "structurally singular column " + std::to_string(k);
+            return false;
+        }
+        if (piv != k) {
+            for (int c = 0; c < n; ++c) {
+                std::swap(M[(size_t)k * n + c], M[(size_t)piv * n + c]);
+                std::swap(Sp[(size_t)k * n + c], Sp[(size_t)piv * n + c]);
+            }
+            std::swap(P.perm[k], P.perm[piv]);
+        }
+        const double d = M[(size_t)k * n + k];
+        for (int r = k + 1; r < n; ++r) {
+            if (!Sp[(size_t)r * n + k]) continue;
+            const double l = d != 0.0 ? M[(size_t)r * n + k] / d : 0.0;
+            for (int c = k + 1; c < n; ++c)
+                if (Sp[(size_t)k * n + c]) {
+                    M[(size_t)r * n + c] -= l * M[(size_t)k * n + c];
+                    Sp[(size_t)r * n + c] = 1;  // fill
+                }
+        }
+    }
+    P.iperm.resize(n);
+    for (int k = 0; k < n; ++k) P.iperm[P.perm[k]] = k;
+    P.slot.assign((size_t)n * n, -1);
+    P.nnz = 0;
+    for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+            if (Sp[(size_t)k * n + j]) P.slot[k * n + j] = P.nnz++;
+    return true;
+}
+
+const char* kPreamble = R"SRC(
+typedef unsigned long long u64;
+struct SpecArgs {
+    const double* dv; u64 stride; u64 count;
+    const double* x0; const double* nodeset;
+    double* x; int* iters; unsigned char* status; double* resid;
+    unsigned int* fail_list; unsigned int* fail_count;
+    double reltol, vabstol, iabstol; int max_it; int fallback_any;
+};
+__device__ __forceinline__ bool spx_fin(double v) { return fabs(v) <= 1.7976931348623157e308; }
+__device__ __forceinline__ bool spx_bad(float p, float iv) { return !(fabsf(p) > 0.f) || !(fabsf(iv) <= 3.0e38f); }
+__device__ __forceinline__ bool spx_bad(double p, double iv) { return !(fabs(p) > 0.0) || !(fabs(iv) <= 1.0e308); }
+__device__ __forceinline__ double spx_lim(double vd, double nvt, double vcrit) {
+    if (vd > vcrit) { double arg = (vd - vcrit) / nvt; return vcrit + nvt * (1.0 + log1p(arg)); }
+    return vd;
+}
+__device__ __forceinline__ void spx_mos(bool pmos, double vth, double beta, double lam, double vgs, double vds,
+                                        double& ids, double& gds, double& gm) {
+    if (pmos) { vgs = -vgs; vds = -vds; }
+    if (vgs < vth) { ids = 0.0; gds = 1e-12; gm = 0.0; }
+    else if (vds < vgs - vth) {
+        double vov = vgs - vth;
+        double i = beta * (vov * vds - 0.5 * vds * vds) * (1.0 + lam * vds);
+        double g = beta * (vov - vds) * (1.0 + lam * vds) + beta * (vov * vds - 0.5 * vds * vds) * lam;
+        double m = beta * vds * (1.0 + lam * vds);
+        ids = pmos ? -i : i; gds = fmax(g, 1e-12); gm = m;
+    } else {
+        double vov = vgs - vth;
+        double i = 0.5 * beta * vov * vov * (1.0 + lam * vds);
+        double g = 0.5 * beta * vov * vov * lam;
+        double m = beta * vov * (1.0 + lam * vds);
+        ids = pmos ? -i : i; gds = fmax(g, 1e-12); gm = m;
+    }
+}
+)SRC";
+
+std::string V(int node) { return node >= 0 ? "x[" + std::to_string(node) + "]" : "0.0"; }
+
+// Element currents into F (and, when jac, conductances into J).
+void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P, const std::vector<int>& doff,
+                   bool jac) {
+    const int nn = t->num_nodes;
+    auto cst = [&](int e, int k) { return "c" + std::to_string(doff[e] + k); };
+    auto J = [&](int r, int c, const std::string& expr, bool neg) {
+        if (r < 0 || c < 0 || !jac) return;
+        o << "    J[" << P.at(r, c) << "] " << (neg ? "-=" : "+=") << " " << expr << ";\n";
+    };
+    auto F = [&](int r, const std::string& expr, bool neg) {
+        if (r < 0) return;
+        o << "    F[" << r << "] " << (neg ? "-=" : "+=") << " " << expr << ";\n";
+    };
+    for (int e = 0; e < t->num_elements; ++e) {
+        const sp_element& el = t->h_elements[e];
+        const int a = el.node[0], b = el.node[1], c = el.node[2];
+        o << "  { // element " << e << "\n";
+        switch (el.kind) {
+            case SP_EL_R:
+                o << "    double i = " << cst(e, 0) << " * (" << V(a) << " - " << V(b) << ");\n";
+                F(a, "i", false), F(b, "i", true);
+                break;  // linear J in J0
+            case SP_EL_V:
+            case SP_EL_L: {
+                const int br = nn + el.branch;
+                F(a, "x[" + std::to_string(br) + "]", false);
+                F(b, "x[" + std::to_string(br) + "]", true);
+                std::string val = el.kind == SP_EL_V ? cst(e, 0) : std::string("0.0");
+                o << "    F[" << br << "] += " << V(a) << " - " << V(b) << " - " << val << ";\n";
+                break;
+            }
+            case SP_EL_I:
+                F(a, cst(e, 0), false), F(b, cst(e, 0), true);
+                break;
+            case SP_EL_C:
+                break;
+            case SP_EL_D:
+                o << "    double vd = " << V(a) << " - " << V(b) << ";\n"
+                  << "    double vl = spx_lim(vd, " << cst(e, 1) << ", " << cst(e, 2) << ");\n"
+                  << "    double vl2 = spx_lim(vl, " << cst(e, 1) << ", " << cst(e, 2) << ");\n"
+                  << "    double ex = exp(vl2 / " << cst(e, 1) << ");\n"
+                  << "    double id = " << cst(e, 0) << " * (ex - 1.0);\n"
+                  << "    double gd = fmax(" << cst(e, 0) << " * ex / " << cst(e, 1) << ", 1e-12);\n"
+                  << "    double i = id + gd * (vd - vl);\n";
+                F(a, "i", false), F(b, "i", true);
+                if (jac) {
+                    o << "    JT g = (JT)gd;\n";
+                    J(a, a, "g", false), J(b, b, "g", false), J(a, b, "g", true), J(b, a, "g", true);
+                }
+                break;
+            case SP_EL_NMOS:
+            case SP_EL_PMOS: {
+                const int d = a, g = b, s = c;
+                o << "    double ids, gds, gm;\n"
+                  << "    spx_mos(" << (el.kind == SP_EL_PMOS ? "true" : "false") << ", " << cst(e, 0) << ", "
+                  << cst(e, 1) << ", " << cst(e, 2) << ", " << V(g) << " - " << V(s) << ", " << V(d) << " - "
+                  << V(s) << ", ids, gds, gm);\n";
+                F(d, "ids", false), F(s, "ids", true);
+                if (jac) {
+                    o << "    JT gdf = (JT)gds, gmf = (JT)gm;\n";
+                    J(d, d, "gdf", false), J(s, s, "gdf", false), J(d, s, "gdf", true), J(s, d, "gdf", true);
+                    J(d, g, "gmf", false), J(d, s, "gmf", true), J(s, g, "gmf", true), J(s, s, "gmf", false);
+                }
+                break;
+            }
+            case SP_EL_NPN:
+            case SP_EL_PNP: {
+                const int cn = a, bn = b, en = c;
+                const bool pnp = el.kind == SP_EL_PNP;
+                o << "    double vbe = " << V(bn) << " - " << V(en) << ", vce = " << V(cn) << " - " << V(en) << ";\n"
+                  << "    double is = " << cst(e, 0) << ", bf = " << cst(e, 1) << ", br = " << cst(e, 2)
+                  << ", nfv = " << cst(e, 3) << ", nrv = " << cst(e, 4) << ", vaf = " << cst(e, 5)
+                  << ", vcf = " << cst(e, 6) << ", vcr = " << cst(e, 7) << ";\n"
+                  << "    double vbe_lim = spx_lim(" << (pnp ? "-vbe" : "vbe") << ", nfv, vcf);\n"
+                  << "    double vbe_ieq = " << (pnp ? "-vbe_lim" : "vbe_lim") << ";\n"
+                  << "    double sgn = " << (pnp ? "-1.0" : "1.0") << ";\n"
+                  << "    double ibe = sgn * vbe, ice = sgn * vce, vbc = ibe - ice;\n"
+                  << "    double exb = exp(spx_lim(ibe, nfv, vcf) / nfv), exc = exp(spx_lim(vbc, nrv, vcr) / nrv);\n"
+                  << "    double i_f = is * (exb - 1.0), i_r = is * (exc - 1.0);\n"
+                  << "    bool vfin = spx_fin(vaf) && vaf > 0.0;\n"
+                  << "    double early = (vfin && ice > 0.0) ? 1.0 + ice / vaf : 1.0;\n"
+                  << "    double ic = (i_f - i_r / br) * early, ib = i_f / bf + i_r / br;\n"
+                  << "    double gmv = (i_f > 1e-20) ? (is * exb / nfv) * early : 1e-12;\n"
+                  << "    double gpi = gmv / bf;\n"
+                  << "    double go_e = (vfin && fabs(ic) > 1e-20) ? fabs(ic) / vaf : 0.0;\n"
+                  << "    double go = fmax(go_e + is * exc / nrv / br * early, 1e-12);\n"
+                  << "    ic = sgn * ic; ib = sgn * ib;\n"
+                  << "    double gm = fmax(gmv, 1e-12); gpi = fmax(gpi, 1e-12); go = fmax(go, 1e-12);\n"
+                  << "    double fc = ic + gm * (vbe - vbe_ieq), fb = ib + gpi * (vbe - vbe_ieq);\n";
+                F(cn, "fc", false), F(bn, "fb", false), F(en, "(fc + fb)", true);
+                if (jac) {
+                    o << "    JT gpf = (JT)gpi, gof = (JT)go, gmf = (JT)gm;\n";
+                    J(bn, bn, "gpf", false), J(en, en, "gpf", false), J(bn, en, "gpf", true), J(en, bn, "gpf", true);
+                    J(cn, cn, "gof", false), J(en, en, "gof", false), J(cn, en, "gof", true), J(en, cn, "gof", true);
+                    J(cn, bn, "gmf", false), J(cn, en, "gmf", true), J(en, bn, "gmf", true), J(en, en, "gmf", false);
+                }
+                break;
+            }
+            default:
+                break;
+        }
+        o << "  }\n";
+    }
+}
+
+// Linear (per-sample constant) Jacobian entries, J0.
+void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pattern& P, const std::vector<int>& doff) {
+    const int nn = t->num_nodes;
+    o << "  JT J0[" << P.nnz << "];\n  #pragma unroll\n  for (int k = 0; k < " << P.nnz << "; ++k) J0[k] = (JT)0;\n";
+    for (int e = 0; e < t->num_elements; ++e) {
+        const sp_element& el = t->h_elements[e];
+        const int a = el.node[0], b = el.node[1];
+        if (el.kind == SP_EL_R) {
+            o << "  { JT g = (JT)c" << doff[e] << ";\n";
+            if (a >= 0) o << "    J0[" << P.at(a, a) << "] += g;\n";
+            if (b >= 0) o << "    J0[" << P.at(b, b) << "] += g;\n";
+            if (a >= 0 && b >= 0) o << "    J0[" << P.at(a, b) << "] -= g; J0[" << P.at(b, a) << "] -= g;\n";
+            o << "  }\n";
+        } else if (el.kind == SP_EL_V || el.kind == SP_EL_L) {
+            const int br = nn + el.branch;
+            if (a >= 0) o << "  J0[" << P.at(a, br) << "] += (JT)1; J0[" << P.at(br, a) << "] += (JT)1;\n";
+            if (b >= 0) o << "  J0[" << P.at(b, br) << "] -= (JT)1; J0[" << P.at(br, b) << "] -= (JT)1;\n";
+        }
+    }
+}
+
+std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
+    const int n = t->n, nn = t->num_nodes;
+    std::vector<int> doff(t->num_elements);
+    for (int e = 0, o = 0; e < t->num_elements; ++e) {
+        doff[e] = o;
+        o += derived_count(t->h_elements[e].kind);
+    }
+    std::ostringstream o;
+    o << kPreamble << "typedef " << (fp32_jac ? "float" : "double") << " JT;\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(128) spec_newton(SpecArgs a) {\n"
+      << "  const u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
+      << "  if (s >= a.count) return;\n"
+      << "  const double* dv = a.dv + s; const u64 st = a.stride;\n";
+    for (int k = 0; k < t->num_derived; ++k) o << "  const double c" << k << " = __ldg(dv + " << k << " * st);\n";
+    emit_linear_jacobian(o, t, P, doff);
+    o << "  double x[" << n << "];\n"
+      << "  const bool warm = a.x0 != 0;\n"
+      << "  if (warm) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n << " + i];\n"
+      << "  } else if (a.nodeset) {\n    #pragma unroll\n    for (int i = 0; i < " << n
+      << "; ++i) x[i] = a.nodeset[i];\n"
+      << "  } else {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = 0.0;\n  }\n"
+      << "  int it = 0, code = 1;\n"
+      << "  while (it < a.max_it) {\n    ++it;\n"
+      << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n"
+      << "    JT J[" << P.nnz << "];\n    #pragma unroll\n    for (int k = 0; k < " << P.nnz << "; ++k) J[k] = J0[k];\n";
+    emit_elements(o, t, P, doff, true);
+    // factorisation over the static pattern
+    o << "    bool sing = false;\n";
+    for (int k = 0; k < n; ++k) {
+        o << "    const JT iv" << k << " = (JT)1 / J[" << P.slot[k * n + k] << "];\n"
+          << "    sing = sing || spx_bad(J[" << P.slot[k * n + k] << "], iv" << k << ");\n";
+        for (int i = k + 1; i < n; ++i) {
+            if (!P.has(i, k)) continue;
+            const int lik = P.slot[i * n + k];
+            o << "    J[" << lik << "] *= iv" << k << ";\n";
+            for (int j = k + 1; j < n; ++j)
+                if (P.has(k, j)) o << "    J[" << P.slot[i * n + j] << "] -= J[" << lik << "] * J[" << P.slot[k * n + j] << "];\n";
+        }
+    }
+    // forward and back substitution on -F (rows permuted)
+    o << "    JT y[" << n << "];\n";
+    for (int i = 0; i < n; ++i) {
+        o << "    y[" << i << "] = (JT)(-F[" << P.perm[i] << "])";
+        for (int k = 0; k < i; ++k)
+            if (P.has(i, k)) o << " - J[" << P.slot[i * n + k] << "] * y[" << k << "]";
+        o << ";\n";
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        o << "    y[" << i << "] = (y[" << i << "]";
+        for (int j = i + 1; j < n; ++j)
+            if (P.has(i, j)) o << " - J[" << P.slot[i * n + j] << "] * y[" << j << "]";
+        o << ") * iv" << i << ";\n";
+    }
+    o << "    bool conv = true;\n";
+    for (int i = 0; i < n; ++i) {
+        o << "    { double xo = x[" << i << "], xn = xo + (double)y[" << i << "];\n"
+          << "      conv = conv && !(fabs(xn - xo) > a.reltol * fmax(fabs(xn), fabs(xo)) + "
+          << (i < nn ? "a.vabstol" : "a.iabstol") << ");\n      x[" << i << "] = xn; }\n";
+    }
+    o << "    if (sing) { code = 2; break; }\n    if (conv) { code = 0; break; }\n  }\n";
+    // status, outputs, miss list, residual
+    o << "  bool fin = true;\n  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) fin = fin && spx_fin(x[i]);\n"
+      << "  unsigned char st8 = !fin ? 3 : (code == 0 ? 0 : (code == 2 ? 2 : 1));\n"
+      << "  if (warm) st8 |= 0x10;\n"
+      << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) a.x[s * " << n << " + i] = x[i];\n"
+      << "  if (a.iters) a.iters[s] = it;\n"
+      << "  if ((st8 & 15) != 0 && (warm || a.fallback_any)) {\n"
+      << "    unsigned int k = atomicAdd(a.fail_count, 1u); a.fail_list[k] = (unsigned int)s;\n"
+      << "  } else if (a.resid) {\n"
+      << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n";
+    emit_elements(o, t, P, doff, false);
+    o << "    double r = 0.0;\n";
+    for (int i = 0; i < nn; ++i) o << "    r = fmax(r, fabs(F[" << i << "]));\n";
+    o << "    a.resid[s] = r;\n  }\n  if (a.status) a.status[s] = st8;\n}\n";
+    return o.str();
+}
+
+}  // namespace
+
+struct SpecArgsHost {
+    const double* dv;
+    unsigned long long stride, count;
+    const double* x0;
+    const double* nodeset;
+    double* x;
+    int* iters;
+    unsigned char* status;
+    double* resid;
+    unsigned int* fail_list;
+    unsigned int* fail_count;
+    double reltol, vabstol, iabstol;
+    int max_it;
+    int fallback_any;
+};
+
+// Build (once) the specialised kernel of topology t for `prec` (MIXED: FP32
+// Jacobian; FP64: FP64 Jacobian).  Returns SP_OK or an error with the reason.
+int spec_prepare(sp_topology* t, int prec, std::string& err) {
+    const int slot = prec == SP_PREC_MIXED ? 0 : 1;
+    if (t->spec_tried[slot]) {
+        if (!t->spec_kernel[slot]) err = t->spec_log[slot];
+        return t->spec_kernel[slot] ? SP_OK : SP_ERR_BACKEND;
+    }
+    t->spec_tried[slot] = true;
+    // cache key: precision, sizes, element list, parameter specs, nodeset
+    std::string key;
+    key.push_back((char)slot);
+    key.append((const char*)&t->num_nodes, sizeof(int));
+    key.append((const char*)&t->num_branches, sizeof(int));
+    key.append((const char*)t->h_elements.data(), sizeof(sp_element) * t->h_elements.size());
+    key.append((const char*)t->h_params.data(), sizeof(sp_param) * t->h_params.size());
+    key.append((const char*)t->h_nodeset.data(), sizeof(double) * t->h_nodeset.size());
+    auto hit = t->ctx->spec_cache.find(key);
+    if (hit != t->ctx->spec_cache.end()) {
+        t->spec_kernel[slot] = hit->second.kernel;
+        t->spec_log[slot] = hit->second.log;
+        t->spec_nnz[slot] = hit->second.nnz;
+        if (!t->spec_kernel[slot]) err = t->spec_log[slot];
+        return t->spec_kernel[slot] ? SP_OK : SP_ERR_BACKEND;
+    }
+    sp_ctx::Spec& entry = t->ctx->spec_cache[key];
+    Pattern P;
+    std::string why;
+    if (!plan(t, P, why)) {
+        entry.log = t->spec_log[slot] = err = "no static pivot order: " + why;
+        return SP_ERR_SOLVER;
+    }
+    entry.nnz = t->spec_nnz[slot] = P.nnz;
+    std::string src = generate(t, P, prec == SP_PREC_MIXED);
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "spec_newton.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+        entry.log = t->spec_log[slot] = err = "nvrtcCreateProgram failed";
+        return SP_ERR_BACKEND;
+    }
+    const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "--fmad=true", "-lineinfo"};
+    nvrtcResult r = nvrtcCompileProgram(prog, 4, opts);
+    size_t logsz = 0;
+    nvrtcGetProgramLogSize(prog, &logsz);
+    std::string log(logsz, '\0');
+    if (logsz) nvrtcGetProgramLog(prog, &log[0]);
+    if (r != NVRTC_SUCCESS) {
+        entry.log = t->spec_log[slot] = err = "NVRTC: " + log.substr(0, 2000);
+        nvrtcDestroyProgram(&prog);
+        return SP_ERR_BACKEND;
+    }
+    size_t cubin_sz = 0;
+    nvrtcGetCUBINSize(prog, &cubin_sz);
+    std::vector<char> cubin(cubin_sz);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    cudaLibrary_t lib = nullptr;
+    cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    cudaKernel_t k = nullptr;
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&k, lib, "spec_newton");
+    if (e != cudaSuccess) {
+        entry.log = t->spec_log[slot] = err = std::string("module load: ") + cudaGetErrorString(e);
+        return SP_ERR_BACKEND;
+    }
+    entry.lib = lib;
+    entry.kernel = t->spec_kernel[slot] = k;
+    entry.log = t->spec_log[slot] = log;
+    return SP_OK;
+}
+
+cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, cudaStream_t st) {
+    const int slot = prec == SP_PREC_MIXED ? 0 : 1;
+    SpecArgsHost a{};
+    a.dv = L.dv.p;
+    a.stride = L.dv.stride;
+    a.count = L.count;
+    a.x0 = L.x0;
+    a.nodeset = L.c.nodeset;
+    a.x = L.x;
+    a.iters = L.iters;
+    a.status = L.status;
+    a.resid = L.resid;
+    a.fail_list = L.fail_list;
+    a.fail_count = L.fail_count;
+    a.reltol = L.cfg.v_reltol;
+    a.vabstol = L.cfg.v_abstol;
+    a.iabstol = L.cfg.i_abstol;
+    a.max_it = L.cfg.max_iterations;
+    a.fallback_any = (L.cfg.fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE)) ? 1 : 0;
+    void* args[] = {&a};
+    const unsigned grid = (unsigned)((L.count + 127) / 128);
+    return cudaLaunchKernel((const void*)t->spec_kernel[slot], dim3(grid), dim3(128), args, 0, st);
+}
+
+void spec_release_all(sp_ctx* ctx) {
+    for (auto& kv : ctx->spec_cache)
+        if (kv.second.lib) cudaLibraryUnload(kv.second.lib);
+    ctx->spec_cache.clear();
+}
+
+}  // namespace sp
+
+extern "C" int sp_specialize_source(const sp_circuit* c, int precision, int compile, char* src, size_t src_len,
+                                    int* nnz) {
+    using namespace sp;
+    if (!c || (c->num_elements && !c->elements) || (c->num_params && !c->params)) return SP_ERR_INVALID_ARGUMENT;
+    if (precision != SP_PREC_MIXED && precision != SP_PREC_FP64) return SP_ERR_INVALID_ARGUMENT;
+    for (int e = 0; e < c->num_elements; ++e) {
+        const sp_element& el = c->elements[e];
+        if (el.kind < SP_EL_R || el.kind > SP_EL_PNP) return SP_ERR_INVALID_ARGUMENT;
+        const int terms = el.kind >= SP_EL_NMOS ? 3 : 2;
+        for (int k = 0; k < terms; ++k)
+            if (el.node[k] < -1 || el.node[k] >= c->num_nodes) return SP_ERR_INVALID_DIMENSION;
+        const int nf = el.kind == SP_EL_D ? 2 : (el.kind >= SP_EL_NMOS ? 6 : 1);
+        for (int f = 0; f < nf; ++f)
+            if (el.field[f] < 0 || el.field[f] >= c->num_params) return SP_ERR_INVALID_DIMENSION;
+        if ((el.kind == SP_EL_V || el.kind == SP_EL_L) && (el.branch < 0 || el.branch >= c->num_branches))
+            return SP_ERR_INVALID_DIMENSION;
+    }
+    sp_topology t;
+    t.num_nodes = c->num_nodes;
+    t.num_branches = c->num_branches;
+    t.n = c->num_nodes + c->num_branches;
+    t.num_elements = c->num_elements;
+    t.num_params = c->num_params;
+    for (int e = 0; e < c->num_elements; ++e) t.num_derived += derived_count(c->elements[e].kind);
+    t.h_elements.assign(c->elements, c->elements + c->num_elements);
+    t.h_params.assign(c->params, c->params + c->num_params);
+    if (c->nodeset) t.h_nodeset.assign(c->nodeset, c->nodeset + t.n);
+    Pattern P;
+    std::string why;
+    auto put = [&](const std::string& s) {
+        if (src && src_len) {
+            std::strncpy(src, s.c_str(), src_len - 1);
+            src[src_len - 1] = '\0';
+        }
+    };
+    if (!plan(&t, P, why)) {
+        put(why);
+        return SP_ERR_SOLVER;
+    }
+    if (nnz) *nnz = P.nnz;
+    std::string code = generate(&t, P, precision == SP_PREC_MIXED);
+    put(code);
+    if (!compile) return SP_OK;
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, code.c_str(), "spec_newton.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        return SP_ERR_BACKEND;
+    const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "--fmad=true", "-lineinfo"};
+    nvrtcResult r = nvrtcCompileProgram(prog, 4, opts);
+    if (r != NVRTC_SUCCESS) {
+        size_t logsz = 0;
+        nvrtcGetProgramLogSize(prog, &logsz);
+        std::string log(logsz, '\0');
+        if (logsz) nvrtcGetProgramLog(prog, &log[0]);
+        put(log);
+    }
+    nvrtcDestroyProgram(&prog);
+    return r == NVRTC_SUCCESS ? SP_OK : SP_ERR_BACKEND;
+}

@@ -42,10 +42,23 @@ def random_slots(circuit: Circuit) -> List[int]:
             if row[0] in (abi.SP_DRAW_GAUSS, abi.SP_DRAW_UNIFORM, abi.SP_DRAW_LOGUNIFORM)]
 
 
-def select_inputs(P: np.ndarray, X: np.ndarray, candidates: List[int], k: int) -> List[int]:
+def newton_tolerance(circuit: Circuit, X: np.ndarray, reltol=1e-3, vntol=1e-6, abstol=1e-12) -> np.ndarray:
+    """Per-unknown convergence tolerance of check_convergence
+    (crates/spicier-solver/src/newton.rs:134-159) at the typical solution."""
+    absx = np.abs(X).mean(0)
+    tol = reltol * absx
+    tol[:circuit.num_nodes] += vntol
+    tol[circuit.num_nodes:] += abstol
+    return tol
+
+
+def select_inputs(P: np.ndarray, X: np.ndarray, candidates: List[int], k: int,
+                  tol: Optional[np.ndarray] = None) -> List[int]:
     """Greedy forward selection of k parameter columns of P maximising the
-    variance of the standardised solution X explained by a linear model."""
-    Xs = (X - X.mean(0)) / np.maximum(X.std(0), 1e-300)
+    variance of the solution X explained by a linear model, with each unknown
+    measured in units of its Newton tolerance `tol` (standard deviations
+    when tol is None)."""
+    Xs = (X - X.mean(0)) / (tol if tol is not None else np.maximum(X.std(0), 1e-300))
     Ps = (P - P.mean(0)) / np.maximum(P.std(0), 1e-300)
     chosen: List[int] = []
     for _ in range(min(k, len(candidates))):
@@ -105,27 +118,58 @@ class WarmStart:
         x, P = x[:rows], P[:rows]
         cand = random_slots(c)
         sub = slice(0, min(select_rows, rows))
-        self.inputs = select_inputs(P[sub].cpu().numpy(), x[sub].cpu().numpy(), cand, self.n_inputs)
+        xs = x[sub].cpu().numpy()
+        tol = newton_tolerance(c, xs)
+        if self.n_inputs >= len(cand):
+            self.inputs = list(cand)
+        else:
+            self.inputs = select_inputs(P[sub].cpu().numpy(), xs, cand, self.n_inputs, tol)
         in_mean = np.array([param_normalization(c, s)[0] for s in self.inputs])
         in_scale = np.array([param_normalization(c, s)[1] for s in self.inputs])
         out_mean = x.mean(0).cpu().numpy()
         out_std = x.std(0).cpu().numpy()
-        out_scale = np.where(out_std > 1e-12 * np.maximum(np.abs(out_mean), 1e-30), out_std, 1.0)
+        # unknowns that do not vary (supply rails) are predicted exactly: scale 0
+        out_scale = np.where(out_std > 1e-9 * np.maximum(np.abs(out_mean), 1e-30) + 1e-300, out_std, 0.0)
+        self.tolerance = tol
         Xin = ((P[:, self.inputs] - torch.tensor(in_mean, device=dev)) / torch.tensor(in_scale, device=dev))
         Xin = Xin.to(torch.float32).contiguous()
-        T = ((x - torch.tensor(out_mean, device=dev)) / torch.tensor(out_scale, device=dev)).to(torch.float32)
+        safe = np.where(out_scale > 0, out_scale, 1.0)
+        T = ((x - torch.tensor(out_mean, device=dev)) / torch.tensor(safe, device=dev)).to(torch.float32)
         T = T.contiguous()
         loss = torch.zeros(epochs, dtype=torch.float32, device=dev)
         stream = torch.cuda.current_stream().cuda_stream
         self.mlp.train_device(Xin, T, rows, batch, epochs, lr, loss, stream=stream)
         torch.cuda.synchronize()
         self.mlp.set_io(self.inputs, in_mean, in_scale, out_mean, out_scale)
+        self._io = (out_mean, out_scale)
         per_epoch = rows // batch
         self.report = TrainReport(samples, int(ok.sum().item()), list(self.inputs),
                                   [c.param_labels[s] for s in self.inputs],
                                   [float(v) / per_epoch for v in loss.cpu().numpy()],
                                   time.perf_counter() - t0)
         return self.report
+
+    def prediction_error(self, topo: Topology, seed: int, count: int) -> np.ndarray:
+        """RMS error of the network's prediction per MNA unknown, in units of
+        that unknown's Newton tolerance, over `count` samples of `seed`."""
+        import torch
+        c = self.circuit
+        dev = torch.device("cuda", self.ctx.device)
+        x = torch.empty((count, c.n), dtype=torch.float64, device=dev)
+        st = torch.empty(count, dtype=torch.uint8, device=dev)
+        P = torch.empty((count, len(c.params)), dtype=torch.float64, device=dev)
+        self.ctx.newton_dc_device(topo, abi.newton_config(precision=abi.SP_PREC_FP64), seed, count, x, status=st,
+                                  params=P)
+        in_mean = torch.tensor([param_normalization(c, s)[0] for s in self.inputs], device=dev)
+        in_scale = torch.tensor([param_normalization(c, s)[1] for s in self.inputs], device=dev)
+        Xin = ((P[:, self.inputs] - in_mean) / in_scale).to(torch.float32).contiguous()
+        y = torch.empty((count, c.n), dtype=torch.float32, device=dev)
+        self.mlp.forward_device(Xin, count, y)
+        torch.cuda.synchronize()
+        io = self._io
+        pred = io[0] + io[1] * y.double().cpu().numpy()
+        err = pred - x.cpu().numpy()
+        return np.sqrt((err ** 2).mean(0)) / self.tolerance
 
     def sweep_device(self, topo: Topology, cfg, seed: int, count: int, x, first: int = 0, iters=None, status=None,
                      resid=None, moments=None, stream: int = 0):

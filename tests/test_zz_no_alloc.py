@@ -41,6 +41,9 @@ def test_static_entry_matches_allocating_entry(product_lib, prec):
     ctx = sg.Context(0)
     circ = configs.miller_opamp()
     topo = ctx.topology(circ)
+    # the static entry runs the generic kernels (compiling a specialised one
+    # would allocate); compare against the same kernels on the allocating side
+    ctx.specialize(topo, abi.SP_PREC_MIXED, False)
     cfg = abi.newton_config(precision=prec)
     N, n = 4096, circ.n
     dev = torch.device("cuda", 0)
