@@ -242,6 +242,9 @@ typedef struct sp_newton_config {
     double src_initial;         /* 0.1   */
     double src_step;            /* 0.1   */
     double src_min_step;        /* 0.01  */
+    int32_t warm_max_iterations; /* cap of the attempt from a warm start before the
+                                    cold restart (0: max_iterations) */
+    int32_t reserved;
 } sp_newton_config;
 
 /* Fill *cfg with the reference defaults (plain FP64, gmin+source fallback). */
@@ -379,6 +382,10 @@ int sp_mlp_set_params(sp_mlp* mlp, const float* host_params);
  * x0[k] = out_mean[k] + out_scale[k] * y[k] (n_out must equal the MNA size). */
 int sp_mlp_set_io(sp_mlp* mlp, const int32_t* in_slots, const float* in_mean,
                   const float* in_scale, const float* out_mean, const float* out_scale);
+/* FP64 linear term of the warm start, lin[n_out][n_in] (NULL removes it):
+ * x0[k] = out_mean[k] + out_scale[k] * y[k] + sum_j lin[k][j] * (p_j - in_mean[j]).
+ * The network then only has to learn what is not linear in the inputs. */
+int sp_mlp_set_linear(sp_mlp* mlp, const double* lin);
 /* y[rows][n_out] = net(x[rows][n_in]) on normalised FP32 data. */
 int sp_mlp_forward_device(sp_mlp* mlp, const float* d_x, uint64_t rows, float* d_y,
                           void* stream);

@@ -584,13 +584,16 @@ inline uint8_t dc_pipeline(const sp_circuit& c, const double* P, const sp_newton
         if (c.nodeset) std::copy(c.nodeset, c.nodeset + n, x);
         else std::fill(x, x + n, 0.0);
     };
+    sp_newton_config first = cfg;  // the warm attempt may have its own cap
     if (x0) {
         std::copy(x0, x0 + n, x);
         flags |= SP_ST_FLAG_WARM;
+        if (cfg.warm_max_iterations > 0 && cfg.warm_max_iterations < cfg.max_iterations)
+            first.max_iterations = cfg.warm_max_iterations;
     } else {
         cold_start();
     }
-    NrOutcome r = newton(c, P, cfg, StampMode::Plain, 0.0, x, m);
+    NrOutcome r = newton(c, P, first, StampMode::Plain, 0.0, x, m);
     total += r.iterations;
     last_singular = r.singular;
     bool ok = r.converged && all_finite(x, n);

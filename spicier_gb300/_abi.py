@@ -130,6 +130,8 @@ class SpNewtonConfig(C.Structure):
         ("src_initial", C.c_double),
         ("src_step", C.c_double),
         ("src_min_step", C.c_double),
+        ("warm_max_iterations", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -151,6 +153,7 @@ def newton_config(
     v_reltol: float = 1e-3,
     i_abstol: float = 1e-12,
     refine_steps: int = 0,
+    warm_max_iterations: int = 0,
 ) -> SpNewtonConfig:
     """ConvergenceCriteria::default() + Gmin/SourceSteppingParams::default()
     (crates/spicier-solver/src/newton.rs:24-34, 187-196, 222-231)."""
@@ -159,4 +162,5 @@ def newton_config(
     c.max_iterations, c.precision, c.fallback, c.refine_steps = max_iterations, precision, fallback, refine_steps
     c.gmin_initial, c.gmin_final, c.gmin_reduction, c.gmin_max_attempts = 1e-3, 1e-12, 10.0, 5
     c.src_max_attempts, c.src_initial, c.src_step, c.src_min_step = 5, 0.1, 0.1, 0.01
+    c.warm_max_iterations, c.reserved = warm_max_iterations, 0
     return c

@@ -286,6 +286,11 @@ class Mlp:
             np.ascontiguousarray(a, dtype=np.float32) for a in (in_mean, in_scale, out_mean, out_scale)]
         check(self.ctx._ptr, load().sp_mlp_set_io(self._ptr, *[_vp(a) for a in arrs]))
 
+    def set_linear(self, lin):
+        """FP64 linear term [n_out][n_in] of the warm start (None removes it)."""
+        arr = None if lin is None else np.ascontiguousarray(lin, dtype=np.float64)
+        check(self.ctx._ptr, load().sp_mlp_set_linear(self._ptr, _vp(arr)))
+
     def forward_device(self, x, rows, y, stream=0):
         check(self.ctx._ptr, load().sp_mlp_forward_device(self._ptr, _vp(x), rows, _vp(y), stream))
 

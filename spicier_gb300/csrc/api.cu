@@ -498,14 +498,18 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
         std::string why;
         use_spec = spec_prepare(const_cast<sp_topology*>(t), prec, why) == SP_OK;
     }
+    // the attempt from a warm start may carry its own iteration cap
+    NewtonLaunch Lp = L;
+    if (d_x0 && cfg->warm_max_iterations > 0 && cfg->warm_max_iterations < cfg->max_iterations)
+        Lp.cfg.max_iterations = cfg->warm_max_iterations;
     cudaError_t e;
     {
         ProfScope prof(ctx, use_spec ? sname[sidx] : kname[prec], st);
         if (use_spec)
-            e = spec_launch(t, prec, L, st);
+            e = spec_launch(t, prec, Lp, st);
         else
-            e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, false, grid, block, smem, st)
-                                           : launch_newton_fast(kprec, L, false, grid, block, smem, st);
+            e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(Lp, false, grid, block, smem, st)
+                                           : launch_newton_fast(kprec, Lp, false, grid, block, smem, st);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "newton launch");
     const bool any_fallback = d_x0 || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE));

@@ -337,6 +337,138 @@ __global__ void init_weights(float* w, int rows, int cols, int real_rows, int re
 
 __host__ __device__ inline int pad32(int x) { return (x + 31) & ~31; }
 
+// Fused inference of the warm-start path: one CTA of 256 threads runs a tile
+// of 64 samples through every layer.  Activations stay in shared memory
+// (BF16, two ping-pong buffers); each layer's weights stream in 32-wide K
+// chunks with cp.async (double buffered); warp w owns output columns
+// [32w, 32w + 32) and all 64 rows (4 x 4 m16n8k16 tiles, FP32 accumulators).
+// The output adds the FP64 linear term:
+//   x0[k] = out_mean[k] + out_scale[k] * y[k] + sum_j lin[k][j] * (p_j - in_mean[j]).
+constexpr int FT = 64;             // samples per CTA
+constexpr int FH = 256;            // widest layer supported by the fused path
+constexpr int APITCH = FH + 8;     // activation row pitch (elements)
+constexpr int WPITCH = 40;         // weight chunk row pitch (elements)
+
+struct FusedArgs {
+    const double* params_soa;
+    size_t stride;
+    int rows;
+    const int* slots;
+    const float* io;      // in_mean[n_in], in_scale[n_in], out_mean[n_out], out_scale[n_out]
+    const double* lin;    // [n_out][n_in] or nullptr
+    int n_in, n_out, kin, kout, H, L;
+    const bf16* wt;       // per layer at woff[l]
+    const float* params;  // biases at boff[l]
+    int woff[9], boff[9];
+    double* x0;
+};
+
+__global__ void __launch_bounds__(256) mlp_infer_fused(FusedArgs a) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    bf16* act0 = reinterpret_cast<bf16*>(fsm);
+    bf16* act1 = act0 + FT * APITCH;
+    bf16* wbuf = act1 + FT * APITCH;  // 2 x [FH][WPITCH]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = blockIdx.x * FT;
+    // inputs: normalised parameters -> BF16 act0[:, 0:kin]
+    for (int i = tid; i < FT * a.kin; i += 256) {
+        const int r = i / a.kin, c = i % a.kin;
+        float v = 0.f;
+        if (r0 + r < a.rows && c < a.n_in)
+            v = (float)((a.params_soa[(size_t)a.slots[c] * a.stride + r0 + r] - (double)a.io[c]) / (double)a.io[a.n_in + c]);
+        act0[r * APITCH + c] = __float2bfloat16(v);
+    }
+    bf16* in = act0;
+    bf16* out = act1;
+    int K = a.kin;
+    for (int l = 0; l < a.L; ++l) {
+        const bool last = (l == a.L - 1);
+        const int N = last ? a.kout : a.H;
+        const bf16* W = a.wt + a.woff[l];
+        const float* bias = a.params + a.boff[l];
+        const bool active = warp * 32 < N;
+        float acc[4][4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+        auto load = [&](int stage, int k0) {
+            bf16* dst = wbuf + stage * FH * WPITCH;
+            for (int c = tid; c < N * 4; c += 256) {
+                const int r = c >> 2, kc = (c & 3) * 8;
+                cp_async16(&dst[r * WPITCH + kc], W + (size_t)r * K + k0 + kc, 16);
+            }
+            cp_async_commit();
+        };
+        const int nk = K / 32;
+        __syncthreads();  // previous layer's activations are complete
+        load(0, 0);
+        for (int t = 0; t < nk; ++t) {
+            if (t + 1 < nk) {
+                load((t + 1) & 1, (t + 1) * 32);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncthreads();
+            const bf16* wb = wbuf + (t & 1) * FH * WPITCH;
+            if (active) {
+#pragma unroll
+                for (int kk = 0; kk < 32; kk += 16) {
+                    uint32_t af[4][4], bfr[4][2];
+#pragma unroll
+                    for (int mi = 0; mi < 4; ++mi)
+                        ldmatrix_x4(af[mi], &in[(mi * 16 + (lane & 15)) * APITCH + t * 32 + kk + (lane >> 4) * 8]);
+#pragma unroll
+                    for (int nj = 0; nj < 2; ++nj) {
+                        uint32_t r[4];
+                        ldmatrix_x4(r, &wb[(warp * 32 + nj * 16 + (lane & 7) + ((lane >> 4) << 3)) * WPITCH + kk +
+                                           ((lane >> 3) & 1) * 8]);
+                        bfr[nj * 2][0] = r[0];
+                        bfr[nj * 2][1] = r[1];
+                        bfr[nj * 2 + 1][0] = r[2];
+                        bfr[nj * 2 + 1][1] = r[3];
+                    }
+#pragma unroll
+                    for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+                        for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], af[mi], bfr[ni]);
+                }
+            }
+            __syncthreads();
+        }
+        if (active) {
+#pragma unroll
+            for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+                for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int row = mi * 16 + (lane >> 2) + ((e >> 1) << 3);
+                        const int col = warp * 32 + ni * 8 + (lane & 3) * 2 + (e & 1);
+                        const float v = acc[mi][ni][e] + bias[col];
+                        if (!last) {
+                            out[row * APITCH + col] = __float2bfloat16(gelu(v));
+                        } else if (col < a.n_out && r0 + row < a.rows) {
+                            const int s = r0 + row;
+                            double x = (double)a.io[2 * a.n_in + col] + (double)a.io[2 * a.n_in + a.n_out + col] * (double)v;
+                            if (a.lin)
+                                for (int j = 0; j < a.n_in; ++j)
+                                    x += a.lin[col * a.n_in + j] *
+                                         (a.params_soa[(size_t)a.slots[j] * a.stride + s] - (double)a.io[j]);
+                            a.x0[(size_t)s * a.n_out + col] = x;
+                        }
+                    }
+        }
+        bf16* tmp = in;
+        in = out;
+        out = tmp;
+        K = N;
+    }
+}
+
 }  // namespace mlp
 }  // namespace sp
 
@@ -361,6 +493,9 @@ struct sp_mlp {
     // I/O of the warm-start path
     int* io_slots = nullptr;  // [n_in]
     int max_slot = -1;        // largest input slot (checked against the circuit)
+    double* lin = nullptr;    // FP64 linear term [n_out][n_in] of the warm start
+    bool has_lin = false;
+    bool fused_ready = false;
     float* io = nullptr;      // in_mean[n_in], in_scale[n_in], out_mean[n_out], out_scale[n_out]
     bool io_set = false;
     // activation workspace for `ws_rows` rows
@@ -665,7 +800,7 @@ int sp_mlp_destroy(sp_mlp* m) {
     cudaSetDevice(m->ctx->device);
     cudaDeviceSynchronize();
     for (void* p : {(void*)m->params, (void*)m->adam_m, (void*)m->adam_v, (void*)m->grads, (void*)m->wt_bf,
-                    (void*)m->w_bf, (void*)m->step, (void*)m->io_slots, (void*)m->io, m->ws})
+                    (void*)m->w_bf, (void*)m->step, (void*)m->io_slots, (void*)m->io, m->ws, (void*)m->lin})
         if (p) cudaFree(p);
     delete m;
     return SP_OK;
@@ -785,10 +920,56 @@ int sp_mlp_train_device(sp_mlp* m, const float* d_x, const float* d_t, uint64_t 
 
 }  // extern "C"
 
+extern "C" int sp_mlp_set_linear(sp_mlp* m, const double* lin) {
+    if (!m) return SP_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(m->ctx->mu);
+    cudaSetDevice(m->ctx->device);
+    if (!lin) {
+        m->has_lin = false;
+        return SP_OK;
+    }
+    const size_t bytes = sizeof(double) * m->d.n_out * m->d.n_in;
+    if (!m->lin && cudaMalloc(&m->lin, bytes) != cudaSuccess) return mlp_fail(m->ctx, SP_ERR_MEMORY_ALLOC, "linear term");
+    if (cudaMemcpy(m->lin, lin, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return SP_ERR_TRANSFER;
+    m->has_lin = true;
+    return SP_OK;
+}
+
 // Warm start for the learned sweep: parameters (SoA) -> network -> x0 (FP64).
 namespace sp {
 cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, int rows, double* x0,
                            cudaStream_t st) {
+    if (m->H <= FH && m->L <= 9) {
+        // fused path: activations never leave shared memory
+        static const size_t smem = (size_t)2 * FT * APITCH * 2 + (size_t)2 * FH * WPITCH * 2;
+        if (!m->fused_ready) {
+            cudaError_t e = cudaFuncSetAttribute(mlp_infer_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            m->fused_ready = true;
+        }
+        FusedArgs a{};
+        a.params_soa = params_soa;
+        a.stride = stride;
+        a.rows = rows;
+        a.slots = m->io_slots;
+        a.io = m->io;
+        a.lin = m->has_lin ? m->lin : nullptr;
+        a.n_in = m->d.n_in;
+        a.n_out = m->d.n_out;
+        a.kin = m->kin;
+        a.kout = m->kout;
+        a.H = m->H;
+        a.L = m->L;
+        a.wt = m->wt_bf;
+        a.params = m->params;
+        for (int l = 0; l < m->L; ++l) {
+            a.woff[l] = (int)m->woff[l];
+            a.boff[l] = (int)m->boff[l];
+        }
+        a.x0 = x0;
+        mlp_infer_fused<<<(rows + FT - 1) / FT, 256, smem, st>>>(a);
+        return cudaGetLastError();
+    }
     if (ensure_ws(m, rows) != SP_OK) return cudaErrorMemoryAllocation;
     const int rp = (rows + 63) & ~63;
     const float* io = m->io;

@@ -250,8 +250,11 @@ extern "C" int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_co
         return report(err, err_len, SP_ERR_INVALID_DIMENSION, "MNA size %d does not fit shared memory", n);
     const size_t smem = per * block;
     const int grid = (int)((num_samples + block - 1) / block);
-    e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, false, grid, block, smem, st)
-                                   : launch_newton_fast(kprec, L, false, grid, block, smem, st);
+    NewtonLaunch Lp = L;
+    if (d_x0 && cfg->warm_max_iterations > 0 && cfg->warm_max_iterations < cfg->max_iterations)
+        Lp.cfg.max_iterations = cfg->warm_max_iterations;
+    e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(Lp, false, grid, block, smem, st)
+                                   : launch_newton_fast(kprec, Lp, false, grid, block, smem, st);
     if (e != cudaSuccess) return report(err, err_len, SP_ERR_BACKEND, "newton launch: %s", cudaGetErrorString(e));
     if (d_x0 || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE))) {
         const int fgrid = std::min(grid, std::max(1, dev->num_sms * 2));

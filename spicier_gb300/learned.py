@@ -126,16 +126,24 @@ class WarmStart:
             self.inputs = select_inputs(P[sub].cpu().numpy(), xs, cand, self.n_inputs, tol)
         in_mean = np.array([param_normalization(c, s)[0] for s in self.inputs])
         in_scale = np.array([param_normalization(c, s)[1] for s in self.inputs])
-        out_mean = x.mean(0).cpu().numpy()
-        out_std = x.std(0).cpu().numpy()
-        # unknowns that do not vary (supply rails) are predicted exactly: scale 0
-        out_scale = np.where(out_std > 1e-9 * np.maximum(np.abs(out_mean), 1e-30) + 1e-300, out_std, 0.0)
         self.tolerance = tol
-        Xin = ((P[:, self.inputs] - torch.tensor(in_mean, device=dev)) / torch.tensor(in_scale, device=dev))
-        Xin = Xin.to(torch.float32).contiguous()
-        safe = np.where(out_scale > 0, out_scale, 1.0)
-        T = ((x - torch.tensor(out_mean, device=dev)) / torch.tensor(safe, device=dev)).to(torch.float32)
-        T = T.contiguous()
+        # FP64 linear term: least squares of x on the centred inputs (normal
+        # equations, all on the device); the network learns the remainder
+        Pc = P[:, self.inputs] - torch.tensor(in_mean, device=dev)
+        A = torch.cat([Pc / torch.tensor(in_scale, device=dev), torch.ones((rows, 1), dtype=torch.float64,
+                                                                             device=dev)], 1)
+        coef = torch.linalg.solve(A.T @ A, A.T @ x)  # [n_in + 1][n]
+        lin = (coef[:-1] / torch.tensor(in_scale, device=dev)[:, None]).T.contiguous()  # [n][n_in], raw units
+        resid_t = x - coef[-1] - Pc @ lin.T
+        out_mean = (coef[-1] + resid_t.mean(0)).cpu().numpy()
+        out_std = resid_t.std(0).cpu().numpy()
+        # unknowns the linear term explains exactly (supply rails) get scale 0
+        out_scale = np.where(out_std > 1e-9 * np.maximum(np.abs(out_mean), 1e-30) + 1e-300, out_std, 0.0)
+        safe = torch.tensor(np.where(out_scale > 0, out_scale, 1.0), device=dev)
+        Xin = (Pc / torch.tensor(in_scale, device=dev)).to(torch.float32).contiguous()
+        T = ((x - torch.tensor(out_mean, device=dev) - Pc @ lin.T) / safe).to(torch.float32).contiguous()
+        self._lin = lin.cpu().numpy()
+        self.mlp.set_linear(self._lin)
         loss = torch.zeros(epochs, dtype=torch.float32, device=dev)
         stream = torch.cuda.current_stream().cuda_stream
         self.mlp.train_device(Xin, T, rows, batch, epochs, lr, loss, stream=stream)
@@ -167,11 +175,17 @@ class WarmStart:
         self.mlp.forward_device(Xin, count, y)
         torch.cuda.synchronize()
         io = self._io
-        pred = io[0] + io[1] * y.double().cpu().numpy()
+        Pc = (P[:, self.inputs] - in_mean.double()).cpu().numpy()
+        pred = io[0] + io[1] * y.double().cpu().numpy() + Pc @ self._lin.T
         err = pred - x.cpu().numpy()
         return np.sqrt((err ** 2).mean(0)) / self.tolerance
 
+    WARM_MAX_ITERATIONS = 8  # a miss restarts cold after this many iterations
+
     def sweep_device(self, topo: Topology, cfg, seed: int, count: int, x, first: int = 0, iters=None, status=None,
                      resid=None, moments=None, stream: int = 0):
+        if cfg.warm_max_iterations == 0:
+            cfg = abi.SpNewtonConfig.from_buffer_copy(cfg)
+            cfg.warm_max_iterations = self.WARM_MAX_ITERATIONS
         newton_dc_learned_device(self.ctx, topo, self.mlp, cfg, seed, count, x, first=first, iters=iters,
                                  status=status, resid=resid, moments=moments, stream=stream)

