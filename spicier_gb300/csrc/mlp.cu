@@ -311,13 +311,19 @@ __global__ void pack_params(const double* __restrict__ params_soa, size_t stride
     X[i] = __float2bfloat16(v);
 }
 
-// Outputs -> FP64 warm start x0 [rows][n_out] = mean + scale * y.
+// Outputs -> FP64 warm start x0 [rows][n_out] = mean + scale * y (+ linear term).
 __global__ void unpack_outputs(const float* __restrict__ y, int rows, int ldy, int n_out, const float* __restrict__ mean,
-                               const float* __restrict__ scale, double* __restrict__ x0) {
+                               const float* __restrict__ scale, double* __restrict__ x0, const double* __restrict__ lin,
+                               const double* __restrict__ params_soa, size_t stride, const int* __restrict__ slots,
+                               const float* __restrict__ in_mean, int n_in) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= rows * n_out) return;
     const int r = i / n_out, c = i % n_out;
-    x0[i] = (double)mean[c] + (double)scale[c] * (double)y[(size_t)r * ldy + c];
+    double x = (double)mean[c] + (double)scale[c] * (double)y[(size_t)r * ldy + c];
+    if (lin)
+        for (int j = 0; j < n_in; ++j)
+            x += lin[c * n_in + j] * (params_soa[(size_t)slots[j] * stride + r] - (double)in_mean[j]);
+    x0[i] = x;
 }
 
 // Deterministic He-uniform initialisation from the hash RNG.
@@ -355,7 +361,7 @@ struct FusedArgs {
     int rows;
     const int* slots;
     const float* io;      // in_mean[n_in], in_scale[n_in], out_mean[n_out], out_scale[n_out]
-    const double* lin;    // [n_out][n_in] or nullptr
+    const float* lin;     // [n_out][n_in] or nullptr (FP32: the warm start needs ~1e-3 relative)
     int n_in, n_out, kin, kout, H, L;
     const bf16* wt;       // per layer at woff[l]
     const float* params;  // biases at boff[l]
@@ -368,14 +374,21 @@ __global__ void __launch_bounds__(256) mlp_infer_fused(FusedArgs a) {
     bf16* act0 = reinterpret_cast<bf16*>(fsm);
     bf16* act1 = act0 + FT * APITCH;
     bf16* wbuf = act1 + FT * APITCH;  // 2 x [FH][WPITCH]
+    float* pc = reinterpret_cast<float*>(wbuf + 2 * FH * WPITCH);  // [FT][n_in] centred inputs
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = blockIdx.x * FT;
-    // inputs: normalised parameters -> BF16 act0[:, 0:kin]
+    // inputs: centred parameters (FP32, kept for the linear term) and their
+    // normalised BF16 copies act0[:, 0:kin]
     for (int i = tid; i < FT * a.kin; i += 256) {
         const int r = i / a.kin, c = i % a.kin;
         float v = 0.f;
-        if (r0 + r < a.rows && c < a.n_in)
-            v = (float)((a.params_soa[(size_t)a.slots[c] * a.stride + r0 + r] - (double)a.io[c]) / (double)a.io[a.n_in + c]);
+        if (r0 + r < a.rows && c < a.n_in) {
+            const float d = (float)(a.params_soa[(size_t)a.slots[c] * a.stride + r0 + r] - (double)a.io[c]);
+            pc[r * a.n_in + c] = d;
+            v = d / a.io[a.n_in + c];
+        } else if (c < a.n_in) {
+            pc[r * a.n_in + c] = 0.f;
+        }
         act0[r * APITCH + c] = __float2bfloat16(v);
     }
     bf16* in = act0;
@@ -453,12 +466,10 @@ __global__ void __launch_bounds__(256) mlp_infer_fused(FusedArgs a) {
                             out[row * APITCH + col] = __float2bfloat16(gelu(v));
                         } else if (col < a.n_out && r0 + row < a.rows) {
                             const int s = r0 + row;
-                            double x = (double)a.io[2 * a.n_in + col] + (double)a.io[2 * a.n_in + a.n_out + col] * (double)v;
+                            float x = a.io[2 * a.n_in + col] + a.io[2 * a.n_in + a.n_out + col] * v;
                             if (a.lin)
-                                for (int j = 0; j < a.n_in; ++j)
-                                    x += a.lin[col * a.n_in + j] *
-                                         (a.params_soa[(size_t)a.slots[j] * a.stride + s] - (double)a.io[j]);
-                            a.x0[(size_t)s * a.n_out + col] = x;
+                                for (int j = 0; j < a.n_in; ++j) x = fmaf(a.lin[col * a.n_in + j], pc[row * a.n_in + j], x);
+                            a.x0[(size_t)s * a.n_out + col] = (double)x;
                         }
                     }
         }
@@ -493,7 +504,8 @@ struct sp_mlp {
     // I/O of the warm-start path
     int* io_slots = nullptr;  // [n_in]
     int max_slot = -1;        // largest input slot (checked against the circuit)
-    double* lin = nullptr;    // FP64 linear term [n_out][n_in] of the warm start
+    double* lin = nullptr;    // linear term [n_out][n_in] of the warm start (as given)
+    float* lin_f32 = nullptr; // the same in FP32 for the fused kernel
     bool has_lin = false;
     bool fused_ready = false;
     float* io = nullptr;      // in_mean[n_in], in_scale[n_in], out_mean[n_out], out_scale[n_out]
@@ -800,7 +812,8 @@ int sp_mlp_destroy(sp_mlp* m) {
     cudaSetDevice(m->ctx->device);
     cudaDeviceSynchronize();
     for (void* p : {(void*)m->params, (void*)m->adam_m, (void*)m->adam_v, (void*)m->grads, (void*)m->wt_bf,
-                    (void*)m->w_bf, (void*)m->step, (void*)m->io_slots, (void*)m->io, m->ws, (void*)m->lin})
+                    (void*)m->w_bf, (void*)m->step, (void*)m->io_slots, (void*)m->io, m->ws, (void*)m->lin,
+                    (void*)m->lin_f32})
         if (p) cudaFree(p);
     delete m;
     return SP_OK;
@@ -928,9 +941,15 @@ extern "C" int sp_mlp_set_linear(sp_mlp* m, const double* lin) {
         m->has_lin = false;
         return SP_OK;
     }
-    const size_t bytes = sizeof(double) * m->d.n_out * m->d.n_in;
-    if (!m->lin && cudaMalloc(&m->lin, bytes) != cudaSuccess) return mlp_fail(m->ctx, SP_ERR_MEMORY_ALLOC, "linear term");
-    if (cudaMemcpy(m->lin, lin, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return SP_ERR_TRANSFER;
+    const size_t cnt = (size_t)m->d.n_out * m->d.n_in;
+    if (!m->lin && cudaMalloc(&m->lin, sizeof(double) * cnt) != cudaSuccess)
+        return mlp_fail(m->ctx, SP_ERR_MEMORY_ALLOC, "linear term");
+    if (!m->lin_f32 && cudaMalloc(&m->lin_f32, sizeof(float) * cnt) != cudaSuccess)
+        return mlp_fail(m->ctx, SP_ERR_MEMORY_ALLOC, "linear term");
+    std::vector<float> f(lin, lin + cnt);
+    if (cudaMemcpy(m->lin, lin, sizeof(double) * cnt, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(m->lin_f32, f.data(), sizeof(float) * cnt, cudaMemcpyHostToDevice) != cudaSuccess)
+        return SP_ERR_TRANSFER;
     m->has_lin = true;
     return SP_OK;
 }
@@ -941,9 +960,11 @@ cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, i
                            cudaStream_t st) {
     if (m->H <= FH && m->L <= 9) {
         // fused path: activations never leave shared memory
-        static const size_t smem = (size_t)2 * FT * APITCH * 2 + (size_t)2 * FH * WPITCH * 2;
+        const size_t smem = (size_t)2 * FT * APITCH * 2 + (size_t)2 * FH * WPITCH * 2 + (size_t)FT * m->d.n_in * 4;
         if (!m->fused_ready) {
-            cudaError_t e = cudaFuncSetAttribute(mlp_infer_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaError_t e = cudaFuncSetAttribute(mlp_infer_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)((size_t)2 * FT * APITCH * 2 + (size_t)2 * FH * WPITCH * 2 +
+                                                       (size_t)FT * 64 * 4));
             if (e != cudaSuccess) return e;
             m->fused_ready = true;
         }
@@ -953,7 +974,7 @@ cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, i
         a.rows = rows;
         a.slots = m->io_slots;
         a.io = m->io;
-        a.lin = m->has_lin ? m->lin : nullptr;
+        a.lin = m->has_lin ? m->lin_f32 : nullptr;
         a.n_in = m->d.n_in;
         a.n_out = m->d.n_out;
         a.kin = m->kin;
@@ -977,9 +998,9 @@ cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, i
                                                            io + m->d.n_in, m->d.n_in, m->kin, m->X);
     cudaError_t e = forward(m, rp, false, st);
     if (e != cudaSuccess) return e;
-    unpack_outputs<<<(rows * m->d.n_out + 255) / 256, 256, 0, st>>>(m->Y, rows, m->kout, m->d.n_out,
-                                                                    io + 2 * m->d.n_in, io + 2 * m->d.n_in + m->d.n_out,
-                                                                    x0);
+    unpack_outputs<<<(rows * m->d.n_out + 255) / 256, 256, 0, st>>>(
+        m->Y, rows, m->kout, m->d.n_out, io + 2 * m->d.n_in, io + 2 * m->d.n_in + m->d.n_out, x0,
+        m->has_lin ? m->lin : nullptr, params_soa, stride, m->io_slots, io, m->d.n_in);
     return cudaGetLastError();
 }
 int mlp_outputs(const sp_mlp* m) { return m->d.n_out; }
