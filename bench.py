@@ -4,13 +4,21 @@ second on one GB300.
 
 Workload (one "step"): Monte Carlo DC operating points of the two-stage Miller
 op-amp buffer (spicier_gb300.configs.miller_opamp, MNA size 12), 65,536
-samples, parameters drawn on the device by the stateless hash RNG (seed 1,
-each step a fresh range of sweep indices), SPICE tolerances reltol 1e-3,
-vntol 1e-6 V, abstol 1e-12 A.  Arms:
-  * headline: mixed precision (FP32 LU, FP64 residual/update) with the
-    learned MLP warm start when a trained network is present, else the
-    circuit nodeset start;
-  * plain FP64 on the GPU (same start rules as the reference API: nodeset);
+samples, parameters drawn on the device by the stateless hash RNG (seed 1;
+each step takes a fresh range of sweep indices), SPICE tolerances reltol 1e-3,
+vntol 1e-6 V, abstol 1e-12 A.
+
+Arms (all on the same sweep):
+  * headline "mixed+learned": the BF16 warm-start network (trained before the
+    timed region on 1,048,576 plain-FP64 solutions of seed 7; inputs: every
+    swept parameter) predicts each sample's operating point, then the
+    topology-specialised mixed-precision Newton kernel (FP32 sparse LU, FP64
+    residual/update) converges it; misses fall back to the nodeset start and
+    the gmin/source-stepping chain;
+  * "plain FP64": the reference algorithm on the GPU — dense partial-pivot FP64
+    LU in the companion form of solve_newton_raphson, started from the nodeset;
+  * ablations: mixed precision from the nodeset; FP64 specialised kernel;
+  * config 4 report: a 10-input network on 262,144 samples vs cold start;
   * --impl reference: the reference algorithm's CPU implementation (the C++
     restatement; Spicier's Rust cannot be built here) on all host cores.
 One JSON line on stdout (rank 0).
@@ -18,6 +26,7 @@ One JSON line on stdout (rank 0).
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -33,6 +42,7 @@ if ROOT not in sys.path:
 METRIC = "converged Newton solves/sec on 1 GB300: mixed+learned vs plain FP64, same tol"
 UNIT = "solves/s"
 SEED = 1
+TRAIN_SEED = 7
 PROFILES = os.path.join(ROOT, "profiles")
 
 
@@ -105,7 +115,7 @@ class Clocks:
 
 
 def structural_nnz(circuit):
-    """Structural nonzeros of the MNA matrix of a circuit (for the flop count)."""
+    """Structural nonzeros of the MNA matrix (for the flop counts)."""
     from spicier_gb300 import abi
     pos = set()
     nn = circuit.num_nodes
@@ -133,9 +143,14 @@ def structural_nnz(circuit):
     return len(pos)
 
 
-def mosfet_count(circuit):
+def derived_slots(circuit):
     from spicier_gb300 import abi
-    return sum(1 for e in circuit.elements if e["kind"] in (abi.SP_EL_NMOS, abi.SP_EL_PMOS))
+    cnt = 0
+    for e in circuit.elements:
+        k = e["kind"]
+        cnt += 3 if k in (abi.SP_EL_D, abi.SP_EL_NMOS, abi.SP_EL_PMOS) else 8 if k in (abi.SP_EL_NPN,
+                                                                                        abi.SP_EL_PNP) else 1
+    return cnt
 
 
 def cpu_baseline(circuit, samples, threads=0):
@@ -154,25 +169,24 @@ def cpu_baseline(circuit, samples, threads=0):
 
 def run_reference(args):
     """--impl reference: the reference algorithm's CPU implementation."""
-    rank = env_int("RANK", 0)
-    if rank != 0:
+    if env_int("RANK", 0) != 0:
         return 0
     from spicier_gb300 import configs
     circ = configs.miller_opamp()
     cores = os.cpu_count() or 1
     sample = min(args.samples, 65536)
+    steps = max(1, min(args.steps, 50))
     for _ in range(max(args.warmup, 0)):
         cpu_baseline(circ, sample)
-    rates, total_t, total_conv = [], 0.0, 0
-    for _ in range(args.steps):
-        r, dt, conv = cpu_baseline(circ, sample)
-        rates.append(r)
+    total_t, total_conv = 0.0, 0
+    for _ in range(steps):
+        _r, dt, conv = cpu_baseline(circ, sample)
         total_t += dt
         total_conv += conv
     value = total_conv / total_t if total_t > 0 else 0.0
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(args.steps, 1),
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "miller_opamp_mc_dc", "samples_per_step": sample, "mna_size": circ.n,
                    "precision": "fp64", "start": "nodeset", "seed": SEED, "parallelism": "host threads"},
@@ -192,6 +206,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--samples", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-config4", action="store_true")
+    ap.add_argument("--train-samples", type=int, default=1 << 20)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -202,6 +218,8 @@ def main():
 
     import spicier_gb300 as sg
     from spicier_gb300 import abi, configs
+    from spicier_gb300._lib import check, load
+    from spicier_gb300.learned import WarmStart, random_slots
 
     rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
     torch.cuda.set_device(local)
@@ -229,33 +247,54 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
     stream = torch.cuda.current_stream().cuda_stream
 
-    # sweep indices: each rank and each step take their own range (weak scaling)
-    per_rank = N * (args.steps + args.warmup + 4)
+    # set-up outside the timed regions: specialised kernel, warm-start network
+    t0 = time.perf_counter()
+    ctx.specialize(topo, abi.SP_PREC_MIXED, True)
+    spec_s = time.perf_counter() - t0
+    ws = WarmStart(ctx, circ, n_inputs=len(random_slots(circ)), seed=3)
+    rep = ws.train(topo, seed=TRAIN_SEED, samples=args.train_samples, epochs=16, batch=4096, lr=2e-3)
 
-    def sweep(cfg, first):
-        ctx.newton_dc_device(topo, cfg, SEED, N, x, first=first, iters=iters, status=status, resid=resid,
+    cfg_plain = abi.newton_config(precision=abi.SP_PREC_FP64)
+    cfg_mixed = abi.newton_config(precision=abi.SP_PREC_MIXED, warm_max_iterations=ws.WARM_MAX_ITERATIONS)
+    base_index = rank * N * 100000
+
+    def plain_step(first):
+        ctx.newton_dc_device(topo, cfg_plain, SEED, N, x, first=first, iters=iters, status=status, resid=resid,
                              moments=moments, stream=stream)
 
-    def timed(cfg, base):
+    def mixed_nodeset_step(first):
+        ctx.newton_dc_device(topo, cfg_mixed, SEED, N, x, first=first, iters=iters, status=status, resid=resid,
+                             moments=moments, stream=stream)
+
+    def learned_step(first):
+        ws.sweep_device(topo, cfg_mixed, SEED, N, x, first=first, iters=iters, status=status, resid=resid,
+                        moments=moments, stream=stream)
+
+    def timed(step, steps, clocks=None):
         for w in range(args.warmup):
-            sweep(cfg, base + w * N)
+            step(base_index + w * N)
         barrier()
         ctx.profile_enable(True)
         ctx.profile_read()
-        total_ms, conv, it_sum, rmax = 0.0, 0, 0, 0.0
+        if clocks:
+            clocks.start()
+        total_ms, conv, it_sum, rmax, flags = 0.0, 0, 0, 0.0, {}
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        for k in range(args.steps):
+        for k in range(steps):
             flush.fill_(float(k))  # L2 flush between timed steps (not timed)
             e0.record()
-            sweep(cfg, base + (args.warmup + k) * N)
+            step(base_index + (args.warmup + k) * N)
             e1.record()
             e1.synchronize()
             total_ms += e0.elapsed_time(e1)
             ok = (status & 0x0F) == 0
             conv += int(ok.sum().item())
             it_sum += int(iters.sum().item())
-            rmax = max(rmax, float(resid[ok].max().item()) if conv else 0.0)
+            rmax = max(rmax, float(resid[ok].max().item()) if bool(ok.any()) else 0.0)
+            for fl, cnt in zip(*np.unique(status.cpu().numpy(), return_counts=True)):
+                flags[int(fl)] = flags.get(int(fl), 0) + int(cnt)
+        clk = clocks.stop() if clocks else None
         barrier()
         prof = ctx.profile_read()
         ctx.profile_enable(False)
@@ -264,84 +303,132 @@ def main():
         if dist is not None:
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        return float(t.item()), int(c.item()), it_sum / (N * args.steps), rmax, prof
+        return dict(ms=float(t.item()), conv=int(c.item()), iters=it_sum / (N * steps), rmax=rmax, prof=prof,
+                    clocks=clk, flags=flags, steps=steps)
 
-    base = rank * per_rank
-    cfg_plain = abi.newton_config(precision=abi.SP_PREC_FP64)
-    cfg_mixed = abi.newton_config(precision=abi.SP_PREC_MIXED)
-    plain_ms, plain_conv, plain_it, plain_r, _ = timed(cfg_plain, base)
-    clocks = Clocks(local)
-    clocks.start()
-    mix_ms, mix_conv, mix_it, mix_r, prof = timed(cfg_mixed, base)
-    clk = clocks.stop()
+    plain = timed(plain_step, args.steps)
+    head = timed(learned_step, args.steps, clocks=Clocks(local))
+    abl_steps = max(3, args.steps // 5)
+    mixed_ns = timed(mixed_nodeset_step, abl_steps)
+    ctx.specialize(topo, abi.SP_PREC_FP64, True)
+    fp64_spec = timed(plain_step, abl_steps)
+    ctx.specialize(topo, abi.SP_PREC_FP64, False)
 
-    value = mix_conv / (mix_ms / 1e3)
-    plain_value = plain_conv / (plain_ms / 1e3)
+    def rate(r):
+        return r["conv"] / (r["ms"] / 1e3)
 
-    # e2e through the public host-buffer API: pinned host outputs, the
-    # circuit description uploaded by the call, outputs read back every step.
+    value, plain_value = rate(head), rate(plain)
+
+    # e2e through the public host-buffer API (pinned host outputs, the circuit
+    # uploaded by the call, all outputs read back every step)
     pin_x = torch.empty((N, n), dtype=torch.float64, pin_memory=True)
     pin_it = torch.empty(N, dtype=torch.int32, pin_memory=True)
     pin_st = torch.empty(N, dtype=torch.uint8, pin_memory=True)
     pin_r = torch.empty(N, dtype=torch.float64, pin_memory=True)
-    from spicier_gb300._lib import check, load
-    import ctypes as C
     cc = circ.to_c()
 
     def host_call(first):
-        check(ctx._ptr, load().sp_newton_dc(ctx._ptr, C.byref(cc), C.byref(cfg_mixed), SEED, first, N, None, 0,
-                                            None, pin_x.data_ptr(), pin_it.data_ptr(), pin_st.data_ptr(),
-                                            pin_r.data_ptr(), None, None))
+        check(ctx._ptr, load().sp_newton_dc_learned(ctx._ptr, C.byref(cc), ws.mlp._ptr, C.byref(cfg_mixed), SEED,
+                                                    first, N, None, 0, pin_x.data_ptr(), pin_it.data_ptr(),
+                                                    pin_st.data_ptr(), pin_r.data_ptr(), None))
 
     for w in range(args.warmup):
-        host_call(base + w * N)
+        host_call(base_index + w * N)
     barrier()
     e2e_s, e2e_conv = 0.0, 0
-    for k in range(args.steps):
+    e2e_steps = min(args.steps, 100)
+    for k in range(e2e_steps):
         flush.fill_(float(k))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        host_call(base + (args.warmup + k) * N)
+        host_call(base_index + (args.warmup + k) * N)
         e2e_s += time.perf_counter() - t0
         e2e_conv += int(((pin_st.numpy() & 0x0F) == 0).sum())
-    h2d = (C.sizeof(sg.abi.SpElement) * len(circ.elements) + C.sizeof(sg.abi.SpParam) * len(circ.params)
-           + 8 * n + 4 * len(circ.elements))
+    h2d = (C.sizeof(abi.SpElement) * len(circ.elements) + C.sizeof(abi.SpParam) * len(circ.params) + 8 * n
+           + 4 * len(circ.elements))
     d2h = N * (8 * n + 4 + 1 + 8)
     t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
     if dist is not None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     e2e_value = e2e_conv * world / float(t.item())
 
-    # roofline of the dominant kernel (the mixed primary Newton kernel)
-    kname = "newton_primary_mixed"
-    launches, kms = prof.get(kname, (0, 0.0))
-    avg_ms = kms / max(launches, 1)
-    m, nnz = mosfet_count(circ), structural_nnz(circ)
-    fp64_per_iter = 30 * m + 4 * nnz + 3 * n          # device models, FP64 residual, update + test
-    fp32_per_iter = (2 * n ** 3) // 3 + 2 * n * n     # FP32 LU factor + solve
-    fp64_flops = fp64_per_iter * mix_it * N
-    fp32_flops = fp32_per_iter * mix_it * N
-    fp64_peak = read_profile_number("pipe_peaks_gb300.txt", "fp64_tflops") or 1.21
-    fp32_peak = read_profile_number("pipe_peaks_gb300.txt", "fp32_tflops") or 70.5
-    ach = fp64_flops / (avg_ms * 1e-3) / 1e12 if avg_ms > 0 else 0.0
-    traffic = read_profile_number("newton_mixed_opamp.txt", "dram_bytes_per_launch")
-    roofline = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": ach / fp64_peak, "traffic": traffic,
-                "peak_source": "measured on this pool's GB300 by the FMA-chain probe (profiles/pipe_peaks_gb300.txt)",
-                "fp32_achieved": fp32_flops / (avg_ms * 1e-3) / 1e12 if avg_ms > 0 else 0.0,
-                "fp32_peak": fp32_peak, "kernel": kname, "avg_launch_ms": avg_ms,
-                "fp64_flops_per_launch": fp64_flops, "fp32_flops_per_launch": fp32_flops}
-    hbm_peak = 6770.8
+    # rooflines of the headline's kernels (average launch durations, live)
+    fp64_peak = read_profile_number("pipe_peaks_gb300.txt", "fp64_tflops") or 1.25
+    fp32_peak = read_profile_number("pipe_peaks_gb300.txt", "fp32_tflops") or 73.3
     try:
-        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
-    except (OSError, KeyError, ValueError):
-        pass
-    per_sample_bytes = 8 * (topo_derived(circ) + n) + 4 + 1 + 8
-    alg_bytes = per_sample_bytes * N
-    roofline_hbm = {"bound": "hbm", "achieved": alg_bytes / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0,
-                    "peak": hbm_peak, "unit": "GB/s",
-                    "frac": alg_bytes / (avg_ms * 1e-3) / 1e9 / hbm_peak if avg_ms > 0 else 0.0,
-                    "bytes_per_launch": alg_bytes}
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        peaks = {}
+    hbm_peak = peaks.get("hbm_gbs", 6770.8)
+    bf16_peak = peaks.get("bf16_tflops", 1892.9)
+    kavg = {k: v[1] / max(v[0], 1) for k, v in head["prof"].items()}
+    m_mos = sum(1 for e in circ.elements if e["kind"] in (abi.SP_EL_NMOS, abi.SP_EL_PMOS))
+    nnz = structural_nnz(circ)
+    rooflines = {}
+    if "newton_primary_mixed_spec" in kavg:
+        ms = kavg["newton_primary_mixed_spec"]
+        f64 = (30 * m_mos + 4 * nnz + 3 * n) * head["iters"] * N
+        a = f64 / (ms * 1e-3) / 1e12
+        rooflines["newton_primary_mixed_spec"] = {
+            "bound": "fp64", "achieved": a, "peak": fp64_peak, "unit": "TFLOP/s", "frac": a / fp64_peak,
+            "traffic": read_profile_number("newton_spec_opamp.txt", "dram_bytes_per_launch"),
+            "avg_launch_ms": ms, "fp64_flops_per_launch": f64,
+            "peak_source": "FP64 FMA-pipe throughput measured on this pool's GB300 (profiles/pipe_peaks_gb300.txt)"}
+    if "mlp_warm_start" in kavg:
+        ms = kavg["mlp_warm_start"]
+        ni = ws.mlp.n_in
+        fl = 2.0 * (ni * 256 + 2 * 256 * 256 + 256 * n) * N
+        a = fl / (ms * 1e-3) / 1e12
+        rooflines["mlp_warm_start"] = {"bound": "tensor", "achieved": a, "peak": bf16_peak, "unit": "TFLOP/s",
+                                       "frac": a / bf16_peak, "traffic": None, "avg_launch_ms": ms,
+                                       "flops_per_launch": fl, "peak_source": "bf16_tflops of MEASURED_PEAKS.json"}
+    if "draw_params" in kavg:
+        ms = kavg["draw_params"]
+        by = 8 * (len(circ.params) + derived_slots(circ)) * N
+        a = by / (ms * 1e-3) / 1e9
+        rooflines["draw_params"] = {"bound": "hbm", "achieved": a, "peak": hbm_peak, "unit": "GB/s",
+                                    "frac": a / hbm_peak, "traffic": None, "avg_launch_ms": ms,
+                                    "bytes_per_launch": by, "note": "limited by FP64 ln/cos, not HBM"}
+    dominant = max(kavg, key=kavg.get) if kavg else None
+    roofline = rooflines.get(dominant) or next(iter(rooflines.values()), None)
+    if roofline is not None:
+        roofline = dict(roofline, kernel=dominant)
+
+    # config 4: a 10-input network (the workload's stated MLP) on 262,144 samples
+    config4 = None
+    if not args.no_config4 and rank == 0:
+        N4 = 262144
+        ws10 = WarmStart(ctx, circ, n_inputs=10, seed=5)
+        rep10 = ws10.train(topo, seed=TRAIN_SEED, samples=args.train_samples, epochs=16, batch=4096, lr=2e-3)
+        x4 = torch.empty((N4, n), dtype=torch.float64, device=dev)
+        it4 = torch.empty(N4, dtype=torch.int32, device=dev)
+        st4 = torch.empty(N4, dtype=torch.uint8, device=dev)
+        res4 = {}
+        for name, run in (("learned", lambda f: ws10.sweep_device(topo, cfg_mixed, SEED, N4, x4, first=f, iters=it4,
+                                                                  status=st4, stream=stream)),
+                          ("cold_nodeset", lambda f: ctx.newton_dc_device(topo, cfg_mixed, SEED, N4, x4, first=f,
+                                                                          iters=it4, status=st4, stream=stream))):
+            for w in range(3):
+                run(w * N4)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            tot, conv, its, fb = 0.0, 0, 0, 0
+            for k in range(5):
+                flush.fill_(float(k))
+                e0.record()
+                run((3 + k) * N4)
+                e1.record()
+                e1.synchronize()
+                tot += e0.elapsed_time(e1)
+                s = st4.cpu().numpy()
+                conv += int(((s & 0x0F) == 0).sum())
+                its += int(it4.sum().item())
+                fb += int(((s & (abi.SP_ST_FLAG_COLD | abi.SP_ST_FLAG_GMIN | abi.SP_ST_FLAG_SOURCE)) != 0).sum())
+            res4[name] = {"solves_per_s": conv / (tot / 1e3), "iters_per_solve": its / (5 * N4),
+                          "fallback_rate": fb / (5 * N4), "converged_fraction": conv / (5 * N4)}
+        config4 = {"samples": N4, "inputs": rep10.input_labels, "train_seconds": rep10.seconds, **res4,
+                   "speedup_vs_cold": res4["learned"]["solves_per_s"] / res4["cold_nodeset"]["solves_per_s"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -350,43 +437,43 @@ def main():
                "sample": f"{N} op-amp Monte Carlo samples (one step), plain FP64 Newton from the nodeset, "
                          f"{dt:.2f} s on all host threads"}
 
-    gpu_launches = sum(v[0] for v in prof.values())
     if rank == 0:
+        def arm(r):
+            return {"value": rate(r), "unit": UNIT, "ms_per_step": r["ms"] / r["steps"],
+                    "iters_per_solve": r["iters"], "max_resid_A": r["rmax"],
+                    "kernel_ms": {k: v[1] / max(v[0], 1) for k, v in r["prof"].items()}}
+
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": mix_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32",
-            "data": "synthetic (hash-RNG Monte Carlo draws on device, seed 1)",
+            "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32/bf16",
+            "data": "synthetic (hash-RNG Monte Carlo draws on device, seed 1; network trained on seed 7)",
             "config": {"workload": "miller_opamp_mc_dc", "samples_per_step": N, "mna_size": n,
-                       "precision": "mixed (FP32 LU, FP64 residual/update/models)",
-                       "warm_start": "nodeset", "tolerances": "reltol 1e-3, vntol 1e-6 V, abstol 1e-12 A",
+                       "precision": "mixed (FP32 sparse LU, FP64 residual/update/models) + BF16 warm start",
+                       "warm_start": f"MLP {ws.mlp.n_in}->3x256 GELU->{n} + FP64-fitted linear term",
+                       "tolerances": "reltol 1e-3, vntol 1e-6 V, abstol 1e-12 A",
                        "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms / args.steps,
-                           "iters_per_solve": plain_it, "max_resid_A": plain_r},
+            "plain_fp64": arm(plain),
             "speedup_vs_plain_fp64": value / plain_value if plain_value else None,
-            "iters_per_solve": mix_it, "max_resid_A": mix_r,
-            "converged_fraction": mix_conv / (N * args.steps * world),
+            "iters_per_solve": head["iters"], "max_resid_A": head["rmax"],
+            "converged_fraction": head["conv"] / (N * args.steps * world),
+            "status_counts": {str(k): v for k, v in head["flags"].items()},
+            "ablations": {"mixed_nodeset": arm(mixed_ns), "fp64_specialised_nodeset": arm(fp64_spec)},
+            "setup": {"specialise_s": spec_s, "train_s": rep.seconds, "train_samples": rep.samples,
+                      "train_loss_first_last": [rep.epoch_loss[0], rep.epoch_loss[-1]]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "roofline": roofline, "roofline_hbm": roofline_hbm,
-            "kernel_ms": {k: v[1] / max(v[0], 1) for k, v in prof.items()},
-            "gpu_launches": gpu_launches,
-            "clocks": clk,
+            "roofline": roofline, "rooflines": rooflines,
+            "kernel_ms": kavg,
+            "gpu_launches": sum(v[0] for v in head["prof"].values()),
+            "clocks": head["clocks"],
+            "config4": config4,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0
-
-
-def topo_derived(circuit):
-    from spicier_gb300 import abi
-    cnt = 0
-    for e in circuit.elements:
-        k = e["kind"]
-        cnt += 3 if k in (abi.SP_EL_D, abi.SP_EL_NMOS, abi.SP_EL_PMOS) else 8 if k in (abi.SP_EL_NPN, abi.SP_EL_PNP) else 1
-    return cnt
 
 
 if __name__ == "__main__":

@@ -411,6 +411,12 @@ int sp_newton_dc_learned_device(sp_ctx* ctx, const sp_topology* topo, sp_mlp* ml
                                 int32_t* d_iters, uint8_t* d_status, double* d_resid,
                                 sp_moments* d_moments, void* stream);
 
+/* Same on host buffers (copies in and out; synchronises). */
+int sp_newton_dc_learned(sp_ctx* ctx, const sp_circuit* circuit, sp_mlp* mlp,
+                         const sp_newton_config* cfg, uint64_t seed, uint64_t first_index,
+                         uint64_t count, const double* table, uint32_t table_cols, double* x,
+                         int32_t* iters, uint8_t* status, double* resid, sp_moments* moments);
+
 /* Draw the per-sample parameter vectors only ([num_samples][num_params]). */
 int sp_draw_params_device(sp_ctx* ctx, const sp_topology* topo, uint64_t seed,
                           uint64_t first_index, uint64_t num_samples,

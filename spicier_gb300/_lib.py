@@ -97,6 +97,8 @@ def _bind(L):
         "sp_mlp_train_device": (i32, [vp, vp, vp, u64, i32, i32, C.c_float, vp, vp]),
         "sp_newton_dc_learned_device": (i32, [vp, vp, vp, P(abi.SpNewtonConfig), u64, u64, u64, vp, u32, vp, vp,
                                               vp, vp, vp, vp]),
+        "sp_newton_dc_learned": (i32, [vp, P(abi.SpCircuit), vp, P(abi.SpNewtonConfig), u64, u64, u64, vp, u32,
+                                       vp, vp, vp, vp, vp]),
         "sp_topology_specialize": (i32, [vp, vp, i32, i32, C.c_char_p, C.c_size_t]),
         "sp_specialize_source": (i32, [P(abi.SpCircuit), i32, i32, C.c_char_p, C.c_size_t, P(i32)]),
         "sp_profile_enable": (i32, [vp, i32]),

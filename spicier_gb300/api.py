@@ -341,6 +341,24 @@ def newton_dc_learned_device(ctx: Context, topo: Topology, mlp: Mlp, cfg, seed, 
                                                        _vp(resid), _vp(moments), stream))
 
 
+def newton_dc_learned(ctx: Context, circuit: Circuit, mlp: Mlp, cfg, seed: int, count: int, first: int = 0,
+                      table=None) -> NewtonResult:
+    """Host-buffer warm-started batched DC operating points (sp_newton_dc_learned)."""
+    n = circuit.n
+    x = np.zeros((count, n))
+    iters = np.zeros(count, np.int32)
+    status = np.zeros(count, np.uint8)
+    r = np.zeros(count)
+    cols = 0
+    if table is not None:
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        cols = table.shape[1]
+    cc = circuit.to_c()
+    check(ctx._ptr, load().sp_newton_dc_learned(ctx._ptr, C.byref(cc), mlp._ptr, C.byref(cfg), seed, first, count,
+                                                _vp(table), cols, _vp(x), _vp(iters), _vp(status), _vp(r), None))
+    return NewtonResult(x, iters, status, r, None, None)
+
+
 # ---------------------------------------------------------------------------
 # BatchedLuSolver mirror and the sweep API
 # ---------------------------------------------------------------------------

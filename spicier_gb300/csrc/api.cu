@@ -555,10 +555,10 @@ int sp_newton_dc_learned_device(sp_ctx* ctx, const sp_topology* topo, sp_mlp* ml
                             d_iters, d_status, d_resid, nullptr, d_moments, (cudaStream_t)stream, mlp);
 }
 
-int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* cfg, uint64_t seed,
-                 uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
-                 const double* x0, double* x, int32_t* iters, uint8_t* status, double* resid, double* params,
-                 sp_moments* moments) {
+static int newton_dc_host(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* cfg, uint64_t seed,
+                          uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
+                          const double* x0, double* x, int32_t* iters, uint8_t* status, double* resid,
+                          double* params, sp_moments* moments, sp_mlp* warm) {
     if (!ctx || !circuit || !cfg) return SP_ERR_INVALID_ARGUMENT;
     if (count == 0) return SP_OK;
     if (!x) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null output x");
@@ -574,7 +574,7 @@ int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
     const int n = t->n;
     // The device buffers of this call sit after the Newton scratch; size both.
     NewtonScratch ns;
-    rc = newton_scratch(ctx, t, count, ns);
+    rc = newton_scratch(ctx, t, count, ns, warm != nullptr);
     if (rc) return rc;
     size_t inner = ns.used;
     size_t bx = align256(8 * count * n), bi = align256(4 * count), bs = align256(count), br = align256(8 * count);
@@ -583,7 +583,7 @@ int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
     size_t bx0 = x0 ? bx : 0;
     rc = ensure_scratch(ctx, inner + bx + bi + bs + br + bpar + bm + btab + bx0);
     if (rc) return rc;
-    rc = newton_scratch(ctx, t, count, ns);  // pointers may have moved
+    rc = newton_scratch(ctx, t, count, ns, warm != nullptr);  // pointers may have moved
     if (rc) return rc;
     char* b = (char*)ctx->scratch + inner;
     double* d_x = (double*)b;
@@ -598,7 +598,7 @@ int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
     if (table) SP_CUDA(ctx, cudaMemcpyAsync(d_tab, table, 8 * count * table_cols, cudaMemcpyHostToDevice, st), "H2D table");
     if (x0) SP_CUDA(ctx, cudaMemcpyAsync(d_x0, x0, 8 * count * n, cudaMemcpyHostToDevice, st), "H2D x0");
     rc = newton_dc_locked(ctx, t, cfg, seed, first_index, count, d_tab, table_cols, d_x0, d_x, d_it, d_st,
-                          resid ? d_res : nullptr, params ? d_par : nullptr, moments ? d_mom : nullptr, st);
+                          resid ? d_res : nullptr, params ? d_par : nullptr, moments ? d_mom : nullptr, st, warm);
     if (rc) return rc;
     SP_CUDA(ctx, cudaMemcpyAsync(x, d_x, 8 * count * n, cudaMemcpyDeviceToHost, st), "D2H x");
     if (iters) SP_CUDA(ctx, cudaMemcpyAsync(iters, d_it, 4 * count, cudaMemcpyDeviceToHost, st), "D2H iters");
@@ -611,6 +611,23 @@ int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
                          "D2H moments");
     SP_CUDA(ctx, cudaStreamSynchronize(st), "newton_dc");
     return SP_OK;
+}
+
+int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* cfg, uint64_t seed,
+                 uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
+                 const double* x0, double* x, int32_t* iters, uint8_t* status, double* resid, double* params,
+                 sp_moments* moments) {
+    return newton_dc_host(ctx, circuit, cfg, seed, first_index, count, table, table_cols, x0, x, iters, status,
+                          resid, params, moments, nullptr);
+}
+
+int sp_newton_dc_learned(sp_ctx* ctx, const sp_circuit* circuit, sp_mlp* mlp, const sp_newton_config* cfg,
+                         uint64_t seed, uint64_t first_index, uint64_t count, const double* table,
+                         uint32_t table_cols, double* x, int32_t* iters, uint8_t* status, double* resid,
+                         sp_moments* moments) {
+    if (!mlp) return SP_ERR_INVALID_ARGUMENT;
+    return newton_dc_host(ctx, circuit, cfg, seed, first_index, count, table, table_cols, nullptr, x, iters,
+                          status, resid, nullptr, moments, mlp);
 }
 
 int sp_draw_params_device(sp_ctx* ctx, const sp_topology* t, uint64_t seed, uint64_t first_index,

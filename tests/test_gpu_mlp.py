@@ -8,7 +8,7 @@ import oracle
 from oracle import mlp_oracle as mo
 import spicier_gb300 as sg
 from spicier_gb300 import abi, configs
-from spicier_gb300.api import Mlp
+from spicier_gb300.api import Mlp, newton_dc_learned
 from spicier_gb300.learned import WarmStart
 
 pytestmark = pytest.mark.gpu
@@ -100,3 +100,8 @@ def test_learned_warm_start_cuts_iterations(ctx):
     tol[:, :nn] = 1e-3 * np.abs(xo[:, :nn]) + 1e-6
     tol[:, nn:] = 1e-3 * np.abs(xo[:, nn:]) + 1e-12
     assert np.all(np.abs(xl - xo) <= tol)
+    # the host-buffer entry point runs the same kernels on the same draws
+    cfg8 = abi.newton_config(precision=abi.SP_PREC_MIXED, warm_max_iterations=ws.WARM_MAX_ITERATIONS)
+    h = newton_dc_learned(ctx, circ, ws.mlp, cfg8, 1, N)
+    assert np.array_equal(h.x.view(np.uint64), xl.view(np.uint64))
+    assert np.array_equal(h.iters, il) and np.array_equal(h.status, sl)
