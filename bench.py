@@ -86,6 +86,10 @@ class Clocks:
                  "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.time()  # nvidia-smi takes a moment to start: wait for its first sample
+        while time.time() - t0 < 10 and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+            time.sleep(0.05)
 
     def stop(self):
         if self.proc is None:
@@ -153,18 +157,24 @@ def derived_slots(circuit):
     return cnt
 
 
-def cpu_baseline(circuit, samples, threads=0):
+def cpu_baseline(circuit, samples, threads=0, min_seconds=0.0):
     """The oracle port (the reference algorithm restated in C++) timed on the
-    host cores over one bounded sample of the workload."""
+    host cores over a bounded sample of the workload: chunks of `samples`
+    sweep indices, repeated until `min_seconds` have passed."""
     import oracle
     from spicier_gb300 import abi
     oracle.lib()
     cfg = abi.newton_config(precision=abi.SP_PREC_FP64)
-    t0 = time.perf_counter()
-    _x, _it, st, _p = oracle.newton_dc(circuit, cfg, SEED, samples, threads=threads)
-    dt = time.perf_counter() - t0
-    conv = int(((st & 0x0F) == 0).sum())
-    return conv / dt, dt, conv
+    dt, conv, done = 0.0, 0, 0
+    while True:
+        t0 = time.perf_counter()
+        _x, _it, st, _p = oracle.newton_dc(circuit, cfg, SEED, samples, first=done, threads=threads)
+        dt += time.perf_counter() - t0
+        conv += int(((st & 0x0F) == 0).sum())
+        done += samples
+        if dt >= min_seconds:
+            break
+    return conv / dt, dt, conv, done
 
 
 def run_reference(args):
@@ -175,12 +185,12 @@ def run_reference(args):
     circ = configs.miller_opamp()
     cores = os.cpu_count() or 1
     sample = min(args.samples, 65536)
-    steps = max(1, min(args.steps, 50))
+    steps = max(1, args.steps)
     for _ in range(max(args.warmup, 0)):
         cpu_baseline(circ, sample)
     total_t, total_conv = 0.0, 0
     for _ in range(steps):
-        _r, dt, conv = cpu_baseline(circ, sample)
+        _r, dt, conv, _done = cpu_baseline(circ, sample)
         total_t += dt
         total_conv += conv
     value = total_conv / total_t if total_t > 0 else 0.0
@@ -432,10 +442,10 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        r, dt, _ = cpu_baseline(circ, N)
+        r, dt, _, done = cpu_baseline(circ, N, min_seconds=10.0)
         cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": f"{N} op-amp Monte Carlo samples (one step), plain FP64 Newton from the nodeset, "
-                         f"{dt:.2f} s on all host threads"}
+               "sample": f"{done} op-amp Monte Carlo samples ({N}-sample chunks), plain FP64 Newton from the "
+                         f"nodeset, {dt:.1f} s on all host threads"}
 
     if rank == 0:
         def arm(r):

@@ -36,6 +36,7 @@ def build(force: bool = False) -> str:
     srcs = [os.path.join(HERE, s) for s in SOURCES]
     deps = srcs + [os.path.join(HERE, h) for h in HEADERS if os.path.exists(os.path.join(HERE, h))]
     deps.append(os.path.join(HERE, "..", "include", "spicier_gb300.h"))
+    deps += [os.path.join(HERE, "..", "spicier_gb300", "csrc", h) for h in ("cr_math.cuh", "cr_tables.h")]
     if not force and os.path.exists(LIB_PATH):
         mt = os.path.getmtime(LIB_PATH)
         if all(os.path.getmtime(d) <= mt for d in deps):
@@ -82,11 +83,43 @@ def _bind(L):
         "or_newton_dc": (i32, [P(abi.SpCircuit), P(abi.SpNewtonConfig), u64, u64, u64, P(d), u32,
                                P(d), P(d), P(C.c_int32), P(C.c_uint8), P(d), i32]),
         "or_moments": (None, [P(d), u64, u32, u32, P(C.c_uint8), P(abi.SpMoments)]),
+        "or_set_math_mode": (None, [i32]),
+        "or_get_math_mode": (i32, []),
+        "or_cr_log": (d, [d, P(C.c_uint)]),
+        "or_cr_cos": (d, [d, P(C.c_uint)]),
+        "or_cr_log_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
+        "or_cr_cos_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
         f.restype, f.argtypes = res, args
     return L
+
+
+class math_mode:
+    """Context manager selecting the Gaussian draw's ln/cos: "libm" (the host
+    libm, the reference's behaviour) or "cr" (the correctly rounded functions
+    of the GPU kernels)."""
+
+    def __init__(self, mode: str):
+        self.mode = {"libm": 0, "cr": 1}[mode]
+
+    def __enter__(self):
+        self.prev = lib().or_get_math_mode()
+        lib().or_set_math_mode(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        lib().or_set_math_mode(self.prev)
+
+
+def cr_batch(fn: str, x):
+    """(values, hard count) of the host build of cr_log / cr_cos over x."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    hard = C.c_uint(0)
+    getattr(lib(), f"or_cr_{fn}_batch")(_dp(x), x.size, _dp(y), C.byref(hard))
+    return y, hard.value
 
 
 def _dp(a):

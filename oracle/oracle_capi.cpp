@@ -48,6 +48,16 @@ double or_uniform(uint64_t seed, uint32_t s, uint32_t p) { return uniform(seed, 
 float or_uniform_f32(uint64_t seed, uint32_t s, uint32_t p) { return uniform_f32(seed, s, p); }
 double or_gaussian(uint64_t seed, uint32_t s, uint32_t p) { return gaussian(seed, s, p); }
 float or_gaussian_f32(uint64_t seed, uint32_t s, uint32_t p) { return gaussian_f32(seed, s, p); }
+void or_set_math_mode(int mode) { math_mode() = mode; }
+int or_get_math_mode() { return math_mode(); }
+double or_cr_log(double x, unsigned* hard) { return sp::cr_log(x, hard); }
+double or_cr_cos(double x, unsigned* hard) { return sp::cr_cos(x, hard); }
+void or_cr_log_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
+    for (uint64_t i = 0; i < n; ++i) y[i] = sp::cr_log(x[i], hard);
+}
+void or_cr_cos_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
+    for (uint64_t i = 0; i < n; ++i) y[i] = sp::cr_cos(x[i], hard);
+}
 
 // kind: 0 uniform, 1 gaussian, 2 uniform_f32, 3 gaussian_f32 (sp_rng_fill_device).
 void or_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t param, uint64_t count,

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../include/spicier_gb300.h"
+#include "../spicier_gb300/csrc/cr_math.cuh"
 
 namespace oracle {
 
@@ -51,12 +52,24 @@ inline float uniform_f32(uint64_t seed, uint32_t sweep, uint32_t param) {
 
 constexpr double PI = 3.14159265358979323846;  // std::f64::consts::PI
 
-// rng.rs:120-131, using the host libm (glibc on Linux) like Rust's f64::ln/cos.
+// ln and cos of the Gaussian draw.  Mode 0 (default): the host libm, as
+// Rust's f64::ln/cos call it (glibc on Linux), i.e. the reference's own bits.
+// Mode 1: the correctly rounded integer fixed-point functions the GPU kernels
+// use (cr_math.cuh, pinned against 400-bit mpmath by the tests), which agree
+// with glibc wherever glibc rounds correctly.
+inline int& math_mode() {
+    static int mode = 0;
+    return mode;
+}
+
+// rng.rs:120-131
 inline double gaussian(uint64_t seed, uint32_t sweep, uint32_t param) {
     double u1 = uniform(seed, sweep, param * 2u);
     double u2 = uniform(seed, sweep, param * 2u + 1u);
     u1 = std::fmax(u1, 1e-10);
-    return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * PI * u2);
+    const double t = 2.0 * PI * u2;
+    if (math_mode() == 1) return std::sqrt(-2.0 * sp::cr_log(u1, nullptr)) * sp::cr_cos(t, nullptr);
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(t);
 }
 
 // rng.rs:138-145

@@ -1,21 +1,275 @@
-// ln and cos for the Box-Muller transform of the hash RNG.
+// Correctly rounded ln and cos for the Box-Muller transform of the hash RNG,
+// evaluated in 128-bit integer fixed point.
+//
+// The reference draws z = sqrt(-2 ln u1) cos(2 pi u2) with the host libm
+// (crates/spicier-batched-sweep/src/rng.rs:120-131), whose ln and cos are not
+// correctly rounded; two libms (or glibc and CUDA) disagree in the last bit of
+// a few percent of draws.  These functions return the correctly rounded
+// result instead, so device and host give the same bits, and they agree with
+// any libm wherever that libm rounds correctly.
+//
+// Why integers: GB300 issues FP64 at about 1/60 of its FP32/INT32 rate, so a
+// double-double evaluation would be several times slower than this one, which
+// runs on the integer pipe (64-bit limbs, 64x64->128 products).
+//
+// Formats: ln works in Q8.120 (value = integer * 2^-120), cos in Q3.125.
+// Every evaluation carries an absolute error bound err (in units of the last
+// bit).  The conversion to double rounds to nearest-even and adds one to
+// *hard whenever the exact value, known only to +-err units, could lie on the
+// other side of a rounding midpoint.  A result is correctly rounded whenever
+// *hard is left unchanged.  The domains cover the Box-Muller arguments with
+// room to spare: ln takes x in [2^-360, 2^360), cos takes |t| < 8; any other
+// input (zero, negative, NaN, Inf, out of range) returns NaN and counts as
+// hard.
+//
+// ln x  = e ln 2 + (-ln c_i) + ln(1 + r),  x = m 2^e, m in [1, 2),
+//         c_i ~ 1/m from the top 8 mantissa bits, r = m c_i - 1 in [0, 2^-8)
+//         exact; ln(1+r) by its Taylor series (15 terms, Horner, the inner
+//         8 levels in Q0.64).  Within 2^-16 of 1 the series runs in
+//         d = |x - 1| instead, relative to d (ln_near1).
+// cos t = +-cos a or +-sin a,  a = |t - k pi/2| <= pi/4,  a = j/128 + d,
+//         cos/sin(j/128) from the table, cos/sin(d) by Taylor series in d^2.
 #pragma once
-#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "cr_tables.h"
 
 #ifndef SP_HD
+#if defined(__CUDACC__)
 #define SP_HD __host__ __device__ __forceinline__
+#else
+#define SP_HD inline
+#endif
 #endif
 
 namespace sp {
+namespace cr {
 
-SP_HD double cr_log(double x, unsigned* hard) {
-    (void)hard;
-    return log(x);
+typedef unsigned __int128 u128;
+
+struct LnRow {
+    uint64_t c, th, tl, pad;
+};
+struct CosRow {
+    uint64_t ch, cl, sh, sl;
+};
+struct W2 {
+    uint64_t hi, lo;
+};
+
+#if defined(__CUDACC__)
+__device__ const LnRow kLnRowsDev[256] = SP_CR_LN_ROWS;
+__device__ const CosRow kCosRowsDev[102] = SP_CR_COS_ROWS;
+#endif
+static const LnRow kLnRowsHost[256] = SP_CR_LN_ROWS;
+static const CosRow kCosRowsHost[102] = SP_CR_COS_ROWS;
+
+SP_HD LnRow ln_row(int i) {
+#if defined(__CUDA_ARCH__)
+    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(&kLnRowsDev[i]);
+    const ulonglong2 a = __ldg(p), b = __ldg(p + 1);
+    return LnRow{a.x, a.y, b.x, b.y};
+#else
+    return kLnRowsHost[i];
+#endif
 }
 
-SP_HD double cr_cos(double x, unsigned* hard) {
-    (void)hard;
-    return cos(x);
+SP_HD CosRow cos_row(int j) {
+#if defined(__CUDA_ARCH__)
+    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(&kCosRowsDev[j]);
+    const ulonglong2 a = __ldg(p), b = __ldg(p + 1);
+    return CosRow{a.x, a.y, b.x, b.y};
+#else
+    return kCosRowsHost[j];
+#endif
+}
+
+SP_HD u128 mk(uint64_t hi, uint64_t lo) { return ((u128)hi << 64) | lo; }
+SP_HD u128 mk(W2 w) { return mk(w.hi, w.lo); }
+SP_HD uint64_t hi64(u128 v) { return (uint64_t)(v >> 64); }
+SP_HD uint64_t lo64(u128 v) { return (uint64_t)v; }
+
+SP_HD int clz64(uint64_t v) {
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)v);
+#else
+    return v ? __builtin_clzll(v) : 64;
+#endif
+}
+
+SP_HD int bitlen(u128 v) {
+    const uint64_t h = hi64(v);
+    return h ? 128 - clz64(h) : 64 - clz64(lo64(v));
+}
+
+SP_HD uint64_t dbits(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+
+SP_HD double bdouble(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+
+// (a * b) >> F for unsigned fixed-point a, b (F in 65..127); the 256-bit
+// product is formed exactly and truncated, so the error is below one unit.
+template <int F>
+SP_HD u128 mulq(u128 a, u128 b) {
+    const uint64_t a0 = lo64(a), a1 = hi64(a), b0 = lo64(b), b1 = hi64(b);
+    const u128 p00 = (u128)a0 * b0, p01 = (u128)a0 * b1, p10 = (u128)a1 * b0, p11 = (u128)a1 * b1;
+    const u128 mid = (u128)hi64(p00) + lo64(p01) + lo64(p10);
+    const u128 top = p11 + hi64(p01) + hi64(p10) + hi64(mid);
+    constexpr int s = F - 64;
+    return (top << (64 - s)) | (lo64(mid) >> s);
+}
+
+// (r0 * h) >> 68: r = r0 2^-68 times a Q8.120 value, below one unit of error.
+SP_HD u128 mul_r68(uint64_t r0, u128 h) {
+    const u128 p0 = (u128)r0 * lo64(h), p1 = (u128)r0 * hi64(h);
+    return (p1 + hi64(p0)) >> 4;
+}
+
+// v 2^-F rounded to nearest-even as a positive double (v needs at least 54
+// significant bits, which every caller guarantees); counts an undecided
+// rounding in *hard.
+SP_HD double round_fixed(u128 v, int F, uint64_t err, unsigned* hard) {
+    const int n = bitlen(v);
+    const int w = n - 53;
+    const uint64_t m = (uint64_t)(v >> w);
+    const u128 rem = v & (((u128)1 << w) - 1);
+    const u128 half = (u128)1 << (w - 1);
+    const u128 dist = rem > half ? rem - half : half - rem;
+    if (hard && dist <= err) ++*hard;
+    const uint64_t up = (rem > half || (rem == half && (m & 1))) ? 1 : 0;
+    return bdouble(((uint64_t)(n - 1 - F + 1023) << 52) + (m - (1ULL << 52)) + up);
+}
+
+// ln x for x within 2^-16 of 1, relative to d = |x - 1| (exact): ln(1 +- d)
+// = +-d B with B = 1 -+ d/2 + d^2/3 -+ ... (8 terms), so the result keeps
+// about 2^-118 relative accuracy however close x is to 1, where the general
+// path's absolute accuracy would not decide the rounding of ln(1 - k 2^-53).
+SP_HD double ln_near1(double x, unsigned* hard) {
+    const bool below = x < 1.0;
+    const double dd = below ? 1.0 - x : x - 1.0;  // exact (Sterbenz)
+    const uint64_t b = dbits(dd);
+    const int bexp = (int)(b >> 52);  // dd >= 2^-53: normal
+    const uint64_t m = (1ULL << 52) | (b & ((1ULL << 52) - 1));
+    const u128 d = (u128)m << (bexp - 1075 + 120);  // Q8.120, exact: d < 2^-16
+    const W2 inv128[6] = SP_CR_LN_INV128;             // 1/2 .. 1/7
+    u128 g = (u128)1 << 117;                          // 1/8
+    const u128 one = (u128)1 << 120;
+    if (below) {
+#pragma unroll
+        for (int j = 5; j >= 0; --j) g = mk(inv128[j]) + mulq<120>(d, g);
+        g = one + mulq<120>(d, g);
+    } else {
+#pragma unroll
+        for (int j = 5; j >= 0; --j) g = mk(inv128[j]) - mulq<120>(d, g);
+        g = one - mulq<120>(d, g);
+    }
+    // |ln x| = m 2^(bexp-1075) B: the 174-bit product m B, shifted right by 48
+    const u128 p0 = (u128)m * lo64(g), p1 = (u128)m * hi64(g);
+    const u128 w12 = p1 + hi64(p0);  // bits 64.. of m B
+    const u128 v = (w12 << 16) | (lo64(p0) >> 48);
+    const double r = round_fixed(v, 1147 - bexp, 80, hard);
+    return below ? -r : r;
+}
+
+SP_HD double out_of_domain(unsigned* hard) {
+    if (hard) ++*hard;
+    return bdouble(0x7ff8000000000000ULL);
+}
+
+}  // namespace cr
+
+// Correctly rounded natural logarithm (see the header comment for the domain).
+SP_HD double cr_log(double x, unsigned* hard) {
+    using namespace cr;
+    const uint64_t b = dbits(x);
+    const int bexp = (int)(b >> 52);  // sign bit included: negative x lands above 2047
+    if (bexp < 1023 - 360 || bexp > 1023 + 359) return out_of_domain(hard);
+    if (x > 1.0 - 0x1p-16 && x < 1.0 + 0x1p-16) return x == 1.0 ? 0.0 : ln_near1(x, hard);
+    const int e = bexp - 1023;
+    const uint64_t frac = b & ((1ULL << 52) - 1);
+    const LnRow row = ln_row((int)(frac >> 44));
+    const uint64_t r0 = ((1ULL << 52) | frac) * row.c;  // m c_i 2^68 - 2^68, exact (< 2^61)
+    // Horner for ln(1+r) = r (1 - r (1/2 - r (1/3 - ... r/15)))
+    const uint64_t r64 = r0 >> 4;
+    const uint64_t inv64[8] = SP_CR_LN_INV64;  // 1/8 .. 1/15, Q0.64
+    uint64_t h = inv64[7];
+#pragma unroll
+    for (int j = 6; j >= 0; --j) h = inv64[j] - (uint64_t)(((u128)r64 * h) >> 64);
+    const W2 inv128[6] = SP_CR_LN_INV128;  // 1/2 .. 1/7, Q8.120
+    u128 H = (u128)h << 56;
+#pragma unroll
+    for (int j = 5; j >= 0; --j) H = mk(inv128[j]) - mul_r68(r0, H);
+    const u128 l1 = ((u128)r0 << 52) - mul_r68(r0, mul_r68(r0, H));
+    const u128 lnm = mk(row.th, row.tl) + l1;  // ln m, in [0, ln 2)
+    const W2 ln2w = {SP_CR_LN2};
+    const uint64_t ae = (uint64_t)(e < 0 ? -e : e);
+    const u128 eln2 = mk(ln2w) * ae;
+    const uint64_t err = 8 + ((ae + 1) >> 1);
+    if (e >= 0) return round_fixed(eln2 + lnm, 120, err, hard);
+    return -round_fixed(eln2 - lnm, 120, err, hard);
+}
+
+// Correctly rounded cosine (see the header comment for the domain).
+SP_HD double cr_cos(double t, unsigned* hard) {
+    using namespace cr;
+    const uint64_t b = dbits(t) & ~(1ULL << 63);  // cos is even
+    const int bexp = (int)(b >> 52);
+    if (bexp >= 1023 + 3) return out_of_domain(hard);  // |t| >= 8, Inf, NaN
+    // |t| < 2^-27: 1 - t^2/2 lies above the midpoint 1 - 2^-54, so cos rounds to 1
+    if (bexp < 1023 - 27) return 1.0;
+    const double at = bdouble(b);
+    const u128 T = (u128)((1ULL << 52) | (b & ((1ULL << 52) - 1))) << (bexp - 1075 + 125);
+    const int k = (int)(at * 0.63661977236758134 + 0.5);
+    const W2 pio2w = {SP_CR_PIO2};
+    const u128 kp = mk(pio2w) * (uint64_t)k;
+    const bool neg = T < kp;
+    const u128 a = neg ? kp - T : T - kp;
+    int j = (int)(a >> 118);
+    uint64_t err = 16;
+    if (j > 101) {  // cannot happen for |t - k pi/2| <= pi/4 + 2^-40
+        j = 101;
+        err = ~0ULL;
+    }
+    const u128 d = a - ((u128)j << 118);
+    const u128 w = mulq<125>(d, d);
+    const W2 cc[6] = SP_CR_COS_COEF;  // 1/2!, 1/4!, ..., 1/12!
+    const W2 sc[6] = SP_CR_SIN_COEF;  // 1/3!, 1/5!, ..., 1/13!
+    u128 accc = mk(cc[5]), accs = mk(sc[5]);
+#pragma unroll
+    for (int i = 4; i >= 0; --i) {
+        accc = mk(cc[i]) - mulq<125>(w, accc);
+        accs = mk(sc[i]) - mulq<125>(w, accs);
+    }
+    const u128 cm = mulq<125>(w, accc);              // 1 - cos d
+    const u128 sd = d - mulq<125>(d, mulq<125>(w, accs));  // sin d
+    const CosRow row = cos_row(j);
+    const u128 c0 = mk(row.ch, row.cl), s0 = mk(row.sh, row.sl);
+    const int q = k & 3;
+    u128 v;
+    if ((q & 1) == 0)
+        v = c0 - mulq<125>(c0, cm) - mulq<125>(s0, sd);  // cos a
+    else
+        v = s0 - mulq<125>(s0, cm) + mulq<125>(c0, sd);  // sin a
+    // cos t = cos a, -sign(z) sin a, -cos a, sign(z) sin a for q = 0..3
+    const bool negative = (q == 2) || (q == 1 && !neg) || (q == 3 && neg);
+    const double r = round_fixed(v, 125, err, hard);
+    return negative ? -r : r;
 }
 
 }  // namespace sp

@@ -132,7 +132,9 @@ class WarmStart:
         Pc = P[:, self.inputs] - torch.tensor(in_mean, device=dev)
         A = torch.cat([Pc / torch.tensor(in_scale, device=dev), torch.ones((rows, 1), dtype=torch.float64,
                                                                              device=dev)], 1)
-        coef = torch.linalg.solve(A.T @ A, A.T @ x)  # [n_in + 1][n]
+        # Gram matrices on the device, the (n_in+1)^2 solve on the host
+        coef = torch.tensor(np.linalg.solve((A.T @ A).cpu().numpy(), (A.T @ x).cpu().numpy()),
+                            device=dev)  # [n_in + 1][n]
         lin = (coef[:-1] / torch.tensor(in_scale, device=dev)[:, None]).T.contiguous()  # [n][n_in], raw units
         resid_t = x - coef[-1] - Pc @ lin.T
         out_mean = (coef[-1] + resid_t.mean(0)).cpu().numpy()

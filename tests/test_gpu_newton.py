@@ -65,6 +65,20 @@ def test_exact_mode_bitwise_with_shared_params(ctx, name, make, N):
     assert same_bits(r.x, xo), "FP64_EXACT must be bit-identical"
 
 
+@pytest.mark.parametrize("name,make,N", [("cs_nmos", configs.cs_nmos_amp, 4096),
+                                         ("opamp", configs.miller_opamp, 8192)])
+def test_exact_mode_bitwise_device_rng(ctx, name, make, N):
+    """Parameters drawn on the device (correctly rounded Box-Muller) and the
+    FP64_EXACT Newton chain: bit-identical to the oracle in "cr" mode."""
+    circ = make()
+    r = ctx.newton_dc(circ, abi.newton_config(precision=EXACT), seed=3, count=N, first=1000, params=True)
+    with oracle.math_mode("cr"):
+        xo, io, so, po = oracle.newton_dc(circ, abi.newton_config(), seed=3, count=N, first=1000)
+    assert np.array_equal(r.params.view(np.uint64), po.view(np.uint64))
+    assert np.array_equal(r.status, so) and np.array_equal(r.iters, io)
+    assert same_bits(r.x, xo)
+
+
 @pytest.mark.parametrize("prec", [FAST, EXACT])
 def test_fp64_parity_device_rng(ctx, prec):
     circ = configs.miller_opamp()
