@@ -386,8 +386,8 @@ def main():
             "peak_source": "FP64 FMA-pipe throughput measured on this pool's GB300 (profiles/pipe_peaks_gb300.txt)"}
     if "mlp_warm_start" in kavg:
         ms = kavg["mlp_warm_start"]
-        ni = ws.mlp.n_in
-        fl = 2.0 * (ni * 256 + 2 * 256 * 256 + 256 * n) * N
+        ni, H, nl = ws.mlp.n_in, ws.mlp.n_hidden, ws.mlp.n_layers
+        fl = 2.0 * (ni * H + (nl - 1) * H * H + H * n) * N
         a = fl / (ms * 1e-3) / 1e12
         rooflines["mlp_warm_start"] = {"bound": "tensor", "achieved": a, "peak": bf16_peak, "unit": "TFLOP/s",
                                        "frac": a / bf16_peak, "traffic": None, "avg_launch_ms": ms,
@@ -460,7 +460,8 @@ def main():
             "data": "synthetic (hash-RNG Monte Carlo draws on device, seed 1; network trained on seed 7)",
             "config": {"workload": "miller_opamp_mc_dc", "samples_per_step": N, "mna_size": n,
                        "precision": "mixed (FP32 sparse LU, FP64 residual/update/models) + BF16 warm start",
-                       "warm_start": f"MLP {ws.mlp.n_in}->3x256 GELU->{n} + FP64-fitted linear term",
+                       "warm_start": f"MLP {ws.mlp.n_in}->{ws.mlp.n_layers}x{ws.mlp.n_hidden} GELU->{n} "
+                                     "(tcgen05, TMEM) + FP64-fitted linear term",
                        "tolerances": "reltol 1e-3, vntol 1e-6 V, abstol 1e-12 A",
                        "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},

@@ -386,6 +386,22 @@ int sp_mlp_set_io(sp_mlp* mlp, const int32_t* in_slots, const float* in_mean,
  * x0[k] = out_mean[k] + out_scale[k] * y[k] + sum_j lin[k][j] * (p_j - in_mean[j]).
  * The network then only has to learn what is not linear in the inputs. */
 int sp_mlp_set_linear(sp_mlp* mlp, const double* lin);
+/* Inference kernel of the warm start.  AUTO picks the tcgen05 kernel (TMEM
+ * accumulators, weights resident in shared memory) when the shape allows it
+ * (n_in <= 32, n_out <= 32, hidden 64 or 128, 1..4 hidden layers), else the
+ * fused mma.sync kernel (hidden <= 256), else the layer-by-layer GEMMs. */
+enum sp_mlp_kernel {
+    SP_MLP_KERNEL_AUTO = 0,
+    SP_MLP_KERNEL_TCGEN05 = 1,
+    SP_MLP_KERNEL_MMA_SYNC = 2,
+    SP_MLP_KERNEL_LAYERED = 3
+};
+int sp_mlp_set_inference_kernel(sp_mlp* mlp, int kind);
+/* The warm start alone: x0[rows][n_out] (FP64) from per-sample parameters in
+ * structure-of-arrays layout (parameter slot s of sample i at
+ * d_params_soa[s * stride + i]), with the I/O mapping and linear term above. */
+int sp_mlp_warm_start_device(sp_mlp* mlp, const double* d_params_soa, uint64_t stride,
+                             uint64_t rows, double* d_x0, void* stream);
 /* y[rows][n_out] = net(x[rows][n_in]) on normalised FP32 data. */
 int sp_mlp_forward_device(sp_mlp* mlp, const float* d_x, uint64_t rows, float* d_y,
                           void* stream);

@@ -291,6 +291,15 @@ class Mlp:
         arr = None if lin is None else np.ascontiguousarray(lin, dtype=np.float64)
         check(self.ctx._ptr, load().sp_mlp_set_linear(self._ptr, _vp(arr)))
 
+    def set_inference_kernel(self, kind: int):
+        """abi.SP_MLP_KERNEL_{AUTO,TCGEN05,MMA_SYNC,LAYERED} for the warm start."""
+        check(self.ctx._ptr, load().sp_mlp_set_inference_kernel(self._ptr, kind))
+
+    def warm_start_device(self, params_soa, stride, rows, x0, stream=0):
+        """x0[rows][n_out] (FP64) from SoA parameters (slot s of sample i at s*stride+i)."""
+        check(self.ctx._ptr, load().sp_mlp_warm_start_device(self._ptr, _vp(params_soa), stride, rows, _vp(x0),
+                                                             stream))
+
     def forward_device(self, x, rows, y, stream=0):
         check(self.ctx._ptr, load().sp_mlp_forward_device(self._ptr, _vp(x), rows, _vp(y), stream))
 

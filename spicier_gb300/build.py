@@ -23,6 +23,7 @@ UNITS = {
     "kernels_fast.cu": [],
     "newton_static.cu": [],
     "mlp.cu": [],
+    "mlp_tc.cu": [],
     "spec.cu": [],
 }
 EXTRA_UNITS: dict = {}

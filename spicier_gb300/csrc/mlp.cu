@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "mlp_tc.h"
 #include "rng.cuh"
 
 using bf16 = __nv_bfloat16;
@@ -508,6 +509,13 @@ struct sp_mlp {
     float* lin_f32 = nullptr; // the same in FP32 for the fused kernel
     bool has_lin = false;
     bool fused_ready = false;
+    // tcgen05 inference (mlp_tc.cu): packed weight image, gathered biases
+    int kernel_kind = SP_MLP_KERNEL_AUTO;
+    bool tc_dirty = true;     // weights changed since the image was packed
+    void* tc_img = nullptr;
+    float* tc_bias = nullptr;
+    int* tc_err = nullptr;
+    int num_sms = 0;
     float* io = nullptr;      // in_mean[n_in], in_scale[n_in], out_mean[n_out], out_scale[n_out]
     bool io_set = false;
     // activation workspace for `ws_rows` rows
@@ -522,6 +530,10 @@ struct sp_mlp {
     size_t part_elems = 0;
     float* loss = nullptr;
 };
+
+namespace sp {
+bool tc_eligible(const sp_mlp* m);
+}
 
 namespace {
 
@@ -813,7 +825,7 @@ int sp_mlp_destroy(sp_mlp* m) {
     cudaDeviceSynchronize();
     for (void* p : {(void*)m->params, (void*)m->adam_m, (void*)m->adam_v, (void*)m->grads, (void*)m->wt_bf,
                     (void*)m->w_bf, (void*)m->step, (void*)m->io_slots, (void*)m->io, m->ws, (void*)m->lin,
-                    (void*)m->lin_f32})
+                    (void*)m->lin_f32, m->tc_img, (void*)m->tc_bias, (void*)m->tc_err})
         if (p) cudaFree(p);
     delete m;
     return SP_OK;
@@ -836,6 +848,7 @@ int sp_mlp_set_params(sp_mlp* m, const float* host) {
     cudaMemset(m->adam_m, 0, m->nparams * 4);
     cudaMemset(m->adam_v, 0, m->nparams * 4);
     cudaMemset(m->step, 0, 4);
+    m->tc_dirty = true;
     if (refresh_all(m, 0) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return SP_ERR_BACKEND;
     return SP_OK;
 }
@@ -912,6 +925,7 @@ int sp_mlp_train_device(sp_mlp* m, const float* d_x, const float* d_t, uint64_t 
     const uint64_t steps_per_epoch = rows / batch;
     const int total = (int)(steps_per_epoch * epochs);
     ProfScope prof(m->ctx, "mlp_train", st);
+    m->tc_dirty = true;
     for (int ep = 0; ep < epochs; ++ep) {
         cudaMemsetAsync(m->loss, 0, 4, st);
         for (uint64_t s = 0; s < steps_per_epoch; ++s) {
@@ -954,11 +968,75 @@ extern "C" int sp_mlp_set_linear(sp_mlp* m, const double* lin) {
     return SP_OK;
 }
 
+extern "C" int sp_mlp_set_inference_kernel(sp_mlp* m, int kind) {
+    if (!m || kind < SP_MLP_KERNEL_AUTO || kind > SP_MLP_KERNEL_LAYERED) return SP_ERR_INVALID_ARGUMENT;
+    if (kind == SP_MLP_KERNEL_TCGEN05 && !sp::tc_eligible(m))
+        return mlp_fail(m->ctx, SP_ERR_INVALID_DIMENSION,
+                        "tcgen05 inference needs n_in <= 32, n_out <= 32, hidden 64 or 128, 1..4 hidden layers");
+    if (kind == SP_MLP_KERNEL_MMA_SYNC && !(m->H <= FH && m->L <= 9))
+        return mlp_fail(m->ctx, SP_ERR_INVALID_DIMENSION, "the fused mma.sync kernel needs hidden <= 256");
+    std::lock_guard<std::mutex> g(m->ctx->mu);
+    m->kernel_kind = kind;
+    return SP_OK;
+}
+
+extern "C" int sp_mlp_warm_start_device(sp_mlp* m, const double* d_params_soa, uint64_t stride, uint64_t rows,
+                                        double* d_x0, void* stream) {
+    if (!m || !d_params_soa || !d_x0) return SP_ERR_INVALID_ARGUMENT;
+    if (rows == 0) return SP_OK;
+    if (rows > kMaxRows || stride < rows) return mlp_fail(m->ctx, SP_ERR_INVALID_DIMENSION, "bad row count or stride");
+    if (!m->io_set) return mlp_fail(m->ctx, SP_ERR_INVALID_ARGUMENT, "sp_mlp_set_io not called");
+    std::lock_guard<std::mutex> g(m->ctx->mu);
+    cudaSetDevice(m->ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    ProfScope prof(m->ctx, "mlp_warm_start", st);
+    if (sp::mlp_warm_start(m, d_params_soa, (size_t)stride, (int)rows, d_x0, st) != cudaSuccess)
+        return mlp_fail(m->ctx, SP_ERR_BACKEND, "warm-start inference launch");
+    return SP_OK;
+}
+
 // Warm start for the learned sweep: parameters (SoA) -> network -> x0 (FP64).
 namespace sp {
+bool tc_eligible(const sp_mlp* m) { return mlptc::supported(m->d.n_in, m->d.n_out, m->H, m->L); }
+
+cudaError_t tc_warm_start(sp_mlp* m, const double* params_soa, size_t stride, int rows, double* x0, cudaStream_t st) {
+    mlptc::Args a{};
+    const int img = mlptc::plan(m->d.n_in, m->d.n_out, m->H, m->L, &a);
+    if (!m->tc_img) {
+        cudaError_t e = cudaMalloc(&m->tc_img, img);
+        if (e == cudaSuccess) e = cudaMalloc(&m->tc_bias, 4 * (size_t)a.bias_total);
+        if (e == cudaSuccess) e = cudaMalloc(&m->tc_err, 4);
+        if (e == cudaSuccess) e = cudaMemset(m->tc_err, 0, 4);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
+        if (e != cudaSuccess) return e;
+    }
+    if (m->tc_dirty) {
+        cudaError_t e = mlptc::pack(m->wt_bf, m->woff.data(), a, m->tc_img, st);
+        for (int l = 0; l < m->L && e == cudaSuccess; ++l)
+            e = cudaMemcpyAsync(m->tc_bias + a.layer[l].bias_off, m->params + m->boff[l], 4 * (size_t)a.layer[l].N,
+                                cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+        m->tc_dirty = false;
+    }
+    a.params_soa = params_soa;
+    a.stride = stride;
+    a.rows = rows;
+    a.slots = m->io_slots;
+    a.io = m->io;
+    a.lin = m->has_lin ? m->lin_f32 : nullptr;
+    a.bias = m->tc_bias;
+    a.img = m->tc_img;
+    a.x0 = x0;
+    a.err = m->tc_err;
+    return mlptc::launch(a, m->num_sms, st);
+}
+
 cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, int rows, double* x0,
                            cudaStream_t st) {
-    if (m->H <= FH && m->L <= 9) {
+    const int kind = m->kernel_kind;
+    if (kind == SP_MLP_KERNEL_TCGEN05 || (kind == SP_MLP_KERNEL_AUTO && tc_eligible(m)))
+        return tc_warm_start(m, params_soa, stride, rows, x0, st);
+    if (kind != SP_MLP_KERNEL_LAYERED && m->H <= FH && m->L <= 9) {
         // fused path: activations never leave shared memory
         const size_t smem = (size_t)2 * FT * APITCH * 2 + (size_t)2 * FH * WPITCH * 2 + (size_t)FT * m->d.n_in * 4;
         if (!m->fused_ready) {

@@ -1,0 +1,377 @@
+// Warm-start inference on the 5th-generation tensor cores (tcgen05, TMEM).
+//
+// One persistent CTA per SM keeps the whole network in shared memory: every
+// layer's BF16 weight matrix W[N][K] is packed once, on the device, into the
+// tensor cores' K-major 128-byte-swizzled layout (8-row x 128-byte atoms,
+// 16-byte chunks XOR-ed with the row), so a CTA fills its shared memory with
+// one linear copy.  Two warpgroups each own a 128-sample tile, an activation
+// buffer in the same layout and 128 TMEM columns:
+//
+//   stage inputs  thread t of the warpgroup = sample row t: centred parameters
+//                 (FP32, kept in registers for the FP32 linear term), scaled to
+//                 BF16 and written as row t of the A operand;
+//   per layer     one thread issues K/16 tcgen05.mma (M=128, N=layer width,
+//                 K=16, BF16 x BF16 -> FP32 in TMEM) and commits them to the
+//                 warpgroup's mbarrier; after the wait every thread reads its
+//                 TMEM lane (tcgen05.ld 32x32b), adds the bias, applies GELU
+//                 and writes the BF16 activations back as the next layer's A;
+//   output        x0[k] = out_mean[k] + out_scale[k] y[k]
+//                         + sum_j lin[k][j] (p_j - in_mean[j])    (FP32, then FP64)
+//
+// While one warpgroup runs its epilogue the other's MMAs run, so the tensor
+// cores and the CUDA cores overlap.  Every mbarrier wait is bounded: on a
+// timeout the warpgroup fills its remaining samples' x0 with NaN (the Newton
+// path then restarts those samples cold), raises the error flag, and the CTA
+// frees its TMEM before it returns.
+//
+// Scope: n_in <= 32, n_out <= 32, hidden width 64 or 128, 1..4 hidden layers;
+// the mma.sync kernel in mlp.cu serves every other shape.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "mlp_tc.h"
+
+namespace sp {
+namespace mlptc {
+
+namespace {
+
+constexpr int kTile = 128;     // samples per tile = MMA M
+constexpr int kThreads = 256;  // two warpgroups
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
+// 1024 bytes apart (stride byte offset); the leading byte offset is unused
+// for this layout; bits 46-47 hold the descriptor version (1).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16_ss(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :
+        : "r"(dtmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try(mbar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+
+// Named barrier of one warpgroup that also ANDs a predicate across it.
+__device__ __forceinline__ bool wg_all(int id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.b32 q, %1, 0;\n\t"
+        "bar.red.and.pred p, %2, 128, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// Byte offset of 16-byte chunk c (8 BF16 along K) of row r in a K-major,
+// 128-byte-swizzled operand with `rows` rows: K-blocks of 64 elements are
+// rows*128 bytes apart, 8-row atoms 1024 bytes apart.
+__host__ __device__ __forceinline__ uint32_t sw128_offset(int rows, int r, int c) {
+    return (uint32_t)((c >> 3) * rows * 128 + (r >> 3) * 1024 + (r & 7) * 128 + (((c & 7) ^ (r & 7)) << 4));
+}
+
+__global__ void pack_kernel(const __nv_bfloat16* __restrict__ wt, int N, int K, int Kp, unsigned char* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // one 16-byte chunk
+    const int chunks = Kp / 8;
+    if (i >= N * chunks) return;
+    const int r = i / chunks, c = i % chunks;
+    uint32_t w[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        const int k0 = c * 8 + 2 * h;
+        const __nv_bfloat16 z = __float2bfloat16(0.f);
+        const __nv_bfloat16 a = k0 < K ? wt[(size_t)r * K + k0] : z;
+        const __nv_bfloat16 b = k0 + 1 < K ? wt[(size_t)r * K + k0 + 1] : z;
+        w[h] = (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+    }
+    *reinterpret_cast<uint4*>(dst + sw128_offset(N, r, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// Shared-memory carve-up (byte offsets from the 1024-aligned base).
+struct Carve {
+    uint32_t abuf, bias, lin, io, mbar, tslot, total;
+};
+
+__host__ __device__ inline Carve carve(const Args& a) {
+    Carve c;
+    c.abuf = (uint32_t)a.img_bytes;                       // multiple of 1024
+    c.bias = c.abuf + 2u * kAbytes;
+    c.lin = c.bias + 4u * (uint32_t)a.bias_total;
+    c.io = c.lin + 4u * (uint32_t)(a.n_out * a.n_in);
+    c.mbar = (c.io + 4u * (uint32_t)(2 * (a.n_in + a.n_out)) + 7u) & ~7u;
+    c.tslot = c.mbar + 16u;
+    c.total = c.tslot + 16u;
+    return c;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte alignment of the swizzled operands (the dynamic window may start lower)
+    unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    const Carve cv = carve(a);
+    unsigned char* wimg = sm;
+    float* bias_s = reinterpret_cast<float*>(sm + cv.bias);
+    float* lin_s = reinterpret_cast<float*>(sm + cv.lin);
+    float* io_s = reinterpret_cast<float*>(sm + cv.io);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + cv.mbar);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + cv.tslot);
+
+    const int tid = threadIdx.x, wg = tid >> 7, t = tid & 127, warp = tid >> 5;
+    // weights, biases, linear term, scales into shared memory
+    for (int i = tid; i < a.img_bytes / 16; i += kThreads)
+        reinterpret_cast<uint4*>(wimg)[i] = __ldg(reinterpret_cast<const uint4*>(a.img) + i);
+    for (int i = tid; i < a.bias_total; i += kThreads) bias_s[i] = a.bias[i];
+    for (int i = tid; i < a.n_out * a.n_in; i += kThreads) lin_s[i] = a.lin ? a.lin[i] : 0.f;
+    for (int i = tid; i < 2 * (a.n_in + a.n_out); i += kThreads) io_s[i] = a.io[i];
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = *tmem_slot + (uint32_t)(wg * 128);  // this warpgroup's 128 columns
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    unsigned char* abuf = sm + cv.abuf + wg * kAbytes;
+    const uint32_t abuf_s = smem_u32(abuf), wimg_s = smem_u32(wimg), mb = smem_u32(&mbar[wg]);
+    const int bar_id = 1 + wg;
+    const float* in_mean = io_s;
+    const float* in_scale = io_s + a.n_in;
+    const float* out_mean = io_s + 2 * a.n_in;
+    const float* out_scale = out_mean + a.n_out;
+
+    const int ntiles = (a.rows + kTile - 1) / kTile;
+    uint32_t phase = 0;
+    bool ok = true;
+    int tile = blockIdx.x * 2 + wg;
+    for (; tile < ntiles; tile += gridDim.x * 2) {
+        const int s = tile * kTile + t;
+        const bool live = s < a.rows;
+        // inputs: row t of A, 64 BF16 (inputs 0..n_in-1, zeros after)
+        float pc[kMaxIn];
+#pragma unroll
+        for (int j = 0; j < kMaxIn; ++j)
+            pc[j] = (j < a.n_in && live) ? (float)(a.params_soa[(size_t)a.slots[j] * a.stride + s] - (double)in_mean[j])
+                                         : 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            uint32_t w[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const int j = c * 8 + 2 * h;
+                const float x0v = (j < kMaxIn && j < a.n_in) ? pc[j < kMaxIn ? j : 0] / in_scale[j] : 0.f;
+                const float x1v = (j + 1 < kMaxIn && j + 1 < a.n_in) ? pc[j + 1 < kMaxIn ? j + 1 : 0] / in_scale[j + 1]
+                                                                     : 0.f;
+                w[h] = pack2(x0v, x1v);
+            }
+            *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, t, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        for (int l = 0; l < a.L; ++l) {
+            const Layer& ly = a.layer[l];
+            fence_async_smem();  // generic-proxy writes of A -> visible to the tensor cores
+            tc_before();
+            wg_sync(bar_id);
+            tc_after();
+            if (t == 0) {
+                const uint32_t id = idesc_bf16(ly.N);
+                const uint32_t wb = wimg_s + (uint32_t)ly.img_off;
+                for (int kb = 0; kb < ly.Kp / 64; ++kb)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        mma_bf16_ss(tmem, sdesc(abuf_s + kb * kTile * 128 + k * 32),
+                                    sdesc(wb + kb * ly.N * 128 + k * 32), id, (kb | k) != 0);
+                mma_commit(mb);
+            }
+            ok = wg_all(bar_id, mbar_wait(mb, phase));
+            phase ^= 1;
+            if (!ok) break;
+            tc_after();
+            const float* bias = bias_s + ly.bias_off;
+            if (l + 1 < a.L) {
+                for (int c0 = 0; c0 < ly.N; c0 += 16) {
+                    float v[16];
+                    tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
+                    uint32_t w[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        w[i] = pack2(gelu(v[2 * i] + bias[c0 + 2 * i]), gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
+                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, t, c0 / 8)) = make_uint4(w[0], w[1], w[2], w[3]);
+                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, t, c0 / 8 + 1)) =
+                        make_uint4(w[4], w[5], w[6], w[7]);
+                }
+            } else {
+                for (int c0 = 0; c0 < a.n_out; c0 += 16) {
+                    float v[16];
+                    tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int k = c0 + i;
+                        if (k < a.n_out && live) {
+                            float x = out_mean[k] + out_scale[k] * (v[i] + bias[k]);
+#pragma unroll
+                            for (int j = 0; j < kMaxIn; ++j)
+                                if (j < a.n_in) x = fmaf(lin_s[k * a.n_in + j], pc[j], x);
+                            a.x0[(size_t)s * a.n_out + k] = (double)x;
+                        }
+                    }
+                }
+            }
+            tc_before();
+        }
+        if (!ok) break;
+    }
+    if (!ok) {
+        // timeout: this warpgroup's remaining samples start cold (NaN warm start)
+        if (t == 0) atomicExch(a.err, 1);
+        for (; tile < ntiles; tile += gridDim.x * 2) {
+            const int s = tile * kTile + t;
+            if (s < a.rows)
+                for (int k = 0; k < a.n_out; ++k)
+                    a.x0[(size_t)s * a.n_out + k] = __longlong_as_double(0x7ff8000000000000LL);
+        }
+    }
+    // every MMA this CTA issued has completed (each warpgroup waited on its
+    // commits, or gave up only after the bounded wait)
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(*tmem_slot) : "memory");
+}
+
+}  // namespace
+
+bool supported(int n_in, int n_out, int hidden, int gemm_layers) {
+    return n_in >= 1 && n_in <= kMaxIn && n_out >= 1 && n_out <= 32 && (hidden == 64 || hidden == 128) &&
+           gemm_layers >= 2 && gemm_layers <= kMaxLayers;
+}
+
+int plan(int n_in, int n_out, int hidden, int gemm_layers, Args* a) {
+    int off = 0, boff = 0;
+    a->L = gemm_layers;
+    for (int l = 0; l < gemm_layers; ++l) {
+        Layer& ly = a->layer[l];
+        ly.N = (l == gemm_layers - 1) ? 32 : hidden;  // padded output width (kout)
+        ly.K = (l == 0) ? 32 : hidden;                // padded input width as stored (kin)
+        ly.Kp = (ly.K + 63) & ~63;
+        ly.img_off = off;
+        ly.bias_off = boff;
+        off += ly.N * ly.Kp * 2;
+        boff += ly.N;
+    }
+    a->img_bytes = off;
+    a->bias_total = boff;
+    a->n_in = n_in;
+    a->n_out = n_out;
+    return off;
+}
+
+size_t smem_bytes(const Args& a) { return 1024 + (size_t)carve(a).total; }
+
+cudaError_t pack(const __nv_bfloat16* wt, const size_t* woff, const Args& a, void* img, cudaStream_t st) {
+    for (int l = 0; l < a.L; ++l) {
+        const Layer& ly = a.layer[l];
+        const int n = ly.N * ly.Kp / 8;
+        pack_kernel<<<(n + 255) / 256, 256, 0, st>>>(wt + woff[l], ly.N, ly.K, ly.Kp,
+                                                     static_cast<unsigned char*>(img) + ly.img_off);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch(const Args& a, int num_sms, cudaStream_t st) {
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t smem = smem_bytes(a);
+    if (dev < 64 && !configured[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e != cudaSuccess) return e;
+        configured[dev] = true;
+    }
+    const int ntiles = (a.rows + kTile - 1) / kTile;
+    int grid = (ntiles + 1) / 2;
+    if (grid > num_sms) grid = num_sms;
+    if (grid < 1) return cudaSuccess;
+    infer_kernel<<<grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace mlptc
+}  // namespace sp

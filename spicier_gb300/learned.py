@@ -88,7 +88,7 @@ class TrainReport:
 class WarmStart:
     """The trained network plus its wiring to one circuit."""
 
-    def __init__(self, ctx: Context, circuit: Circuit, n_inputs: int = 10, n_hidden: int = 256, n_layers: int = 3,
+    def __init__(self, ctx: Context, circuit: Circuit, n_inputs: int = 10, n_hidden: int = 128, n_layers: int = 3,
                  seed: int = 0):
         self.ctx, self.circuit = ctx, circuit
         self.n_inputs = n_inputs

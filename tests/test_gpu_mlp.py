@@ -105,3 +105,43 @@ def test_learned_warm_start_cuts_iterations(ctx):
     h = newton_dc_learned(ctx, circ, ws.mlp, cfg8, 1, N)
     assert np.array_equal(h.x.view(np.uint64), xl.view(np.uint64))
     assert np.array_equal(h.iters, il) and np.array_equal(h.status, sl)
+
+
+@pytest.mark.parametrize("H,nl", [(128, 3), (64, 2), (128, 1)])
+def test_inference_kernels_match_oracle(ctx, H, nl):
+    """The tcgen05 warm-start kernel, the fused mma.sync kernel and the
+    layer-by-layer GEMMs against the numpy oracle (same BF16 rounding points),
+    including the I/O mapping and the linear term, on a ragged row count."""
+    n_in, n_out, nslots, rows = 17, 12, 24, 70001
+    m = Mlp(ctx, n_in, n_out, H, nl, seed=21)
+    rng = np.random.default_rng(H + nl)
+    slots = rng.choice(nslots, n_in, replace=False).astype(np.int32)
+    in_mean = rng.normal(0, 1, n_in).astype(np.float32)
+    in_scale = rng.uniform(0.5, 2, n_in).astype(np.float32)
+    out_mean = rng.normal(0, 1, n_out).astype(np.float32)
+    out_scale = rng.uniform(0.1, 1, n_out).astype(np.float32)
+    lin = rng.normal(0, 0.1, (n_out, n_in))
+    m.set_io(slots, in_mean, in_scale, out_mean, out_scale)
+    m.set_linear(lin)
+    P = rng.normal(0, 1, (nslots, rows))
+    dP = torch.tensor(P, device="cuda")
+    layers = m.unflatten(m.get_params())
+    pc = (P[slots].T - in_mean.astype(np.float64)).astype(np.float32)
+    Y, _, _ = mo.forward_backward(layers, pc / in_scale, np.zeros((rows, n_out), np.float32), n_out)
+    ref = out_mean + out_scale * Y[:, :n_out].astype(np.float64) + pc.astype(np.float64) @ lin.T
+    for kind in (abi.SP_MLP_KERNEL_TCGEN05, abi.SP_MLP_KERNEL_MMA_SYNC, abi.SP_MLP_KERNEL_LAYERED):
+        m.set_inference_kernel(kind)
+        x0 = torch.full((rows, n_out), float("nan"), dtype=torch.float64, device="cuda")
+        m.warm_start_device(dP, rows, rows, x0)
+        torch.cuda.synchronize()
+        err = np.abs(x0.cpu().numpy() - ref) / out_scale
+        assert np.isfinite(err).all(), kind
+        assert err.max() < 3e-2 and err.mean() < 2e-3, (kind, err.max(), err.mean())
+    m.close()
+
+
+def test_tcgen05_rejects_unsupported_shape(ctx):
+    m = Mlp(ctx, 17, 12, 256, 3, seed=1)
+    with pytest.raises(sg.SpicierError):
+        m.set_inference_kernel(abi.SP_MLP_KERNEL_TCGEN05)
+    m.close()

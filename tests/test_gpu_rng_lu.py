@@ -44,7 +44,8 @@ def test_gaussian_bit_exact_correctly_rounded(ctx):
         c = rng_cpu(1, 1, 0, 3, n)
     assert np.array_equal(g.view(np.uint64), c.view(np.uint64))
     gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "rng_golden.json")))["gaussian"]
-    block = [w for s, sw, p, w in gold if s == f"{1:016x}" and p == 3 and sw < 4096]
+    block = [w for s, sw, p, w in gold[:4096]]  # the file starts with sweeps 0..4095 of (seed 1, param 3)
+    assert all(s == f"{1:016x}" and p == 3 and sw == i for i, (s, sw, p, _) in enumerate(gold[:4096]))
     want = np.array([struct.unpack(">d", bytes.fromhex(w))[0] for w in block])
     assert np.array_equal(g[:len(want)].view(np.uint64), want.view(np.uint64))
     # the reference's host-libm draws differ only where the libm misrounds
