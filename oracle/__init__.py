@@ -89,6 +89,7 @@ def _bind(L):
         "or_cr_cos": (d, [d, P(C.c_uint)]),
         "or_cr_log_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
         "or_cr_cos_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
+        "or_cr_exp_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -114,7 +115,7 @@ class math_mode:
 
 
 def cr_batch(fn: str, x):
-    """(values, hard count) of the host build of cr_log / cr_cos over x."""
+    """(values, hard count) of the host build of cr_log / cr_cos / cr_exp over x."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.empty_like(x)
     hard = C.c_uint(0)

@@ -3,14 +3,13 @@
 Forward and backward of the BF16 network in numpy with the same rounding
 points as the GPU kernels (spicier_gb300/csrc/mlp.cu): BF16 inputs, weights
 and stored activations (round to nearest even), FP32 accumulation, GELU in
-its exact erf form evaluated on the FP32 pre-activation, GELU' on the stored
+its tanh form evaluated on the FP32 pre-activation, GELU' on the stored
 BF16 pre-activation, BF16 output-gradient.  `exact=True` disables every
 rounding (FP64 throughout) for finite-difference checks of the formulas.
 """
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf
 
 
 def bf16(a: np.ndarray) -> np.ndarray:
@@ -20,12 +19,17 @@ def bf16(a: np.ndarray) -> np.ndarray:
     return ((b + r) & 0xFFFF0000).astype(np.uint32).view(np.float32)
 
 
+_C, _A = np.sqrt(2.0 / np.pi), 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """GELU in its tanh form (the kernels' activation, mlp_act.cuh)."""
+    return 0.5 * z * (1.0 + np.tanh(_C * (z + _A * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(_C * (z + _A * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3.0 * _A * z * z)
 
 
 def pad(a, cols):

@@ -58,6 +58,9 @@ void or_cr_log_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
 void or_cr_cos_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
     for (uint64_t i = 0; i < n; ++i) y[i] = sp::cr_cos(x[i], hard);
 }
+void or_cr_exp_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
+    for (uint64_t i = 0; i < n; ++i) y[i] = sp::cr_exp(x[i], hard);
+}
 
 // kind: 0 uniform, 1 gaussian, 2 uniform_f32, 3 gaussian_f32 (sp_rng_fill_device).
 void or_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t param, uint64_t count,

@@ -93,6 +93,8 @@ inline double draw_param(const sp_param& p, uint64_t seed, uint32_t sweep, const
         case SP_DRAW_GAUSS: return gaussian_scaled(seed, sweep, p.rng_index, p.a, p.b);
         case SP_DRAW_UNIFORM: return p.a + uniform(seed, sweep, p.rng_index) * (p.b - p.a);
         case SP_DRAW_LOGUNIFORM:
+            if (math_mode() == 1)
+                return p.a * sp::cr_exp(uniform(seed, sweep, p.rng_index) * sp::cr_log(p.b / p.a, nullptr), nullptr);
             return p.a * std::exp(uniform(seed, sweep, p.rng_index) * std::log(p.b / p.a));
         case SP_DRAW_TABLE: return table_row ? table_row[p.rng_index] : NAN;
     }

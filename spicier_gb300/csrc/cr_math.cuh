@@ -1,5 +1,5 @@
-// Correctly rounded ln and cos for the Box-Muller transform of the hash RNG,
-// evaluated in 128-bit integer fixed point.
+// Correctly rounded ln, exp and cos for the hash-RNG draws (Box-Muller,
+// log-uniform), evaluated in 128-bit integer fixed point.
 //
 // The reference draws z = sqrt(-2 ln u1) cos(2 pi u2) with the host libm
 // (crates/spicier-batched-sweep/src/rng.rs:120-131), whose ln and cos are not
@@ -30,6 +30,7 @@
 // cos t = +-cos a or +-sin a,  a = |t - k pi/2| <= pi/4,  a = j/128 + d,
 //         cos/sin(j/128) from the table, cos/sin(d) by Taylor series in d^2.
 #pragma once
+#include <math.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -58,12 +59,27 @@ struct W2 {
     uint64_t hi, lo;
 };
 
+struct ExpRow {
+    uint64_t hi, lo;
+};
+
 #if defined(__CUDACC__)
 __device__ const LnRow kLnRowsDev[256] = SP_CR_LN_ROWS;
 __device__ const CosRow kCosRowsDev[102] = SP_CR_COS_ROWS;
+__device__ const ExpRow kExpRowsDev[181] = SP_CR_EXP_ROWS;
 #endif
 static const LnRow kLnRowsHost[256] = SP_CR_LN_ROWS;
 static const CosRow kCosRowsHost[102] = SP_CR_COS_ROWS;
+static const ExpRow kExpRowsHost[181] = SP_CR_EXP_ROWS;
+
+SP_HD ExpRow exp_row(int i) {
+#if defined(__CUDA_ARCH__)
+    const ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2*>(&kExpRowsDev[i]));
+    return ExpRow{a.x, a.y};
+#else
+    return kExpRowsHost[i];
+#endif
+}
 
 SP_HD LnRow ln_row(int i) {
 #if defined(__CUDA_ARCH__)
@@ -223,6 +239,37 @@ SP_HD double cr_log(double x, unsigned* hard) {
     const uint64_t err = 8 + ((ae + 1) >> 1);
     if (e >= 0) return round_fixed(eln2 + lnm, 120, err, hard);
     return -round_fixed(eln2 - lnm, 120, err, hard);
+}
+
+// Correctly rounded exponential for x in [-708, 709] (normal results);
+// |x| < 2^-54 returns 1, other inputs NaN (counted as hard).
+//   exp x = 2^k exp(j/256) exp(d),  x - k ln 2 = j/256 + d,  d in [0, 2^-8),
+// with x - k ln 2 formed exactly in Q12.116 (up to ln 2's rounding, carried
+// in the error bound) and exp(d) - 1 by its 12-term Taylor series.
+SP_HD double cr_exp(double x, unsigned* hard) {
+    using namespace cr;
+    typedef __int128 s128;
+    const uint64_t b = dbits(x);
+    const int bexp = (int)((b >> 52) & 0x7ff);
+    if (bexp < 1023 - 54) return 1.0;  // exp(x) within 2^-54 of 1 rounds to 1
+    if (!(x >= -708.0 && x <= 709.0)) return out_of_domain(hard);
+    const u128 X = (u128)((1ULL << 52) | (b & ((1ULL << 52) - 1))) << (bexp - 1075 + 116);  // |x|, Q12.116
+    const int k = (int)floor(x * 1.4426950408889634 + 0.5);
+    const W2 ln2w = {SP_CR_EXP_LN2};
+    const uint64_t ak = (uint64_t)(k < 0 ? -k : k);
+    const u128 kl = mk(ln2w) * ak;
+    const s128 r = ((b >> 63) ? -(s128)X : (s128)X) - (k < 0 ? -(s128)kl : (s128)kl);
+    const int j = (int)(r >> 108);                            // floor(256 r)
+    const u128 d = (u128)(r - ((s128)j << 108)) << 10;         // Q2.126, [0, 2^-8)
+    const W2 coef[11] = SP_CR_EXP_COEF;                         // 1/2! .. 1/12!
+    u128 acc = mk(coef[10]);
+#pragma unroll
+    for (int i = 9; i >= 0; --i) acc = mk(coef[i]) + mulq<126>(d, acc);
+    const u128 em1 = mulq<126>(d, ((u128)1 << 126) + mulq<126>(d, acc));  // exp(d) - 1
+    const ExpRow row = exp_row(j + 90);
+    const u128 t = mk(row.hi, row.lo);
+    const u128 v = t + mulq<126>(t, em1);
+    return round_fixed(v, 126 - k, 16 + 768 * ak, hard);
 }
 
 // Correctly rounded cosine (see the header comment for the domain).

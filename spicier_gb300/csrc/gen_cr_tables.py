@@ -9,6 +9,7 @@ ln (format Q8.120, value = integer * 2^-120):
   mantissa m in [1 + i/256, 1 + (i+1)/256), r = m c_i - 1 lies in [0, 2^-7.8);
   the table holds C_i = c_i 2^16 and -ln(c_i); plus ln 2 and 1/j (j = 2..7).
   The tail coefficients 1/j (j = 8..15) are Q0.64.
+exp (format Q2.126): exp(j/256) for j = -90..90, ln 2 (Q12.116) and 1/k!.
 cos (format Q3.125):
   cos(j/128) and sin(j/128) for j = 0..101, pi/2, and the Taylor
   coefficients 1/k! of the cos (k = 2..12) and sin (k = 3..13) series.
@@ -19,7 +20,7 @@ import mpmath as mp
 
 mp.mp.prec = 400
 HERE = os.path.dirname(os.path.abspath(__file__))
-F_LN, F_COS = 120, 125
+F_LN, F_COS, F_EXP = 120, 125, 126
 
 
 def fixed(v, frac_bits, total_bits=128):
@@ -80,6 +81,18 @@ def main():
     w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_COS))}}}" for k in range(2, 13, 2)) + " }")
     w("#define SP_CR_SIN_COEF \\")
     w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_COS))}}}" for k in range(3, 14, 2)) + " }")
+    # ---------------------------------------------------------------- exp
+    w("")
+    w("// exp: rows {exp(j/256) hi, lo} for j = -90..90 (Q2.126), ln 2 in Q12.116,")
+    w("// and the Taylor coefficients 1/k! (k = 2..12, Q2.126)")
+    w("#define SP_CR_EXP_ROWS \\")
+    w("    { \\")
+    for j in range(-90, 91):
+        w(f"    {{{words(fixed(mp.exp(mp.mpf(j) / 256), F_EXP))}}}, \\")
+    w("    }")
+    w(f"#define SP_CR_EXP_LN2 {words(fixed(mp.log(2), 116))}")
+    w("#define SP_CR_EXP_COEF \\")
+    w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_EXP))}}}" for k in range(2, 13)) + " }")
     open(os.path.join(HERE, "cr_tables.h"), "w").write("\n".join(out) + "\n")
 
 

@@ -17,7 +17,7 @@ __device__ inline double draw_one(const sp_param& p, uint64_t seed, uint32_t swe
         case SP_DRAW_GAUSS: return p.a + rng_gaussian(seed, sweep, p.rng_index, hard) * p.b;
         case SP_DRAW_UNIFORM: return p.a + rng_uniform(seed, sweep, p.rng_index) * (p.b - p.a);
         case SP_DRAW_LOGUNIFORM:
-            return p.a * exp(rng_uniform(seed, sweep, p.rng_index) * log(p.b / p.a));
+            return p.a * cr_exp(rng_uniform(seed, sweep, p.rng_index) * cr_log(p.b / p.a, hard), hard);
         case SP_DRAW_TABLE: return row ? row[p.rng_index] : CUDART_NAN;
     }
     return CUDART_NAN;

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "mlp_act.cuh"
 #include "mlp_tc.h"
 #include "rng.cuh"
 
@@ -71,11 +72,8 @@ __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// GELU with the exact erf form, and its derivative.
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_grad(float z) {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
-}
+using act::gelu;
+using act::gelu_grad;
 
 template <int EPI>
 __global__ void __launch_bounds__(128) gemm_tn(GemmArgs g) {

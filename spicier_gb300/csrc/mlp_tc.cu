@@ -4,23 +4,24 @@
 // layer's BF16 weight matrix W[N][K] is packed once, on the device, into the
 // tensor cores' K-major 128-byte-swizzled layout (8-row x 128-byte atoms,
 // 16-byte chunks XOR-ed with the row), so a CTA fills its shared memory with
-// one linear copy.  Two warpgroups each own a 128-sample tile, an activation
-// buffer in the same layout and 128 TMEM columns:
+// one linear copy.  Two teams of 256 threads each own a 128-sample tile, an activation
+// buffer in the same layout and 128 TMEM columns; a team is 8 warps, warp w
+// reading TMEM lanes 32 (w % 4).. (its sample rows) and column half w / 4:
 //
-//   stage inputs  thread t of the warpgroup = sample row t: centred parameters
+//   stage inputs  thread t of the team = sample row: centred parameters
 //                 (FP32, kept in registers for the FP32 linear term), scaled to
 //                 BF16 and written as row t of the A operand;
 //   per layer     one thread issues K/16 tcgen05.mma (M=128, N=layer width,
 //                 K=16, BF16 x BF16 -> FP32 in TMEM) and commits them to the
-//                 warpgroup's mbarrier; after the wait every thread reads its
+//                 team's mbarrier; after the wait every thread reads its
 //                 TMEM lane (tcgen05.ld 32x32b), adds the bias, applies GELU
 //                 and writes the BF16 activations back as the next layer's A;
 //   output        x0[k] = out_mean[k] + out_scale[k] y[k]
 //                         + sum_j lin[k][j] (p_j - in_mean[j])    (FP32, then FP64)
 //
-// While one warpgroup runs its epilogue the other's MMAs run, so the tensor
+// While one team runs its epilogue the other's MMAs run, so the tensor
 // cores and the CUDA cores overlap.  Every mbarrier wait is bounded: on a
-// timeout the warpgroup fills its remaining samples' x0 with NaN (the Newton
+// timeout the team fills its remaining samples' x0 with NaN (the Newton
 // path then restarts those samples cold), raises the error flag, and the CTA
 // frees its TMEM before it returns.
 //
@@ -29,6 +30,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include "mlp_act.cuh"
 #include "mlp_tc.h"
 
 namespace sp {
@@ -37,7 +39,8 @@ namespace mlptc {
 namespace {
 
 constexpr int kTile = 128;     // samples per tile = MMA M
-constexpr int kThreads = 256;  // two warpgroups
+constexpr int kTeam = 256;      // threads per tile: 8 warps, two per TMEM lane quarter
+constexpr int kThreads = 512;  // two tiles in flight
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -92,13 +95,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return true;
 }
 
-// Named barrier of one warpgroup that also ANDs a predicate across it.
-__device__ __forceinline__ bool wg_all(int id, bool v) {
+// Named barrier of one team (256 threads) that also ANDs a predicate across it.
+__device__ __forceinline__ bool team_all(int id, bool v) {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\t"
         "setp.ne.b32 q, %1, 0;\n\t"
-        "bar.red.and.pred p, %2, 128, q;\n\t"
+        "bar.red.and.pred p, %2, 256, q;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(r)
         : "r"((uint32_t)v), "r"(id)
@@ -106,7 +109,7 @@ __device__ __forceinline__ bool wg_all(int id, bool v) {
     return r != 0;
 }
 
-__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -126,7 +129,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
 
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
@@ -186,8 +188,10 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + cv.mbar);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + cv.tslot);
 
-    const int tid = threadIdx.x, wg = tid >> 7, t = tid & 127, warp = tid >> 5;
-    // weights, biases, linear term, scales into shared memory
+    // team = tile slot (0/1); warp w of a team reads TMEM lanes 32 (w % 4)..+31
+    // (sample rows) and the column half w / 4 of every layer's output
+    const int tid = threadIdx.x, team = tid / kTeam, tt = tid % kTeam, warp = tid >> 5;
+    const int quarter = (tt >> 5) & 3, half = tt >> 7, row = quarter * 32 + (tid & 31);
     for (int i = tid; i < a.img_bytes / 16; i += kThreads)
         reinterpret_cast<uint4*>(wimg)[i] = __ldg(reinterpret_cast<const uint4*>(a.img) + i);
     for (int i = tid; i < a.bias_total; i += kThreads) bias_s[i] = a.bias[i];
@@ -207,11 +211,11 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
     tc_before();
     __syncthreads();
     tc_after();
-    const uint32_t tmem = *tmem_slot + (uint32_t)(wg * 128);  // this warpgroup's 128 columns
-    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-    unsigned char* abuf = sm + cv.abuf + wg * kAbytes;
-    const uint32_t abuf_s = smem_u32(abuf), wimg_s = smem_u32(wimg), mb = smem_u32(&mbar[wg]);
-    const int bar_id = 1 + wg;
+    const uint32_t tmem = *tmem_slot + (uint32_t)(team * 128);  // this team's 128 columns
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    unsigned char* abuf = sm + cv.abuf + team * kAbytes;
+    const uint32_t abuf_s = smem_u32(abuf), wimg_s = smem_u32(wimg), mb = smem_u32(&mbar[team]);
+    const int bar_id = 1 + team;
     const float* in_mean = io_s;
     const float* in_scale = io_s + a.n_in;
     const float* out_mean = io_s + 2 * a.n_in;
@@ -220,36 +224,43 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
     const int ntiles = (a.rows + kTile - 1) / kTile;
     uint32_t phase = 0;
     bool ok = true;
-    int tile = blockIdx.x * 2 + wg;
+    int tile = blockIdx.x * 2 + team;
     for (; tile < ntiles; tile += gridDim.x * 2) {
-        const int s = tile * kTile + t;
+        const int s = tile * kTile + row;
         const bool live = s < a.rows;
-        // inputs: row t of A, 64 BF16 (inputs 0..n_in-1, zeros after)
+        // inputs: half 0 writes chunks 0..3 of row `row` (inputs 0..31, kept in
+        // registers for the linear term), half 1 the zero chunks 4..7
         float pc[kMaxIn];
 #pragma unroll
         for (int j = 0; j < kMaxIn; ++j)
-            pc[j] = (j < a.n_in && live) ? (float)(a.params_soa[(size_t)a.slots[j] * a.stride + s] - (double)in_mean[j])
-                                         : 0.f;
+            pc[j] = (half == 0 && j < a.n_in && live)
+                        ? (float)(a.params_soa[(size_t)a.slots[j] * a.stride + s] - (double)in_mean[j])
+                        : 0.f;
+        if (half == 0) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            uint32_t w[4];
+            for (int c = 0; c < 4; ++c) {
+                uint32_t w[4];
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                const int j = c * 8 + 2 * h;
-                const float x0v = (j < kMaxIn && j < a.n_in) ? pc[j < kMaxIn ? j : 0] / in_scale[j] : 0.f;
-                const float x1v = (j + 1 < kMaxIn && j + 1 < a.n_in) ? pc[j + 1 < kMaxIn ? j + 1 : 0] / in_scale[j + 1]
-                                                                     : 0.f;
-                w[h] = pack2(x0v, x1v);
+                for (int h = 0; h < 4; ++h) {
+                    const int j = c * 8 + 2 * h;
+                    const float x0v = j < a.n_in ? pc[j] / in_scale[j] : 0.f;
+                    const float x1v = j + 1 < a.n_in ? pc[j + 1] / in_scale[j + 1] : 0.f;
+                    w[h] = pack2(x0v, x1v);
+                }
+                *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(w[0], w[1], w[2], w[3]);
             }
-            *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, t, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+        } else {
+#pragma unroll
+            for (int c = 4; c < 8; ++c)
+                *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(0u, 0u, 0u, 0u);
         }
         for (int l = 0; l < a.L; ++l) {
             const Layer& ly = a.layer[l];
             fence_async_smem();  // generic-proxy writes of A -> visible to the tensor cores
             tc_before();
-            wg_sync(bar_id);
+            team_sync(bar_id);
             tc_after();
-            if (t == 0) {
+            if (tt == 0) {
                 const uint32_t id = idesc_bf16(ly.N);
                 const uint32_t wb = wimg_s + (uint32_t)ly.img_off;
                 for (int kb = 0; kb < ly.Kp / 64; ++kb)
@@ -259,24 +270,27 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
                                     sdesc(wb + kb * ly.N * 128 + k * 32), id, (kb | k) != 0);
                 mma_commit(mb);
             }
-            ok = wg_all(bar_id, mbar_wait(mb, phase));
+            ok = team_all(bar_id, mbar_wait(mb, phase));
             phase ^= 1;
             if (!ok) break;
             tc_after();
             const float* bias = bias_s + ly.bias_off;
             if (l + 1 < a.L) {
-                for (int c0 = 0; c0 < ly.N; c0 += 16) {
+                const int hw = ly.N / 2;
+                for (int c0 = half * hw; c0 < (half + 1) * hw; c0 += 16) {
                     float v[16];
                     tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
                     uint32_t w[8];
 #pragma unroll
                     for (int i = 0; i < 8; ++i)
-                        w[i] = pack2(gelu(v[2 * i] + bias[c0 + 2 * i]), gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
-                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, t, c0 / 8)) = make_uint4(w[0], w[1], w[2], w[3]);
-                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, t, c0 / 8 + 1)) =
+                        w[i] = pack2(act::gelu(v[2 * i] + bias[c0 + 2 * i]),
+                                     act::gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
+                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8)) =
+                        make_uint4(w[0], w[1], w[2], w[3]);
+                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8 + 1)) =
                         make_uint4(w[4], w[5], w[6], w[7]);
                 }
-            } else {
+            } else if (half == 0) {
                 for (int c0 = 0; c0 < a.n_out; c0 += 16) {
                     float v[16];
                     tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
@@ -298,16 +312,16 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
         if (!ok) break;
     }
     if (!ok) {
-        // timeout: this warpgroup's remaining samples start cold (NaN warm start)
-        if (t == 0) atomicExch(a.err, 1);
+        // timeout: this team's remaining samples start cold (NaN warm start)
+        if (tt == 0) atomicExch(a.err, 1);
         for (; tile < ntiles; tile += gridDim.x * 2) {
-            const int s = tile * kTile + t;
-            if (s < a.rows)
+            const int s = tile * kTile + row;
+            if (s < a.rows && half == 0)
                 for (int k = 0; k < a.n_out; ++k)
                     a.x0[(size_t)s * a.n_out + k] = __longlong_as_double(0x7ff8000000000000LL);
         }
     }
-    // every MMA this CTA issued has completed (each warpgroup waited on its
+    // every MMA this CTA issued has completed (each team waited on its
     // commits, or gave up only after the bounded wait)
     tc_before();
     __syncthreads();

@@ -9,9 +9,10 @@ rng_golden.json   hash-RNG draws computed here in pure Python (integers) and
                   draws z = sqrt(-2 ln max(u1, 1e-10)) cos(2pi_d u2), the
                   formula of crates/spicier-batched-sweep/src/rng.rs:120-131
                   with correctly rounded ln and cos.
-cr_math_golden.json  correctly rounded ln and cos at inputs chosen to be hard
-                  for fixed-precision evaluation: ln(1 - k 2^-53), ln(1 + k
-                  2^-52), u1 grid values, and cos next to multiples of pi/2.
+cr_math_golden.json  correctly rounded ln, cos and exp at inputs chosen to be
+                  hard for fixed-precision evaluation: ln(1 - k 2^-53), ln(1 +
+                  k 2^-52), u1 grid values, cos next to multiples of pi/2, exp
+                  of k 2^-53 and of log-uniform exponents.
 
 No reference code runs here: the SplitMix64 finaliser and the index mixing
 are restated from the reference's rng.rs (lines 39-56, 80-85), and every
@@ -96,8 +97,13 @@ def cr_golden():
             coss.append(v)
             v = math.nextafter(v, math.inf)
     coss += [TWO_PI * (rnd.getrandbits(53) * 2.0 ** -53) for _ in range(2000)]
+    exps = [k * 2.0 ** -53 for k in range(-100, 101) if k] + [k * 2.0 ** -40 for k in range(1, 100)]
+    exps += [rnd.uniform(0, 1) * math.log(100.0) for _ in range(1000)]             # log-uniform draws
+    exps += [math.log(1e-12) + rnd.uniform(0, 1) * math.log(100.0) for _ in range(500)]
+    exps += [rnd.uniform(-708, 709) for _ in range(500)] + [-708.0, 709.0, 0.5, -0.5, 1.0]
     return {"log": [[hexbits(x), hexbits(cr(mp.log, x))] for x in logs],
-            "cos": [[hexbits(x), hexbits(cr(mp.cos, x))] for x in coss if x < 8.0]}
+            "cos": [[hexbits(x), hexbits(cr(mp.cos, x))] for x in coss if x < 8.0],
+            "exp": [[hexbits(x), hexbits(cr(mp.exp, x))] for x in exps]}
 
 
 def main():

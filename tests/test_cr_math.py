@@ -27,7 +27,7 @@ def rng_gold():
     return json.load(open(os.path.join(GOLDEN, "rng_golden.json")))
 
 
-@pytest.mark.parametrize("fn", ["log", "cos"])
+@pytest.mark.parametrize("fn", ["log", "cos", "exp"])
 def test_cr_functions_match_golden(cr_gold, fn):
     x = np.array([f(a) for a, _ in cr_gold[fn]])
     want = np.array([f(b) for _, b in cr_gold[fn]])
@@ -53,6 +53,20 @@ def test_cr_functions_random_against_mpmath():
     assert hard == 0
     want = np.array([to_float(mp.cos(mp.mpf(float(v)))._mpf_, rnd="n") for v in t])
     assert np.array_equal(y, want)
+
+
+def test_cr_exp_random_against_mpmath():
+    mp = pytest.importorskip("mpmath")
+    from mpmath.libmp import to_float
+    mp.mp.prec = 300
+    x = np.random.default_rng(12).uniform(-700, 700, 3000)
+    y, hard = oracle.cr_batch("exp", x)
+    assert hard == 0
+    assert np.array_equal(y, [to_float(mp.exp(mp.mpf(float(v)))._mpf_, rnd="n") for v in x])
+    y, hard = oracle.cr_batch("exp", np.array([0.0, -0.0, 1e-300, 2.0 ** -55, -(2.0 ** -55)]))
+    assert (y == 1.0).all() and hard == 0
+    y, hard = oracle.cr_batch("exp", np.array([710.0, -709.0, np.nan, np.inf]))
+    assert np.isnan(y).all() and hard == 4
 
 
 def test_cr_out_of_domain_is_nan_and_hard():
