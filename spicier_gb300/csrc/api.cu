@@ -399,7 +399,7 @@ static int newton_scratch(sp_ctx* ctx, const sp_topology* t, uint64_t count, New
     size_t bd = align256(8 * (size_t)t->num_derived * count);
     size_t bl = align256(4 * count);
     size_t bc = 256;
-    uint32_t mb = (uint32_t)std::min<uint64_t>(256, std::max<uint64_t>(1, count / 1024));
+    uint32_t mb = (uint32_t)std::max<uint64_t>(256, (count + 511) / 512);  // partials per column
     size_t bm = align256(sizeof(sp_moments) * mb * (size_t)t->n);
     size_t bx = want_x0 ? align256(8 * (size_t)t->n * count) : 0;
     int rc = ensure_scratch(ctx, bp + bd + bl + bc + bm + bx);
@@ -671,7 +671,7 @@ int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32
     if (cols > ld) return fail(ctx, SP_ERR_INVALID_DIMENSION, "cols > ld");
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaSetDevice(ctx->device);
-    uint32_t mb = (uint32_t)std::min<uint64_t>(256, std::max<uint64_t>(1, rows / 1024));
+    uint32_t mb = (uint32_t)std::max<uint64_t>(256, (rows + 511) / 512);  // partials per column
     int rc = ensure_scratch(ctx, align256(sizeof(sp_moments) * mb * (size_t)cols));
     if (rc) return rc;
     ScratchOrder order(ctx, (cudaStream_t)stream);

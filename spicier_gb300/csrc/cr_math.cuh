@@ -172,19 +172,19 @@ SP_HD double round_fixed(u128 v, int F, uint64_t err, unsigned* hard) {
     return bdouble(((uint64_t)(n - 1 - F + 1023) << 52) + (m - (1ULL << 52)) + up);
 }
 
-// ln x for x within 2^-16 of 1, relative to d = |x - 1| (exact): ln(1 +- d)
-// = +-d B with B = 1 -+ d/2 + d^2/3 -+ ... (8 terms), so the result keeps
-// about 2^-118 relative accuracy however close x is to 1, where the general
-// path's absolute accuracy would not decide the rounding of ln(1 - k 2^-53).
-SP_HD double ln_near1(double x, unsigned* hard) {
-    const bool below = x < 1.0;
-    const double dd = below ? 1.0 - x : x - 1.0;  // exact (Sterbenz)
-    const uint64_t b = dbits(dd);
-    const int bexp = (int)(b >> 52);  // dd >= 2^-53: normal
-    const uint64_t m = (1ULL << 52) | (b & ((1ULL << 52) - 1));
-    const u128 d = (u128)m << (bexp - 1075 + 120);  // Q8.120, exact: d < 2^-16
-    const W2 inv128[6] = SP_CR_LN_INV128;             // 1/2 .. 1/7
-    u128 g = (u128)1 << 117;                          // 1/8
+// ln x for x within 2^-16 of 1, relative to d = |x - 1| = D 2^-e exactly
+// (e = 53 below 1, 52 above): ln(1 +- d) = +-d B with B = 1 -+ d/2 + d^2/3
+// -+ ... (8 terms), so the result keeps about 2^-118 relative accuracy however
+// close x is to 1, where the general path's absolute accuracy would not decide
+// the rounding of ln(1 - k 2^-53).  Integer operations only.
+SP_HD double ln_near1(uint64_t xb, unsigned* hard) {
+    const bool below = xb < 0x3FF0000000000000ULL;
+    const uint64_t frac = xb & ((1ULL << 52) - 1);
+    const uint64_t D = below ? (1ULL << 52) - frac : frac;  // < 2^37
+    const int e = below ? 53 : 52;
+    const u128 d = (u128)D << (120 - e);                    // Q8.120, exact
+    const W2 inv128[6] = SP_CR_LN_INV128;                    // 1/2 .. 1/7
+    u128 g = (u128)1 << 117;                                 // 1/8
     const u128 one = (u128)1 << 120;
     if (below) {
 #pragma unroll
@@ -195,12 +195,21 @@ SP_HD double ln_near1(double x, unsigned* hard) {
         for (int j = 5; j >= 0; --j) g = mk(inv128[j]) - mulq<120>(d, g);
         g = one - mulq<120>(d, g);
     }
-    // |ln x| = m 2^(bexp-1075) B: the 174-bit product m B, shifted right by 48
-    const u128 p0 = (u128)m * lo64(g), p1 = (u128)m * hi64(g);
-    const u128 w12 = p1 + hi64(p0);  // bits 64.. of m B
-    const u128 v = (w12 << 16) | (lo64(p0) >> 48);
-    const double r = round_fixed(v, 1147 - bexp, 80, hard);
+    // |ln x| = Dn B 2^-(e+z+120) with Dn = D 2^z normalised to 53 bits: the
+    // product Dn B (< 2^174) shifted right by 48 keeps 124+ significant bits
+    const int z = clz64(D) - 11;
+    const uint64_t Dn = D << z;
+    const u128 p0 = (u128)Dn * lo64(g), p1 = (u128)Dn * hi64(g);
+    const u128 v = (p1 << 16) + (p0 >> 48);
+    const double r = round_fixed(v, e + z + 72, 80, hard);
     return below ? -r : r;
+}
+
+// D 2^-53 as a double for an integer D < 2^53 (exact), by integer operations.
+SP_HD double u53_to_double(uint64_t m) {
+    if (m == 0) return 0.0;
+    const int p = 63 - clz64(m);
+    return bdouble(((uint64_t)(1023 + p - 53) << 52) | ((m << (52 - p)) & ((1ULL << 52) - 1)));
 }
 
 SP_HD double out_of_domain(unsigned* hard) {
@@ -216,7 +225,8 @@ SP_HD double cr_log(double x, unsigned* hard) {
     const uint64_t b = dbits(x);
     const int bexp = (int)(b >> 52);  // sign bit included: negative x lands above 2047
     if (bexp < 1023 - 360 || bexp > 1023 + 359) return out_of_domain(hard);
-    if (x > 1.0 - 0x1p-16 && x < 1.0 + 0x1p-16) return x == 1.0 ? 0.0 : ln_near1(x, hard);
+    // x in (1 - 2^-16, 1 + 2^-16): positive doubles order like their bit patterns
+    if (b > 0x3FEFFFE000000000ULL && b < 0x3FF0001000000000ULL) return b == 0x3FF0000000000000ULL ? 0.0 : ln_near1(b, hard);
     const int e = bexp - 1023;
     const uint64_t frac = b & ((1ULL << 52) - 1);
     const LnRow row = ln_row((int)(frac >> 44));
@@ -280,11 +290,14 @@ SP_HD double cr_cos(double t, unsigned* hard) {
     if (bexp >= 1023 + 3) return out_of_domain(hard);  // |t| >= 8, Inf, NaN
     // |t| < 2^-27: 1 - t^2/2 lies above the midpoint 1 - 2^-54, so cos rounds to 1
     if (bexp < 1023 - 27) return 1.0;
-    const double at = bdouble(b);
     const u128 T = (u128)((1ULL << 52) | (b & ((1ULL << 52) - 1))) << (bexp - 1075 + 125);
-    const int k = (int)(at * 0.63661977236758134 + 0.5);
+    // k = the multiple of pi/2 nearest to t (t < 8: k <= 5), by comparisons
     const W2 pio2w = {SP_CR_PIO2};
-    const u128 kp = mk(pio2w) * (uint64_t)k;
+    const u128 pio2 = mk(pio2w);
+    int k = 0;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) k += (T >= pio2 * (uint64_t)m + (pio2 >> 1)) ? 1 : 0;
+    const u128 kp = pio2 * (uint64_t)k;
     const bool neg = T < kp;
     const u128 a = neg ? kp - T : T - kp;
     int j = (int)(a >> 118);

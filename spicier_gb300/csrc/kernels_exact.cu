@@ -23,21 +23,31 @@ __device__ inline double draw_one(const sp_param& p, uint64_t seed, uint32_t swe
     return CUDART_NAN;
 }
 
-__global__ void draw_kernel(DrawLaunch L) {
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= L.count) return;
+// One block = 32 samples x 8 lanes: lane y draws parameter slots y, y+8, ...
+// of its sample (the draws are long integer computations, so eight threads
+// per sample keep the SMs busy), then, after the block barrier, derives the
+// constants of elements y, y+8, ... from the slots the block just wrote.
+constexpr int kDrawSamples = 32, kDrawLanes = 8;
+
+__global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 3) draw_kernel(DrawLaunch L) {
+    const uint64_t s = (uint64_t)blockIdx.x * kDrawSamples + threadIdx.x;
+    const bool live = s < L.count;
     const DevCircuit& c = L.c;
     const uint32_t sweep = (uint32_t)(L.first_index + s);
-    const double* row = L.table ? L.table + s * L.table_cols : nullptr;
+    const double* row = (L.table && live) ? L.table + s * L.table_cols : nullptr;
     unsigned hard = 0;
-    for (int k = 0; k < c.num_params; ++k) {
-        double v = draw_one(c.par[k], L.seed, sweep, row, &hard);
-        L.params_soa[(size_t)k * L.count + s] = v;
-        if (L.params_out) L.params_out[s * c.num_params + k] = v;
+    if (live) {
+        for (int k = threadIdx.y; k < c.num_params; k += kDrawLanes) {
+            const double v = draw_one(c.par[k], L.seed, sweep, row, &hard);
+            L.params_soa[(size_t)k * L.count + s] = v;
+            if (L.params_out) L.params_out[s * c.num_params + k] = v;
+        }
     }
     if (hard && L.hard) atomicAdd(L.hard, hard);
+    __syncthreads();  // this block's parameter slots are written
+    if (!live) return;
     auto P = [&](int slot) { return L.params_soa[(size_t)slot * L.count + s]; };
-    for (int e = 0; e < c.num_elements; ++e) {
+    for (int e = threadIdx.y; e < c.num_elements; e += kDrawLanes) {
         const sp_element el = c.el[e];
         double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
         const size_t st = L.count;
@@ -47,9 +57,8 @@ __global__ void draw_kernel(DrawLaunch L) {
 
 cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st) {
     if (L.count == 0) return cudaSuccess;
-    const int block = 128;
-    const uint64_t grid = (L.count + block - 1) / block;
-    draw_kernel<<<(unsigned)grid, block, 0, st>>>(L);
+    const uint64_t grid = (L.count + kDrawSamples - 1) / kDrawSamples;
+    draw_kernel<<<(unsigned)grid, dim3(kDrawSamples, kDrawLanes), 0, st>>>(L);
     return cudaGetLastError();
 }
 

@@ -7,6 +7,7 @@
 
 #define SP_KERNEL_NS kfast
 #include "internal.h"
+#include <algorithm>
 
 namespace sp {
 
@@ -218,10 +219,56 @@ __global__ void moments_final_kernel(const sp_moments* __restrict__ partial, uin
     out[col] = m;
 }
 
+// Narrow tables (cols <= 32): thread t of a block accumulates column t % cp
+// (cp = cols rounded up to a power of two) over rows t / cp, t / cp + 256 / cp,
+// ... of the block's chunk, so a warp reads whole rows (coalesced); the
+// groups of a column are then merged in a fixed order, and the chunks'
+// partials by the final kernel: the result depends only on rows and cols.
+constexpr int kMomChunk = 512;
+
+__global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
+                                                           uint32_t cols, uint32_t cp,
+                                                           const uint8_t* __restrict__ status,
+                                                           sp_moments* __restrict__ partial) {
+    __shared__ sp_moments sh[256];
+    const uint32_t c = threadIdx.x % cp, g = threadIdx.x / cp, groups = 256 / cp;
+    const uint64_t lo = (uint64_t)blockIdx.x * kMomChunk, hi = min(rows, lo + kMomChunk);
+    sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+    if (c < cols) {
+        for (uint64_t i = lo + g; i < hi; i += groups) {
+            if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+            const double x = v[i * ld + c];
+            m.count += 1;
+            m.sum += x;
+            m.sum_sq += x * x;
+            m.min = fmin(m.min, x);
+            m.max = fmax(m.max, x);
+        }
+    }
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    if (threadIdx.x < cols) {
+        sp_moments t = sh[threadIdx.x];
+        for (uint32_t k = 1; k < groups; ++k) mom_merge(t, sh[k * cp + threadIdx.x]);
+        partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+    }
+}
+
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
                            cudaStream_t st) {
     if (cols == 0) return cudaSuccess;
+    if (cols <= 32 && (rows + kMomChunk - 1) / kMomChunk <= nblocks) {
+        uint32_t cp = 1;
+        while (cp < cols) cp <<= 1;
+        const uint32_t nb = (uint32_t)((rows + kMomChunk - 1) / kMomChunk);
+        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, status, partial);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        moments_final_kernel<<<(cols + 127) / 128, 128, 0, st>>>(partial, nb, cols, out);
+        return cudaGetLastError();
+    }
+    nblocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(nblocks, 256), std::max<uint64_t>(1, rows / 1024));
     dim3 grid(nblocks, cols);
     moments_partial_kernel<<<grid, 256, 0, st>>>(values, rows, ld, cols, status, partial);
     cudaError_t e = cudaGetLastError();

@@ -29,10 +29,11 @@ SP_HD uint64_t combine_indices(uint64_t seed, uint32_t sweep, uint32_t param) {
            ((uint64_t)param * 0x5851f42d4c957f2dULL);
 }
 
-// (h >> 11) * 2^-53: exact (53-bit integer times a power of two).
+// (h >> 11) * 2^-53: exact (53-bit integer times a power of two), built from
+// the integer directly (no FP64 instruction).
 SP_HD double rng_uniform(uint64_t seed, uint32_t sweep, uint32_t param) {
     uint64_t h = splitmix64(combine_indices(seed, sweep, param));
-    return (double)(h >> 11) * 1.1102230246251565e-16;
+    return cr::u53_to_double(h >> 11);
 }
 
 SP_HD float rng_uniform_f32(uint64_t seed, uint32_t sweep, uint32_t param) {
@@ -46,10 +47,12 @@ SP_HD float rng_uniform_f32(uint64_t seed, uint32_t sweep, uint32_t param) {
 SP_HD double rng_gaussian(uint64_t seed, uint32_t sweep, uint32_t param, unsigned* hard) {
     double u1 = rng_uniform(seed, sweep, param * 2u);
     double u2 = rng_uniform(seed, sweep, param * 2u + 1u);
-    u1 = u1 > 1e-10 ? u1 : 1e-10;
-    double l = cr_log(u1, hard);
-    double c = cr_cos(6.283185307179586 * u2, hard);
-    return sqrt(-2.0 * l) * c;
+    // max(u1, 1e-10) on the bit patterns (both non-negative)
+    u1 = cr::dbits(u1) > 0x3DDB7CDFD9D7BDBBULL ? u1 : 1e-10;
+    const double l = cr_log(u1, hard);  // < 0, normal
+    const double c = cr_cos(6.283185307179586 * u2, hard);
+    // -2 l exactly: flip the sign and raise the exponent by one
+    return sqrt(cr::bdouble((cr::dbits(l) ^ (1ULL << 63)) + (1ULL << 52))) * c;
 }
 
 // FP32 variant (rng.rs:138-145): the reference's f32 ln/cos are not pinned
