@@ -158,18 +158,24 @@ SP_HD u128 mul_r68(uint64_t r0, u128 h) {
 }
 
 // v 2^-F rounded to nearest-even as a positive double (v needs at least 54
-// significant bits, which every caller guarantees); counts an undecided
-// rounding in *hard.
+// significant bits, which every caller guarantees), with gradual underflow
+// (subnormal results round at 2^-1074) and overflow to +Inf; counts an
+// undecided rounding in *hard.
 SP_HD double round_fixed(u128 v, int F, uint64_t err, unsigned* hard) {
     const int n = bitlen(v);
-    const int w = n - 53;
+    const int ex = n - 1 - F;                     // exponent of the leading bit
+    if (ex > 1023) return bdouble(0x7FF0000000000000ULL);
+    const bool sub = ex < -1022;
+    const int w = sub ? F - 1074 : n - 53;         // discarded low bits (1..127)
+    if (w >= 128) return 0.0;                      // below half the smallest subnormal
     const uint64_t m = (uint64_t)(v >> w);
     const u128 rem = v & (((u128)1 << w) - 1);
     const u128 half = (u128)1 << (w - 1);
     const u128 dist = rem > half ? rem - half : half - rem;
     if (hard && dist <= err) ++*hard;
     const uint64_t up = (rem > half || (rem == half && (m & 1))) ? 1 : 0;
-    return bdouble(((uint64_t)(n - 1 - F + 1023) << 52) + (m - (1ULL << 52)) + up);
+    if (sub) return bdouble(m + up);               // a carry into bit 52 gives the smallest normal
+    return bdouble(((uint64_t)(ex + 1023) << 52) + (m - (1ULL << 52)) + up);  // a carry may give +Inf
 }
 
 // ln x for x within 2^-16 of 1, relative to d = |x - 1| = D 2^-e exactly
@@ -251,8 +257,9 @@ SP_HD double cr_log(double x, unsigned* hard) {
     return -round_fixed(eln2 - lnm, 120, err, hard);
 }
 
-// Correctly rounded exponential for x in [-708, 709] (normal results);
-// |x| < 2^-54 returns 1, other inputs NaN (counted as hard).
+// Correctly rounded exponential (subnormal results and overflow to +Inf
+// included); |x| < 2^-54 returns 1, x < -746 returns 0, x > 710 +Inf, NaN
+// returns NaN (counted as hard).
 //   exp x = 2^k exp(j/256) exp(d),  x - k ln 2 = j/256 + d,  d in [0, 2^-8),
 // with x - k ln 2 formed exactly in Q12.116 (up to ln 2's rounding, carried
 // in the error bound) and exp(d) - 1 by its 12-term Taylor series.
@@ -262,7 +269,9 @@ SP_HD double cr_exp(double x, unsigned* hard) {
     const uint64_t b = dbits(x);
     const int bexp = (int)((b >> 52) & 0x7ff);
     if (bexp < 1023 - 54) return 1.0;  // exp(x) within 2^-54 of 1 rounds to 1
-    if (!(x >= -708.0 && x <= 709.0)) return out_of_domain(hard);
+    if (x != x) return out_of_domain(hard);
+    if (x < -746.0) return 0.0;
+    if (x > 710.0) return bdouble(0x7FF0000000000000ULL);
     const u128 X = (u128)((1ULL << 52) | (b & ((1ULL << 52) - 1))) << (bexp - 1075 + 116);  // |x|, Q12.116
     const int k = (int)floor(x * 1.4426950408889634 + 0.5);
     const W2 ln2w = {SP_CR_EXP_LN2};
@@ -280,6 +289,16 @@ SP_HD double cr_exp(double x, unsigned* hard) {
     const u128 t = mk(row.hi, row.lo);
     const u128 v = t + mulq<126>(t, em1);
     return round_fixed(v, 126 - k, 16 + 768 * ak, hard);
+}
+
+// log1p for a > -1 from the correctly rounded ln (Goldberg's correction):
+// u = 1 + a rounded, then ln(u) a / (u - 1).  Accurate to about an ulp, not
+// correctly rounded, but built only from cr_log and IEEE operations without
+// contraction, so host and device give the same bits.
+SP_HD double pm_log1p(double a, unsigned* hard) {
+    const double u = 1.0 + a;
+    if (u == 1.0) return a;
+    return cr_log(u, hard) * (a / (u - 1.0));
 }
 
 // Correctly rounded cosine (see the header comment for the domain).

@@ -65,8 +65,21 @@ def test_cr_exp_random_against_mpmath():
     assert np.array_equal(y, [to_float(mp.exp(mp.mpf(float(v)))._mpf_, rnd="n") for v in x])
     y, hard = oracle.cr_batch("exp", np.array([0.0, -0.0, 1e-300, 2.0 ** -55, -(2.0 ** -55)]))
     assert (y == 1.0).all() and hard == 0
-    y, hard = oracle.cr_batch("exp", np.array([710.0, -709.0, np.nan, np.inf]))
-    assert np.isnan(y).all() and hard == 4
+    y, hard = oracle.cr_batch("exp", np.array([710.0, np.inf, -746.5, -np.inf]))
+    assert list(y) == [np.inf, np.inf, 0.0, 0.0] and hard == 0
+    y, hard = oracle.cr_batch("exp", np.array([np.nan]))
+    assert np.isnan(y).all() and hard == 1
+    # gradual underflow: round at 2^-1074 (exact rounding computed here; mpmath's
+    # to_float rounds twice on subnormals)
+    x = np.random.default_rng(13).uniform(-745.1, -708.5, 500)
+    y, hard = oracle.cr_batch("exp", x)
+    assert hard == 0
+    for xi, yi in zip(x, y):
+        m = mp.exp(mp.mpf(float(xi))) * mp.mpf(2) ** 1074
+        r = int(mp.floor(m))
+        f = m - r
+        r += 1 if (f > 0.5 or (f == 0.5 and r % 2)) else 0
+        assert yi == float(mp.mpf(r) * mp.mpf(2) ** -1074)
 
 
 def test_cr_out_of_domain_is_nan_and_hard():

@@ -136,10 +136,10 @@ def test_inference_kernels_match_oracle(ctx, H, nl):
         torch.cuda.synchronize()
         err = np.abs(x0.cpu().numpy() - ref) / out_scale
         assert np.isfinite(err).all(), kind
-        # the SFU tanh (relative error ~2^-11) flips an occasional BF16 rounding
-        # of an activation against the oracle's exact tanh; a layout or
-        # indexing error would be O(1) everywhere
-        assert err.mean() < 2e-3 and np.quantile(err, 0.999) < 1e-2 and err.max() < 0.1, \
+        # FP32 accumulation order and the SFU tanh flip an occasional BF16
+        # rounding of an activation against the oracle; a layout or indexing
+        # error would be O(1) everywhere
+        assert err.mean() < 2e-3 and np.quantile(err, 0.999) < 3e-2 and err.max() < 0.1, \
             (kind, err.max(), err.mean(), np.quantile(err, 0.999))
     m.close()
 
