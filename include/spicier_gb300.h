@@ -218,6 +218,36 @@ typedef struct sp_circuit {
     const double* nodeset;
 } sp_circuit;
 
+/* ---------------------------------------------------------------------- */
+/* Batched nonlinear transient of RC-diode ladders (no counterpart in the  */
+/* reference, whose transient solvers are linear): every instance is a     */
+/* ladder of N sections (R in series, C and a Shockley diode to ground)    */
+/* driven by a PULSE source, integrated with the reference's TR-BDF2 step  */
+/* (companion.rs:41-150, solver.rs:186-251) under the reference's adaptive */
+/* step controller (solver.rs:494-676), each stage solved by Newton with   */
+/* the reference's convergence test (newton.rs:134-159).                   */
+/* ---------------------------------------------------------------------- */
+typedef struct sp_ladder_config {
+    double tstop, h_init, h_min, h_max;  /* AdaptiveTransientParams (types.rs)   */
+    double lte_reltol, lte_abstol;       /* step acceptance tolerance            */
+    double v_reltol, v_abstol, i_abstol; /* Newton convergence per stage         */
+    double r_lo, r_hi, c_lo, c_hi;       /* log-uniform section R and C ranges   */
+    double diode_is, diode_n;            /* Shockley diode of every section      */
+    sp_pulse pulse;                      /* source waveform                      */
+    int32_t min_sections, max_sections;  /* N = min + floor((max-min+1) u)       */
+    int32_t max_iterations;              /* Newton iterations per stage          */
+    int32_t max_steps;                   /* accepted + rejected steps per instance */
+    int32_t precision;                   /* SP_PREC_*                            */
+    int32_t num_probe;                   /* probe samples of v(N) over [0, tstop] */
+} sp_ladder_config;
+
+/* Defaults: 4,096-instance workload values (tstop 100 ns, h_init 1 ns,
+ * h_min 1 fs, h_max tstop/100, reltol 1e-3, abstol 1e-6, SPICE Newton
+ * tolerances, R 100 ohm-10 kohm, C 1-100 pF, IS 1e-14, N 1, PULSE 0->1.8 V
+ * with tr = tf = 1 ns, pw 10 ns, per 20 ns, td 0; N in 8..512; 50 Newton
+ * iterations; 200,000 steps; FP64; 101 probe samples). */
+void sp_ladder_config_default(sp_ladder_config* cfg);
+
 /* ConvergenceCriteria (newton.rs:9-34) + stepping parameters
  * (newton.rs:173-231) + backend choices. */
 enum sp_fallback_bits {

@@ -25,7 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle_spicier.so")
 SOURCES = ["oracle_capi.cpp"]
-HEADERS = ["oracle_core.hpp", "oracle_transient.hpp", "oracle_gmres.hpp"]
+HEADERS = ["transient.hpp", "oracle_core.hpp", "oracle_transient.hpp", "oracle_gmres.hpp"]
 
 _lock = threading.Lock()
 _lib = None
@@ -59,7 +59,7 @@ def lib():
 
 def _bind(L):
     from spicier_gb300 import _abi as abi
-    d, u64, u32, i32 = C.c_double, C.c_uint64, C.c_uint32, C.c_int
+    d, u64, u32, i32, vp_ = C.c_double, C.c_uint64, C.c_uint32, C.c_int, C.c_void_p
     P = C.POINTER
     sig = {
         "or_splitmix64": (u64, [u64]),
@@ -84,6 +84,9 @@ def _bind(L):
                                P(d), P(d), P(C.c_int32), P(C.c_uint8), P(d), i32]),
         "or_moments": (None, [P(d), u64, u32, u32, P(C.c_uint8), P(abi.SpMoments)]),
         "or_set_math_mode": (None, [i32]),
+        "or_ladder_draw": (i32, [vp_, u64, u32, P(d), P(d)]),
+        "or_ladder_transient": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(i32), P(i32), P(C.c_uint8),
+                                       P(d), i32]),
         "or_get_math_mode": (i32, []),
         "or_cr_log": (d, [d, P(C.c_uint)]),
         "or_cr_cos": (d, [d, P(C.c_uint)]),
@@ -168,3 +171,29 @@ def solve_batch(mats, rhs, n, batch, threads=0):
     sing = np.zeros(batch, np.uint8)
     L.or_solve_batch(_dp(mats), _dp(rhs), n, batch, _dp(sol), sing.ctypes.data_as(C.POINTER(C.c_uint8)), threads)
     return sol, sing
+
+
+def ladder_transient(cfg, seed, count, first=0, threads=0):
+    """Oracle ladder transients: dict of x_final[count][max_sections+2], n, accepted,
+    rejected, iterations, status, probe[count][num_probe]."""
+    L = lib()
+    ld = cfg.max_sections + 2
+    x = np.zeros((count, ld))
+    n = np.zeros(count, np.int32)
+    acc = np.zeros(count, np.int32)
+    rej = np.zeros(count, np.int32)
+    it = np.zeros(count, np.int32)
+    st = np.zeros(count, np.uint8)
+    pr = np.zeros((count, max(cfg.num_probe, 1)))
+    i32p = C.POINTER(C.c_int32)
+    L.or_ladder_transient(C.byref(cfg), seed, first, count, _dp(x), n.ctypes.data_as(i32p), acc.ctypes.data_as(i32p),
+                          rej.ctypes.data_as(i32p), it.ctypes.data_as(i32p),
+                          st.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(pr), threads)
+    return dict(x=x, n=n, accepted=acc, rejected=rej, iterations=it, status=st, probe=pr[:, :cfg.num_probe])
+
+
+def ladder_draw(cfg, seed, inst):
+    R = np.zeros(cfg.max_sections)
+    Cc = np.zeros(cfg.max_sections)
+    N = lib().or_ladder_draw(C.byref(cfg), seed, inst, _dp(R), _dp(Cc))
+    return N, R[:N], Cc[:N]

@@ -10,6 +10,7 @@
 #include <thread>
 
 #include "oracle_core.hpp"
+#include "transient.hpp"
 
 
 using namespace oracle;
@@ -200,6 +201,38 @@ void or_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t col,
         m.max = std::fmax(m.max, v);
     }
     *out = m;
+}
+
+// Section draws of ladder instance `inst` (R, C with room for max_sections).
+int or_ladder_draw(const sp_ladder_config* c, uint64_t seed, uint32_t inst, double* R, double* C) {
+    Ladder L = ladder_draw(*c, seed, inst);
+    for (int k = 1; k <= L.N; ++k) {
+        R[k - 1] = 1.0 / L.g[k];
+        C[k - 1] = L.C[k];
+    }
+    return L.N;
+}
+
+// Ladder transients of instances first..first+count-1: x_final[count][max_sections+2],
+// probe[count][num_probe].
+void or_ladder_transient(const sp_ladder_config* c, uint64_t seed, uint64_t first, uint64_t count,
+                         double* x_final, int32_t* n, int32_t* accepted, int32_t* rejected, int32_t* iters,
+                         uint8_t* status, double* probe, int threads) {
+    const int ld = c->max_sections + 2;
+    parallel_for(count, threads, [&](int, uint64_t lo, uint64_t hi) {
+        std::vector<double> pr(std::max(c->num_probe, 1));
+        for (uint64_t i = lo; i < hi; ++i) {
+            Ladder L = ladder_draw(*c, seed, (uint32_t)(first + i));
+            LadderOutcome o = ladder_transient(*c, L, x_final + i * ld, pr.data());
+            for (int k = L.N + 2; k < ld; ++k) x_final[i * ld + k] = 0.0;
+            if (probe) std::copy(pr.begin(), pr.begin() + c->num_probe, probe + i * c->num_probe);
+            n[i] = L.N + 2;
+            accepted[i] = o.accepted;
+            rejected[i] = o.rejected;
+            iters[i] = o.iterations;
+            status[i] = o.status;
+        }
+    });
 }
 
 }  // extern "C"

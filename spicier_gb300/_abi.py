@@ -166,3 +166,29 @@ def newton_config(
     c.src_max_attempts, c.src_initial, c.src_step, c.src_min_step = 5, 0.1, 0.1, 0.01
     c.warm_max_iterations, c.reserved = warm_max_iterations, 0
     return c
+
+
+class SpLadderConfig(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("tstop", "h_init", "h_min", "h_max", "lte_reltol", "lte_abstol",
+                                          "v_reltol", "v_abstol", "i_abstol", "r_lo", "r_hi", "c_lo", "c_hi",
+                                          "diode_is", "diode_n")] + [("pulse", SpPulse)] + [
+        (k, C.c_int32) for k in ("min_sections", "max_sections", "max_iterations", "max_steps", "precision",
+                                 "num_probe")]
+
+
+def ladder_config(**kw) -> SpLadderConfig:
+    """The 4,096-ladder workload's transient settings (AdaptiveTransientParams::
+    for_tstop(100 ns), crates/spicier-solver/src/transient/types.rs:95-118, and
+    the SPICE Newton tolerances); keyword arguments override fields."""
+    c = SpLadderConfig()
+    c.tstop, c.h_init, c.h_min, c.h_max = 100e-9, 1e-9, 1e-15, 100e-9 / 100.0
+    c.lte_reltol, c.lte_abstol = 1e-3, 1e-6
+    c.v_reltol, c.v_abstol, c.i_abstol = 1e-3, 1e-6, 1e-12
+    c.r_lo, c.r_hi, c.c_lo, c.c_hi = 100.0, 10e3, 1e-12, 100e-12
+    c.diode_is, c.diode_n = 1e-14, 1.0
+    c.pulse = SpPulse(0.0, 1.8, 0.0, 1e-9, 1e-9, 10e-9, 20e-9)
+    c.min_sections, c.max_sections, c.max_iterations, c.max_steps = 8, 512, 50, 200000
+    c.precision, c.num_probe = SP_PREC_FP64, 101
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c

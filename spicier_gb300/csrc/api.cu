@@ -153,6 +153,33 @@ int sp_set_config(sp_ctx* ctx, const sp_batch_config* cfg) {
     return SP_OK;
 }
 
+void sp_ladder_config_default(sp_ladder_config* c) {
+    if (!c) return;
+    *c = sp_ladder_config{};
+    c->tstop = 100e-9;
+    c->h_init = 1e-9;
+    c->h_min = 1e-15;
+    c->h_max = c->tstop / 100.0;  // AdaptiveTransientParams::for_tstop
+    c->lte_reltol = 1e-3;
+    c->lte_abstol = 1e-6;
+    c->v_reltol = 1e-3;
+    c->v_abstol = 1e-6;
+    c->i_abstol = 1e-12;
+    c->r_lo = 100.0;
+    c->r_hi = 10e3;
+    c->c_lo = 1e-12;
+    c->c_hi = 100e-12;
+    c->diode_is = 1e-14;
+    c->diode_n = 1.0;
+    c->pulse = sp_pulse{0.0, 1.8, 0.0, 1e-9, 1e-9, 10e-9, 20e-9};
+    c->min_sections = 8;
+    c->max_sections = 512;
+    c->max_iterations = 50;
+    c->max_steps = 200000;
+    c->precision = SP_PREC_FP64;
+    c->num_probe = 101;
+}
+
 void sp_newton_config_default(sp_newton_config* c) {
     if (!c) return;
     std::memset(c, 0, sizeof *c);

@@ -224,7 +224,17 @@ __global__ void moments_final_kernel(const sp_moments* __restrict__ partial, uin
 // ... of the block's chunk, so a warp reads whole rows (coalesced); the
 // groups of a column are then merged in a fixed order, and the chunks'
 // partials by the final kernel: the result depends only on rows and cols.
-constexpr int kMomChunk = 512;
+constexpr int kMomChunk = 256;
+
+// Order-preserving integer key of a double (IEEE bits with the negative half
+// reflected): min/max run on the integer pipe; NaN never reaches here.
+__device__ __forceinline__ long long order_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (long long)(0x8000000000000000ULL - (unsigned long long)b) - 1;
+}
+__device__ __forceinline__ double from_key(long long k) {
+    return __longlong_as_double(k >= 0 ? k : (long long)(0x8000000000000000ULL - (unsigned long long)(k + 1)));
+}
 
 __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
                                                            uint32_t cols, uint32_t cp,
@@ -234,6 +244,7 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
     const uint32_t c = threadIdx.x % cp, g = threadIdx.x / cp, groups = 256 / cp;
     const uint64_t lo = (uint64_t)blockIdx.x * kMomChunk, hi = min(rows, lo + kMomChunk);
     sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+    long long kmin = order_key(CUDART_INF), kmax = order_key(-CUDART_INF);
     if (c < cols) {
         for (uint64_t i = lo + g; i < hi; i += groups) {
             if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
@@ -241,10 +252,13 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
             m.count += 1;
             m.sum += x;
             m.sum_sq += x * x;
-            m.min = fmin(m.min, x);
-            m.max = fmax(m.max, x);
+            const long long k = order_key(x);
+            kmin = k < kmin ? k : kmin;
+            kmax = k > kmax ? k : kmax;
         }
     }
+    m.min = from_key(kmin);
+    m.max = from_key(kmax);
     sh[threadIdx.x] = m;
     __syncthreads();
     if (threadIdx.x < cols) {

@@ -9,7 +9,8 @@
 // reading TMEM lanes 32 (w % 4).. (its sample rows) and column half w / 4:
 //
 //   stage inputs  thread t of the team = sample row: centred parameters
-//                 (FP32, kept in registers for the FP32 linear term), scaled to
+//                 p - in_mean in FP32 (kept in registers for the FP32 linear
+//                 term; relative error ~2^-24 / |p/in_mean - 1|), scaled to
 //                 BF16 and written as row t of the A operand;
 //   per layer     one thread issues K/16 tcgen05.mma (M=128, N=layer width,
 //                 K=16, BF16 x BF16 -> FP32 in TMEM) and commits them to the
@@ -130,6 +131,29 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
 }
 
 
+// FP64 <-> FP32 conversions on the integer pipe (GB300's FP64 pipe issues
+// conversions slowly, and the kernel converts every input and output).
+// Normal numbers only; zeros, subnormals, Inf and NaN take the ordinary path.
+__device__ __forceinline__ float f64_to_f32(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    if (e <= 0 || e >= 255) return __double2float_rn(x);
+    const uint64_t m = b & ((1ULL << 52) - 1);
+    uint32_t f = ((uint32_t)(b >> 32) & 0x80000000u) | ((uint32_t)e << 23) | (uint32_t)(m >> 29);
+    const uint64_t rem = m & ((1ULL << 29) - 1), half = 1ULL << 28;
+    f += (rem > half || (rem == half && (f & 1))) ? 1u : 0u;  // a carry rounds into the exponent
+    return __uint_as_float(f);
+}
+
+__device__ __forceinline__ double f32_to_f64(float x) {
+    const uint32_t f = __float_as_uint(x);
+    const uint32_t e = (f >> 23) & 0xff;
+    if (e == 0 || e == 255) return (double)x;
+    const uint64_t b = ((uint64_t)(f & 0x80000000u) << 32) | ((uint64_t)(e - 127 + 1023) << 52) |
+                       ((uint64_t)(f & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)b);
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&h);
@@ -234,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
 #pragma unroll
         for (int j = 0; j < kMaxIn; ++j)
             pc[j] = (half == 0 && j < a.n_in && live)
-                        ? (float)(a.params_soa[(size_t)a.slots[j] * a.stride + s] - (double)in_mean[j])
+                        ? f64_to_f32(a.params_soa[(size_t)a.slots[j] * a.stride + s]) - in_mean[j]
                         : 0.f;
         if (half == 0) {
 #pragma unroll
@@ -302,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
 #pragma unroll
                             for (int j = 0; j < kMaxIn; ++j)
                                 if (j < a.n_in) x = fmaf(lin_s[k * a.n_in + j], pc[j], x);
-                            a.x0[(size_t)s * a.n_out + k] = (double)x;
+                            a.x0[(size_t)s * a.n_out + k] = f32_to_f64(x);
                         }
                     }
                 }
