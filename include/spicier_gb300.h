@@ -248,6 +248,21 @@ typedef struct sp_ladder_config {
  * iterations; 200,000 steps; FP64; 101 probe samples). */
 void sp_ladder_config_default(sp_ladder_config* cfg);
 
+/* Transients of ladder instances first_index .. first_index + count - 1
+ * (instance i draws its sections from the hash RNG with sweep index i):
+ * x_final[count][max_sections + 2] holds [v_in, v_1..v_N, I_src, 0...] at
+ * tstop, n[i] = N + 2, accepted/rejected steps, Newton iterations summed
+ * over stages, status (SP_ST_*), probe[count][num_probe] = v_N at
+ * j tstop / (num_probe - 1) by linear interpolation between accepted steps. */
+int sp_ladder_transient_device(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed,
+                               uint64_t first_index, uint64_t count, double* d_x_final,
+                               int32_t* d_n, int32_t* d_accepted, int32_t* d_rejected,
+                               int32_t* d_iters, uint8_t* d_status, double* d_probe, void* stream);
+/* Same on host buffers (copies out; synchronises). */
+int sp_ladder_transient(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed, uint64_t first_index,
+                        uint64_t count, double* x_final, int32_t* n, int32_t* accepted,
+                        int32_t* rejected, int32_t* iters, uint8_t* status, double* probe);
+
 /* ConvergenceCriteria (newton.rs:9-34) + stepping parameters
  * (newton.rs:173-231) + backend choices. */
 enum sp_fallback_bits {

@@ -232,6 +232,30 @@ class Context:
     def profile_enable(self, on: bool = True):
         check(self._ptr, load().sp_profile_enable(self._ptr, 1 if on else 0))
 
+    # -- ladder transients -----------------------------------------------------
+    def ladder_transient(self, cfg, seed: int, count: int, first: int = 0) -> dict:
+        """Host-buffer batched RC-diode ladder transients (sp_ladder_transient):
+        dict of x (final state [count][max_sections+2]), n, accepted, rejected,
+        iterations, status, probe [count][num_probe]."""
+        ld = cfg.max_sections + 2
+        out = dict(x=np.zeros((count, ld)), n=np.zeros(count, np.int32), accepted=np.zeros(count, np.int32),
+                   rejected=np.zeros(count, np.int32), iterations=np.zeros(count, np.int32),
+                   status=np.zeros(count, np.uint8), probe=np.zeros((count, max(cfg.num_probe, 1))))
+        check(self._ptr, load().sp_ladder_transient(self._ptr, C.byref(cfg), seed, first, count, _vp(out["x"]),
+                                                    _vp(out["n"]), _vp(out["accepted"]), _vp(out["rejected"]),
+                                                    _vp(out["iterations"]), _vp(out["status"]),
+                                                    _vp(out["probe"]) if cfg.num_probe else None))
+        out["probe"] = out["probe"][:, :cfg.num_probe]
+        return out
+
+    def ladder_transient_device(self, cfg, seed, count, x, n, accepted, rejected, iterations, status, probe=None,
+                                first: int = 0, stream: int = 0):
+        """Device-buffer variant (torch CUDA tensors): x [count][max_sections+2] f64, n/accepted/rejected/
+        iterations int32 [count], status uint8 [count], probe [count][num_probe] f64."""
+        check(self._ptr, load().sp_ladder_transient_device(self._ptr, C.byref(cfg), seed, first, count, _vp(x), _vp(n),
+                                                           _vp(accepted), _vp(rejected), _vp(iterations),
+                                                           _vp(status), _vp(probe), stream))
+
     def profile_read(self) -> dict:
         """{kernel name: (launches, total_ms)} since the last read."""
         from ._lib import SpKernelTime

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "ladder.cuh"
 
 using namespace sp;
 
@@ -742,6 +743,145 @@ int sp_profile_read(sp_ctx* ctx, sp_kernel_time* out, int cap, int* count) {
     }
     ctx->recs.clear();
     *count = k;
+    return SP_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batched RC-diode ladder transients (ladder.cuh)
+// ---------------------------------------------------------------------------
+static int ladder_validate(sp_ctx* ctx, const sp_ladder_config* c, uint64_t count) {
+    if (!c) return SP_ERR_INVALID_ARGUMENT;
+    if (c->min_sections < 2 || c->max_sections < c->min_sections || c->max_sections > 4000)
+        return fail(ctx, SP_ERR_INVALID_DIMENSION, "sections must satisfy 2 <= min <= max <= 4000");
+    if (!(c->tstop > 0) || !(c->h_min > 0) || !(c->h_max >= c->h_min) || !(c->h_init > 0))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad time-step settings");
+    if (!(c->r_lo > 0) || !(c->r_hi >= c->r_lo) || !(c->c_lo > 0) || !(c->c_hi >= c->c_lo) || !(c->diode_is > 0) ||
+        !(c->diode_n > 0))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad element ranges");
+    if (c->max_iterations < 1 || c->max_steps < 1 || c->num_probe < 0)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad iteration, step or probe counts");
+    if (c->precision < SP_PREC_FP64 || c->precision > SP_PREC_FP64_EXACT)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (count > 0xffffffffull) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "more than 2^32 instances");
+    return SP_OK;
+}
+
+struct LadderPlan {
+    int stride;
+    size_t smem;
+    uint64_t blocks;
+    size_t bh, bo, bn, bw;
+    size_t bytes() const { return bh + bo + bn + bw; }
+};
+
+static LadderPlan ladder_plan(const sp_ctx* ctx, const sp_ladder_config* c, uint64_t count) {
+    LadderPlan p;
+    p.stride = (c->max_sections + 2 + 31) & ~31;
+    p.smem = (size_t)4 * 4 * p.stride * 8;  // four warps x (diag, rhs, c', d')
+    const int bpsm = std::max(1, std::min(8, (int)((228 * 1024 - 1024) / (p.smem + 1024))));
+    p.blocks = std::min<uint64_t>((count + 3) / 4, (uint64_t)ctx->num_sms * bpsm);
+    const int bins = c->max_sections - c->min_sections + 1;
+    p.bh = align256(4 * (size_t)bins);
+    p.bo = align256(4 * count);
+    p.bn = 256;
+    p.bw = align256((size_t)p.blocks * 4 * LA_COUNT * p.stride * 8);
+    return p;
+}
+
+static int ladder_locked(sp_ctx* ctx, const sp_ladder_config* c, uint64_t seed, uint64_t first, uint64_t count,
+                         double* d_x, int32_t* d_n, int32_t* d_acc, int32_t* d_rej, int32_t* d_it, uint8_t* d_st,
+                         double* d_probe, size_t extra, cudaStream_t st) {
+    const LadderPlan p = ladder_plan(ctx, c, count);
+    if (p.smem > (size_t)ctx->max_smem) return fail(ctx, SP_ERR_INVALID_DIMENSION, "ladder too long for shared memory");
+    const int stride = p.stride;
+    const size_t smem = p.smem, bh = p.bh, bo = p.bo, bn = p.bn;
+    const uint64_t blocks = p.blocks;
+    int rc = ensure_scratch(ctx, extra + p.bytes());
+    if (rc) return rc;
+    char* b = (char*)ctx->scratch + extra;
+    LadderLaunch L{};
+    L.cfg = *c;
+    L.seed = seed;
+    L.first = first;
+    L.count = count;
+    unsigned int* hist = (unsigned int*)b;
+    L.order = (const uint32_t*)(b + bh);
+    L.next = (unsigned int*)(b + bh + bo);
+    L.ws = (double*)(b + bh + bo + bn);
+    L.stride = stride;
+    L.slots = (int)(blocks * 4);
+    L.x_final = d_x;
+    L.n = d_n;
+    L.accepted = d_acc;
+    L.rejected = d_rej;
+    L.iters = d_it;
+    L.status = d_st;
+    L.probe = d_probe;
+    SP_CUDA(ctx, launch_ladder_prelude(*c, seed, first, count, hist, (uint32_t*)L.order, L.next, st), "ladder order");
+    static const char* names[3] = {"ladder_transient_fp64", "ladder_transient_mixed", "ladder_transient_fp64_exact"};
+    ProfScope prof(ctx, names[c->precision], st);
+    if (c->precision == SP_PREC_FP64_EXACT)
+        SP_CUDA(ctx, launch_ladder_exact(L, (int)blocks, smem, st), "ladder launch");
+    else
+        SP_CUDA(ctx, launch_ladder_fast(L, c->precision, (int)blocks, smem, st), "ladder launch");
+    return SP_OK;
+}
+
+int sp_ladder_transient_device(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed, uint64_t first_index,
+                               uint64_t count, double* d_x_final, int32_t* d_n, int32_t* d_accepted,
+                               int32_t* d_rejected, int32_t* d_iters, uint8_t* d_status, double* d_probe,
+                               void* stream) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    int rc = ladder_validate(ctx, cfg, count);
+    if (rc) return rc;
+    if (count == 0) return SP_OK;
+    if (!d_x_final || !d_n || !d_accepted || !d_rejected || !d_iters || !d_status || (cfg->num_probe && !d_probe))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "missing output buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    return ladder_locked(ctx, cfg, seed, first_index, count, d_x_final, d_n, d_accepted, d_rejected, d_iters,
+                         d_status, cfg->num_probe ? d_probe : nullptr, 0, (cudaStream_t)stream);
+}
+
+int sp_ladder_transient(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed, uint64_t first_index,
+                        uint64_t count, double* x_final, int32_t* n, int32_t* accepted, int32_t* rejected,
+                        int32_t* iters, uint8_t* status, double* probe) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    int rc = ladder_validate(ctx, cfg, count);
+    if (rc) return rc;
+    if (count == 0) return SP_OK;
+    if (!x_final || !n || !accepted || !rejected || !iters || !status || (cfg->num_probe && !probe))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "missing output buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    ScratchOrder order(ctx, st);
+    const size_t ld = (size_t)cfg->max_sections + 2, np = (size_t)cfg->num_probe;
+    const size_t bx = align256(8 * ld * count), bi = align256(4 * count), bs = align256(count),
+                 bp = align256(8 * np * count);
+    const size_t extra = bx + 4 * bi + bs + bp;
+    rc = ensure_scratch(ctx, extra + ladder_plan(ctx, cfg, count).bytes());  // once: the pointers below stay valid
+    if (rc) return rc;
+    char* b = (char*)ctx->scratch;
+    double* dx = (double*)b;
+    int32_t* dn = (int32_t*)(b + bx);
+    int32_t* da = (int32_t*)(b + bx + bi);
+    int32_t* dr = (int32_t*)(b + bx + 2 * bi);
+    int32_t* di = (int32_t*)(b + bx + 3 * bi);
+    uint8_t* ds = (uint8_t*)(b + bx + 4 * bi);
+    double* dp = np ? (double*)(b + bx + 4 * bi + bs) : nullptr;
+    rc = ladder_locked(ctx, cfg, seed, first_index, count, dx, dn, da, dr, di, ds, dp, extra, st);
+    if (rc) return rc;
+    SP_CUDA(ctx, cudaMemcpyAsync(x_final, b, 8 * ld * count, cudaMemcpyDeviceToHost, st), "D2H x");
+    SP_CUDA(ctx, cudaMemcpyAsync(n, b + bx, 4 * count, cudaMemcpyDeviceToHost, st), "D2H n");
+    SP_CUDA(ctx, cudaMemcpyAsync(accepted, b + bx + bi, 4 * count, cudaMemcpyDeviceToHost, st), "D2H accepted");
+    SP_CUDA(ctx, cudaMemcpyAsync(rejected, b + bx + 2 * bi, 4 * count, cudaMemcpyDeviceToHost, st), "D2H rejected");
+    SP_CUDA(ctx, cudaMemcpyAsync(iters, b + bx + 3 * bi, 4 * count, cudaMemcpyDeviceToHost, st), "D2H iterations");
+    SP_CUDA(ctx, cudaMemcpyAsync(status, b + bx + 4 * bi, count, cudaMemcpyDeviceToHost, st), "D2H status");
+    if (np) SP_CUDA(ctx, cudaMemcpyAsync(probe, b + bx + 4 * bi + bs, 8 * np * count, cudaMemcpyDeviceToHost, st), "D2H probe");
+    SP_CUDA(ctx, cudaStreamSynchronize(st), "ladder transient");
     return SP_OK;
 }
 

@@ -30,6 +30,13 @@ struct DrawLaunch {
     unsigned int* hard;   // count of draws whose rounding was undecided (or nullptr)
 };
 
+struct LadderLaunch;
+// Ladder transient launchers (ladder.cuh): 128-thread blocks, one warp per instance.
+cudaError_t launch_ladder_exact(const LadderLaunch& L, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_ladder_fast(const LadderLaunch& L, int precision, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_ladder_prelude(const sp_ladder_config& c, uint64_t seed, uint64_t first, uint64_t count,
+                                  unsigned int* hist, uint32_t* order, unsigned int* next, cudaStream_t st);
+
 // kernels_exact.cu (no FMA contraction)
 cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st);
 cudaError_t launch_newton_exact(const NewtonLaunch& L, bool fallback, int grid, int block, size_t smem,

@@ -5,6 +5,7 @@
 #include <math_constants.h>
 
 #include "rng.cuh"
+#include "ladder.cuh"
 
 namespace sp {
 
@@ -126,12 +127,20 @@ cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, 
     return cudaGetLastError();
 }
 
+cudaError_t launch_ladder_exact(const LadderLaunch& L, int grid, size_t smem, cudaStream_t st) {
+    SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT><<<grid, 128, smem, st>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t prepare_exact_kernels(int max_smem) {
     cudaError_t e;
     e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(lu_batch_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

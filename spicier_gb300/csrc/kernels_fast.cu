@@ -7,6 +7,7 @@
 
 #define SP_KERNEL_NS kfast
 #include "internal.h"
+#include "ladder.cuh"
 #include <algorithm>
 
 namespace sp {
@@ -224,7 +225,7 @@ __global__ void moments_final_kernel(const sp_moments* __restrict__ partial, uin
 // ... of the block's chunk, so a warp reads whole rows (coalesced); the
 // groups of a column are then merged in a fixed order, and the chunks'
 // partials by the final kernel: the result depends only on rows and cols.
-constexpr int kMomChunk = 256;
+constexpr int kMomChunk = 1024;
 
 // Order-preserving integer key of a double (IEEE bits with the negative half
 // reflected): min/max run on the integer pipe; NaN never reaches here.
@@ -261,11 +262,29 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
     m.max = from_key(kmax);
     sh[threadIdx.x] = m;
     __syncthreads();
-    if (threadIdx.x < cols) {
-        sp_moments t = sh[threadIdx.x];
-        for (uint32_t k = 1; k < groups; ++k) mom_merge(t, sh[k * cp + threadIdx.x]);
-        partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+    // pairwise tree over the groups (fixed order; FP64 latency, not count, bounds this)
+    for (uint32_t w = groups / 2; w >= 1; w >>= 1) {
+        if (g < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w * cp]);
+        __syncthreads();
     }
+    if (threadIdx.x < cols) partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
+}
+
+// One block per column: each thread merges partials t, t + 256, ... in order,
+// then a pairwise tree; deterministic for a given partial count.
+__global__ void __launch_bounds__(256) moments_tree_kernel(const sp_moments* __restrict__ partial, uint32_t nblocks,
+                                                           sp_moments* __restrict__ out) {
+    __shared__ sp_moments sh[256];
+    const uint32_t col = blockIdx.x;
+    sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+    for (uint32_t b = threadIdx.x; b < nblocks; b += 256) mom_merge(m, partial[(size_t)col * nblocks + b]);
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = 128; w >= 1; w >>= 1) {
+        if ((int)threadIdx.x < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[col] = sh[0];
 }
 
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
@@ -279,7 +298,7 @@ cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uin
         moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, status, partial);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        moments_final_kernel<<<(cols + 127) / 128, 128, 0, st>>>(partial, nb, cols, out);
+        moments_tree_kernel<<<cols, 256, 0, st>>>(partial, nb, out);
         return cudaGetLastError();
     }
     nblocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(nblocks, 256), std::max<uint64_t>(1, rows / 1024));
@@ -291,8 +310,57 @@ cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uin
     return cudaGetLastError();
 }
 
+// Ladder order, largest first: a histogram of the section counts, its
+// exclusive scan from the largest count down, and a scatter.
+__global__ void ladder_hist_kernel(sp_ladder_config c, uint64_t seed, uint64_t first, uint64_t count,
+                                   unsigned int* hist) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int N = ladder_sections(c, seed, (uint32_t)(first + i));
+    atomicAdd(&hist[c.max_sections - N], 1u);
+}
+
+__global__ void ladder_scan_kernel(unsigned int* hist, int bins) {
+    unsigned int acc = 0;
+    for (int b = 0; b < bins; ++b) {
+        const unsigned int v = hist[b];
+        hist[b] = acc;
+        acc += v;
+    }
+}
+
+__global__ void ladder_order_kernel(sp_ladder_config c, uint64_t seed, uint64_t first, uint64_t count,
+                                    unsigned int* offsets, uint32_t* order) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int N = ladder_sections(c, seed, (uint32_t)(first + i));
+    order[atomicAdd(&offsets[c.max_sections - N], 1u)] = (uint32_t)i;
+}
+
+cudaError_t launch_ladder_prelude(const sp_ladder_config& c, uint64_t seed, uint64_t first, uint64_t count,
+                                  unsigned int* hist, uint32_t* order, unsigned int* next, cudaStream_t st) {
+    const int bins = c.max_sections - c.min_sections + 1;
+    cudaError_t e = cudaMemsetAsync(hist, 0, 4 * (size_t)bins, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(next, 0, 4, st);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)((count + 255) / 256);
+    ladder_hist_kernel<<<grid, 256, 0, st>>>(c, seed, first, count, hist);
+    ladder_scan_kernel<<<1, 1, 0, st>>>(hist, bins);
+    ladder_order_kernel<<<grid, 256, 0, st>>>(c, seed, first, count, hist, order);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ladder_fast(const LadderLaunch& L, int precision, int grid, size_t smem, cudaStream_t st) {
+    if (precision == SP_PREC_MIXED)
+        SP_KERNEL_NS::ladder_kernel<SP_PREC_MIXED><<<grid, 128, smem, st>>>(L);
+    else
+        SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64><<<grid, 128, smem, st>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t prepare_fast_kernels(int max_smem) {
     const void* fns[] = {
+        (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_MIXED>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
         (const void*)lu_batch_mixed_kernel, (const void*)lu_batch_escalate_kernel};
