@@ -263,6 +263,41 @@ int sp_ladder_transient(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed,
                         uint64_t count, double* x_final, int32_t* n, int32_t* accepted,
                         int32_t* rejected, int32_t* iters, uint8_t* status, double* probe);
 
+/* ---------------------------------------------------------------------- */
+/* Corner sweep of a resistive power-grid mesh with MOSFET current sinks,  */
+/* each Newton linear solve by restarted GMRES with Jacobi (right)         */
+/* preconditioning (gmres/real.rs:218-397, preconditioner.rs:43-101).      */
+/* Instance i: layout i / 4 (edge resistances, sink nodes and gate drives   */
+/* from the hash RNG with sweep index i / 4), corner i % 4 (bit 0: all     */
+/* resistances x r_scale_hi else x r_scale_lo; bit 1: all VTO + vto_shift  */
+/* else - vto_shift).  Unknowns: rows x cols node voltages + the VDD       */
+/* branch current; VDD drives corner (0,0), the three other corners are    */
+/* tied to it by straps of conductance strap_g; every sink is a Level-1    */
+/* NMOS from its node to ground with an ideal gate drive VGS.              */
+/* ---------------------------------------------------------------------- */
+typedef struct sp_grid_config {
+    int32_t rows, cols, num_sinks;
+    int32_t max_newton;          /* Newton iterations                      */
+    int32_t restart;             /* GMRES(m)                               */
+    int32_t max_krylov;          /* GMRES iterations per linear solve      */
+    int32_t precision;           /* SP_PREC_FP64 or SP_PREC_MIXED          */
+    int32_t reserved;
+    double r_lo, r_hi;           /* log-uniform branch resistance          */
+    double r_scale_lo, r_scale_hi, vto_shift;
+    double vdd, strap_g;
+    double vgs_lo, vgs_hi;       /* uniform gate drive                     */
+    double vto, kp, lambda, w, l;
+    double v_reltol, v_abstol, i_abstol;  /* Newton convergence            */
+    double krylov_tol;           /* relative residual of each linear solve */
+    double resid_target;         /* final KCL residual bound (A)           */
+} sp_grid_config;
+
+/* Defaults: 64 x 64 mesh, 512 sinks, R 0.5-2 ohm x {0.9, 1.1}, VTO 0.7 V
+ * +- 50 mV, KP 110e-6, LAMBDA 0.04, W/L 5u/0.5u, VGS 0.8-1.2 V, VDD 1 V,
+ * straps 1e3 S, GMRES(30), 1e-9 relative linear tolerance, 20,000 Krylov
+ * iterations per solve, 30 Newton iterations, residual target 1e-9 A. */
+void sp_grid_config_default(sp_grid_config* cfg);
+
 /* ConvergenceCriteria (newton.rs:9-34) + stepping parameters
  * (newton.rs:173-231) + backend choices. */
 enum sp_fallback_bits {

@@ -25,7 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle_spicier.so")
 SOURCES = ["oracle_capi.cpp"]
-HEADERS = ["transient.hpp", "oracle_core.hpp", "oracle_transient.hpp", "oracle_gmres.hpp"]
+HEADERS = ["transient.hpp", "powergrid.hpp", "oracle_core.hpp", "oracle_transient.hpp", "oracle_gmres.hpp"]
 
 _lock = threading.Lock()
 _lib = None
@@ -85,6 +85,8 @@ def _bind(L):
         "or_moments": (None, [P(d), u64, u32, u32, P(C.c_uint8), P(abi.SpMoments)]),
         "or_set_math_mode": (None, [i32]),
         "or_ladder_draw": (i32, [vp_, u64, u32, P(d), P(d)]),
+        "or_grid_solve": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(C.c_uint8), P(d), i32]),
+        "or_grid_sinks": (None, [vp_, u64, u32, P(i32), P(d)]),
         "or_ladder_transient": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(i32), P(i32), P(C.c_uint8),
                                        P(d), i32]),
         "or_get_math_mode": (i32, []),
@@ -197,3 +199,18 @@ def ladder_draw(cfg, seed, inst):
     Cc = np.zeros(cfg.max_sections)
     N = lib().or_ladder_draw(C.byref(cfg), seed, inst, _dp(R), _dp(Cc))
     return N, R[:N], Cc[:N]
+
+
+def grid_solve(cfg, seed, count, first=0, threads=0):
+    """Oracle power-grid corners: dict of x[count][rows*cols+1], newton, krylov, status, resid."""
+    L = lib()
+    n = cfg.rows * cfg.cols + 1
+    x = np.zeros((count, n))
+    nw = np.zeros(count, np.int32)
+    kr = np.zeros(count, np.int32)
+    st = np.zeros(count, np.uint8)
+    rs = np.zeros(count)
+    i32p = C.POINTER(C.c_int32)
+    L.or_grid_solve(C.byref(cfg), seed, first, count, _dp(x), nw.ctypes.data_as(i32p), kr.ctypes.data_as(i32p),
+                    st.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(rs), threads)
+    return dict(x=x, newton=nw, krylov=kr, status=st, resid=rs)

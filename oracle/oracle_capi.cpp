@@ -11,6 +11,7 @@
 
 #include "oracle_core.hpp"
 #include "transient.hpp"
+#include "powergrid.hpp"
 
 
 using namespace oracle;
@@ -201,6 +202,31 @@ void or_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t col,
         m.max = std::fmax(m.max, v);
     }
     *out = m;
+}
+
+// Power-grid corner instances first..first+count-1: x[count][rows*cols+1].
+void or_grid_solve(const sp_grid_config* c, uint64_t seed, uint64_t first, uint64_t count, double* x,
+                   int32_t* newton, int32_t* krylov, uint8_t* status, double* resid, int threads) {
+    const int n = c->rows * c->cols + 1;
+    parallel_for(count, threads, [&](int, uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            Grid G = grid_draw(*c, seed, (uint32_t)(first + i));
+            GridOutcome o = grid_solve(*c, G, x + i * n);
+            newton[i] = o.newton;
+            krylov[i] = o.krylov;
+            status[i] = o.status;
+            resid[i] = o.resid;
+        }
+    });
+}
+
+// Sink nodes and gate drives of instance `inst` (arrays of num_sinks).
+void or_grid_sinks(const sp_grid_config* c, uint64_t seed, uint32_t inst, int32_t* node, double* vgs) {
+    Grid G = grid_draw(*c, seed, inst);
+    for (int s = 0; s < c->num_sinks; ++s) {
+        node[s] = G.sink[s];
+        vgs[s] = G.vgs[s];
+    }
 }
 
 // Section draws of ladder instance `inst` (R, C with room for max_sections).

@@ -192,3 +192,26 @@ def ladder_config(**kw) -> SpLadderConfig:
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+class SpGridConfig(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in ("rows", "cols", "num_sinks", "max_newton", "restart", "max_krylov",
+                                         "precision", "reserved")] + [
+        (k, C.c_double) for k in ("r_lo", "r_hi", "r_scale_lo", "r_scale_hi", "vto_shift", "vdd", "strap_g",
+                                  "vgs_lo", "vgs_hi", "vto", "kp", "lambda_", "w", "l", "v_reltol", "v_abstol",
+                                  "i_abstol", "krylov_tol", "resid_target")]
+
+
+def grid_config(**kw) -> SpGridConfig:
+    """The 256-corner power-grid workload's settings; keyword arguments override fields."""
+    c = SpGridConfig()
+    c.rows, c.cols, c.num_sinks, c.max_newton, c.restart, c.max_krylov = 64, 64, 512, 30, 30, 20000
+    c.precision, c.reserved = SP_PREC_FP64, 0
+    c.r_lo, c.r_hi, c.r_scale_lo, c.r_scale_hi, c.vto_shift = 0.5, 2.0, 0.9, 1.1, 0.05
+    c.vdd, c.strap_g, c.vgs_lo, c.vgs_hi = 1.0, 1e3, 0.8, 1.2
+    c.vto, c.kp, c.lambda_, c.w, c.l = 0.7, 110e-6, 0.04, 5e-6, 0.5e-6
+    c.v_reltol, c.v_abstol, c.i_abstol = 1e-3, 1e-6, 1e-12
+    c.krylov_tol, c.resid_target = 1e-9, 1e-9
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c

@@ -154,6 +154,36 @@ int sp_set_config(sp_ctx* ctx, const sp_batch_config* cfg) {
     return SP_OK;
 }
 
+void sp_grid_config_default(sp_grid_config* c) {
+    if (!c) return;
+    *c = sp_grid_config{};
+    c->rows = c->cols = 64;
+    c->num_sinks = 512;
+    c->max_newton = 30;
+    c->restart = 30;
+    c->max_krylov = 20000;
+    c->precision = SP_PREC_FP64;
+    c->r_lo = 0.5;
+    c->r_hi = 2.0;
+    c->r_scale_lo = 0.9;
+    c->r_scale_hi = 1.1;
+    c->vto_shift = 0.05;
+    c->vdd = 1.0;
+    c->strap_g = 1e3;
+    c->vgs_lo = 0.8;
+    c->vgs_hi = 1.2;
+    c->vto = 0.7;
+    c->kp = 110e-6;
+    c->lambda = 0.04;
+    c->w = 5e-6;
+    c->l = 0.5e-6;
+    c->v_reltol = 1e-3;
+    c->v_abstol = 1e-6;
+    c->i_abstol = 1e-12;
+    c->krylov_tol = 1e-9;
+    c->resid_target = 1e-9;
+}
+
 void sp_ladder_config_default(sp_ladder_config* c) {
     if (!c) return;
     *c = sp_ladder_config{};
