@@ -298,6 +298,19 @@ typedef struct sp_grid_config {
  * iterations per solve, 30 Newton iterations, residual target 1e-9 A. */
 void sp_grid_config_default(sp_grid_config* cfg);
 
+/* Instances first_index .. first_index + count - 1: x[count][rows*cols+1] at
+ * the last Newton iterate, Newton iterations, Krylov iterations summed over
+ * the Newton solves, status (SP_ST_*), and the max |KCL residual| over the
+ * node rows at x (A).  The mixed precision keeps iterating until the
+ * residual also meets resid_target. */
+int sp_grid_solve_device(sp_ctx* ctx, const sp_grid_config* cfg, uint64_t seed, uint64_t first_index,
+                         uint64_t count, double* d_x, int32_t* d_newton, int32_t* d_krylov,
+                         uint8_t* d_status, double* d_resid, void* stream);
+/* Same on host buffers (copies out; synchronises). */
+int sp_grid_solve(sp_ctx* ctx, const sp_grid_config* cfg, uint64_t seed, uint64_t first_index,
+                  uint64_t count, double* x, int32_t* newton, int32_t* krylov, uint8_t* status,
+                  double* resid);
+
 /* ConvergenceCriteria (newton.rs:9-34) + stepping parameters
  * (newton.rs:173-231) + backend choices. */
 enum sp_fallback_bits {

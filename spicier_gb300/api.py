@@ -256,6 +256,22 @@ class Context:
                                                            _vp(accepted), _vp(rejected), _vp(iterations),
                                                            _vp(status), _vp(probe), stream))
 
+    # -- power-grid corners ----------------------------------------------------
+    def grid_solve(self, cfg, seed: int, count: int, first: int = 0) -> dict:
+        """Host-buffer power-grid corner sweep (sp_grid_solve): dict of x [count][rows*cols+1],
+        newton, krylov, status, resid."""
+        n = cfg.rows * cfg.cols + 1
+        out = dict(x=np.zeros((count, n)), newton=np.zeros(count, np.int32), krylov=np.zeros(count, np.int32),
+                   status=np.zeros(count, np.uint8), resid=np.zeros(count))
+        check(self._ptr, load().sp_grid_solve(self._ptr, C.byref(cfg), seed, first, count, _vp(out["x"]),
+                                              _vp(out["newton"]), _vp(out["krylov"]), _vp(out["status"]),
+                                              _vp(out["resid"])))
+        return out
+
+    def grid_solve_device(self, cfg, seed, count, x, newton, krylov, status, resid, first: int = 0, stream: int = 0):
+        check(self._ptr, load().sp_grid_solve_device(self._ptr, C.byref(cfg), seed, first, count, _vp(x),
+                                                     _vp(newton), _vp(krylov), _vp(status), _vp(resid), stream))
+
     def profile_read(self) -> dict:
         """{kernel name: (launches, total_ms)} since the last read."""
         from ._lib import SpKernelTime

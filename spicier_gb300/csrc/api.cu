@@ -9,6 +9,7 @@
 
 #include "internal.h"
 #include "ladder.cuh"
+#include "powergrid.cuh"
 
 using namespace sp;
 
@@ -808,7 +809,7 @@ struct LadderPlan {
 static LadderPlan ladder_plan(const sp_ctx* ctx, const sp_ladder_config* c, uint64_t count) {
     LadderPlan p;
     p.stride = (c->max_sections + 2 + 31) & ~31;
-    p.smem = (size_t)4 * 4 * p.stride * 8;  // four warps x (diag, rhs, c', d')
+    p.smem = (size_t)4 * (4 * p.stride + 64) * 8;  // four warps x (diag, rhs, c', d', block unknowns)
     const int bpsm = std::max(1, std::min(8, (int)((228 * 1024 - 1024) / (p.smem + 1024))));
     p.blocks = std::min<uint64_t>((count + 3) / 4, (uint64_t)ctx->num_sms * bpsm);
     const int bins = c->max_sections - c->min_sections + 1;
@@ -912,6 +913,98 @@ int sp_ladder_transient(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed,
     SP_CUDA(ctx, cudaMemcpyAsync(status, b + bx + 4 * bi, count, cudaMemcpyDeviceToHost, st), "D2H status");
     if (np) SP_CUDA(ctx, cudaMemcpyAsync(probe, b + bx + 4 * bi + bs, 8 * np * count, cudaMemcpyDeviceToHost, st), "D2H probe");
     SP_CUDA(ctx, cudaStreamSynchronize(st), "ladder transient");
+    return SP_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Power-grid corner sweep (powergrid.cuh)
+// ---------------------------------------------------------------------------
+static int grid_validate(sp_ctx* ctx, const sp_grid_config* c, uint64_t count) {
+    if (!c) return SP_ERR_INVALID_ARGUMENT;
+    if (c->rows < 2 || c->cols < 2 || (uint64_t)c->rows * c->cols + 1 > (uint64_t)kGridThreads * kGridRowsPerThread)
+        return fail(ctx, SP_ERR_INVALID_DIMENSION, "grid must be at least 2 x 2 with at most %d unknowns",
+                    kGridThreads * kGridRowsPerThread);
+    if (c->restart < 1 || c->restart > kGridMaxRestart)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "restart must be 1..%d", kGridMaxRestart);
+    if (c->num_sinks < 0 || c->max_newton < 1 || c->max_krylov < 1)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad sink, Newton or Krylov counts");
+    if (c->precision != SP_PREC_FP64 && c->precision != SP_PREC_MIXED)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "precision must be SP_PREC_FP64 or SP_PREC_MIXED");
+    if (!(c->r_lo > 0) || !(c->r_hi >= c->r_lo) || !(c->krylov_tol > 0))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad resistance range or tolerance");
+    if (count > 0x7fffffffull) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "too many instances");
+    const size_t smem = grid_smem_bytes(*c, c->precision == SP_PREC_MIXED ? 4 : 8);
+    if (smem > (size_t)ctx->max_smem) return fail(ctx, SP_ERR_INVALID_DIMENSION, "grid too large for shared memory");
+    return SP_OK;
+}
+
+static int grid_locked(sp_ctx* ctx, const sp_grid_config* c, uint64_t seed, uint64_t first, uint64_t count, double* d_x,
+                       int32_t* d_newton, int32_t* d_krylov, uint8_t* d_status, double* d_resid, size_t extra,
+                       cudaStream_t st) {
+    const GridWs W = grid_ws(*c, c->precision == SP_PREC_MIXED ? 4 : 8);
+    int rc = ensure_scratch(ctx, extra + W.total * count);
+    if (rc) return rc;
+    GridLaunch L{};
+    L.cfg = *c;
+    L.seed = seed;
+    L.first = first;
+    L.count = count;
+    L.ws = (char*)ctx->scratch + extra;
+    L.ws_stride = W.total;
+    L.x = d_x;
+    L.newton = d_newton;
+    L.krylov = d_krylov;
+    L.status = d_status;
+    L.resid = d_resid;
+    ProfScope prof(ctx, c->precision == SP_PREC_MIXED ? "grid_newton_gmres_mixed" : "grid_newton_gmres_fp64", st);
+    SP_CUDA(ctx, launch_grid(L, c->precision, st), "grid launch");
+    return SP_OK;
+}
+
+int sp_grid_solve_device(sp_ctx* ctx, const sp_grid_config* cfg, uint64_t seed, uint64_t first_index, uint64_t count,
+                         double* d_x, int32_t* d_newton, int32_t* d_krylov, uint8_t* d_status, double* d_resid,
+                         void* stream) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    int rc = grid_validate(ctx, cfg, count);
+    if (rc) return rc;
+    if (count == 0) return SP_OK;
+    if (!d_x || !d_newton || !d_krylov || !d_status || !d_resid)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "missing output buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    return grid_locked(ctx, cfg, seed, first_index, count, d_x, d_newton, d_krylov, d_status, d_resid, 0,
+                       (cudaStream_t)stream);
+}
+
+int sp_grid_solve(sp_ctx* ctx, const sp_grid_config* cfg, uint64_t seed, uint64_t first_index, uint64_t count,
+                  double* x, int32_t* newton, int32_t* krylov, uint8_t* status, double* resid) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    int rc = grid_validate(ctx, cfg, count);
+    if (rc) return rc;
+    if (count == 0) return SP_OK;
+    if (!x || !newton || !krylov || !status || !resid) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "missing output buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    ScratchOrder order(ctx, st);
+    const size_t n = (size_t)cfg->rows * cfg->cols + 1;
+    const size_t bx = align256(8 * n * count), bi = align256(4 * count), bs = align256(count), br = align256(8 * count);
+    const size_t extra = bx + 2 * bi + bs + br;
+    const GridWs W = grid_ws(*cfg, cfg->precision == SP_PREC_MIXED ? 4 : 8);
+    rc = ensure_scratch(ctx, extra + W.total * count);  // once: the pointers below stay valid
+    if (rc) return rc;
+    char* b = (char*)ctx->scratch;
+    rc = grid_locked(ctx, cfg, seed, first_index, count, (double*)b, (int32_t*)(b + bx), (int32_t*)(b + bx + bi),
+                     (uint8_t*)(b + bx + 2 * bi), (double*)(b + bx + 2 * bi + bs), extra, st);
+    if (rc) return rc;
+    SP_CUDA(ctx, cudaMemcpyAsync(x, b, 8 * n * count, cudaMemcpyDeviceToHost, st), "D2H x");
+    SP_CUDA(ctx, cudaMemcpyAsync(newton, b + bx, 4 * count, cudaMemcpyDeviceToHost, st), "D2H newton");
+    SP_CUDA(ctx, cudaMemcpyAsync(krylov, b + bx + bi, 4 * count, cudaMemcpyDeviceToHost, st), "D2H krylov");
+    SP_CUDA(ctx, cudaMemcpyAsync(status, b + bx + 2 * bi, count, cudaMemcpyDeviceToHost, st), "D2H status");
+    SP_CUDA(ctx, cudaMemcpyAsync(resid, b + bx + 2 * bi + bs, 8 * count, cudaMemcpyDeviceToHost, st), "D2H resid");
+    SP_CUDA(ctx, cudaStreamSynchronize(st), "grid solve");
     return SP_OK;
 }
 

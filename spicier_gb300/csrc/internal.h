@@ -31,6 +31,8 @@ struct DrawLaunch {
 };
 
 struct LadderLaunch;
+struct GridLaunch;
+cudaError_t launch_grid(const GridLaunch& L, int precision, cudaStream_t st);
 // Ladder transient launchers (ladder.cuh): 128-thread blocks, one warp per instance.
 cudaError_t launch_ladder_exact(const LadderLaunch& L, int grid, size_t smem, cudaStream_t st);
 cudaError_t launch_ladder_fast(const LadderLaunch& L, int precision, int grid, size_t smem, cudaStream_t st);

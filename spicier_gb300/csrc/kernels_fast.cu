@@ -8,6 +8,7 @@
 #define SP_KERNEL_NS kfast
 #include "internal.h"
 #include "ladder.cuh"
+#include "powergrid.cuh"
 #include <algorithm>
 
 namespace sp {
@@ -358,8 +359,17 @@ cudaError_t launch_ladder_fast(const LadderLaunch& L, int precision, int grid, s
     return cudaGetLastError();
 }
 
+cudaError_t launch_grid(const GridLaunch& L, int precision, cudaStream_t st) {
+    if (precision == SP_PREC_MIXED)
+        SP_KERNEL_NS::grid_kernel<SP_PREC_MIXED><<<(unsigned)L.count, kGridThreads, grid_smem_bytes(L.cfg, 4), st>>>(L);
+    else
+        SP_KERNEL_NS::grid_kernel<SP_PREC_FP64><<<(unsigned)L.count, kGridThreads, grid_smem_bytes(L.cfg, 8), st>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t prepare_fast_kernels(int max_smem) {
     const void* fns[] = {
+        (const void*)SP_KERNEL_NS::grid_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::grid_kernel<SP_PREC_FP64>,
         (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_MIXED>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,

@@ -65,6 +65,78 @@ __host__ __device__ inline double ladder_pulse(const sp_pulse& p, double t) {
 #ifdef SP_KERNEL_NS
 namespace SP_KERNEL_NS {
 
+// Warp-parallel solve of the chain's tridiagonal system (rows 1..N, sub-diagonal
+// -g_i, super-diagonal -g_{i+1}, diagonal B, right-hand side D; diagonally
+// dominant, so no pivoting): the partition method.  The rows are split into P
+// contiguous blocks (P = min(32, N/2), one per lane); each lane eliminates
+// inside its block downwards and upwards, so that every row i reads
+//   L_i x_{lo-1} + B_i x_i + R_i x_{hi} = D_i,
+// lane 0 solves the 2P-unknown system of the blocks' first and last rows
+// (an affine recurrence over the blocks), and every lane then recovers its
+// rows.  On exit D[i] = x_i.  L, R: scratch rows; fl: 2 x 32 scratch values.
+template <class T>
+__device__ inline void warp_partition_solve(int N, int lane, const double* g, T* B, T* D, T* L, T* R, T* fl) {
+    const int P = N / 2 < 32 ? N / 2 : 32;
+    int lo = 0, hi = 0;
+    if (lane < P) {
+        lo = 1 + (int)(((long long)lane * N) / P);
+        hi = 1 + (int)(((long long)(lane + 1) * N) / P);
+        // downward: move the sub-diagonal into the left spike L
+        L[lo] = lo > 1 ? -(T)g[lo] : (T)0;
+        for (int i = lo + 1; i < hi; ++i) {
+            const T a = -(T)g[i], cprev = -(T)g[i];  // c_{i-1} = -g_i = a_i
+            const T f = a / B[i - 1];
+            L[i] = -f * L[i - 1];
+            B[i] = B[i] - f * cprev;
+            D[i] = D[i] - f * D[i - 1];
+        }
+        // upward: move the super-diagonal into the right spike R
+        R[hi - 1] = hi - 1 < N ? -(T)g[hi] : (T)0;
+        for (int i = hi - 2; i >= lo; --i) {
+            const T cc = -(T)g[i + 1];
+            const T f = cc / B[i + 1];
+            L[i] = L[i] - f * L[i + 1];
+            R[i] = -f * R[i + 1];
+            D[i] = D[i] - f * D[i + 1];
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        // forward over blocks: l_{j-1} = al + be f_j;  f_j = p_j + q_j f_{j+1};  l_j = al_j + be_j f_{j+1}
+        T al = 0, be = 0;
+        T pq[2 * 32];
+        for (int j = 0; j < P; ++j) {
+            const int l0 = 1 + (int)(((long long)j * N) / P), h1 = (int)(((long long)(j + 1) * N) / P);  // h1 = hi - 1
+            const T den = B[l0] + L[l0] * be;
+            const T pj = (D[l0] - L[l0] * al) / den, qj = -R[l0] / den;
+            const T nal = (D[h1] - L[h1] * al - L[h1] * be * pj) / B[h1];
+            const T nbe = (-L[h1] * be * qj - R[h1]) / B[h1];
+            pq[2 * j] = pj;
+            pq[2 * j + 1] = qj;
+            fl[2 * j] = nbe;  // al_j, be_j kept for the back pass
+            fl[2 * j + 1] = nal;
+            al = nal;
+            be = nbe;
+        }
+        // backward: f_P = 0
+        T fnext = 0;
+        for (int j = P - 1; j >= 0; --j) {
+            const T fj = pq[2 * j] + pq[2 * j + 1] * fnext;
+            const T lj = fl[2 * j + 1] + fl[2 * j] * fnext;
+            fl[2 * j] = fj;
+            fl[2 * j + 1] = lj;
+            fnext = fj;
+        }
+    }
+    __syncwarp();
+    if (lane < P) {
+        const T xl = lane > 0 ? fl[2 * (lane - 1) + 1] : (T)0;  // last of the previous block
+        const T xr = lane + 1 < P ? fl[2 * (lane + 1)] : (T)0;  // first of the next block
+        for (int i = lo; i < hi; ++i) D[i] = (D[i] - L[i] * xl - R[i] * xr) / B[i];
+    }
+    __syncwarp();
+}
+
 template <int PREC>
 struct LadderWarp {
     const LadderLaunch& L;
@@ -74,16 +146,27 @@ struct LadderWarp {
     double* srhs;
     double* scp;
     double* sdp;
+    double* sfl;  // 64 values: the partition solve's block unknowns
     int N, lane;
-    double nvt, vcrit;
+    double nvt, inv_nvt, vcrit;
     unsigned hard;
 
     __device__ double limit(double vd) {
         if (vd > vcrit) {
-            const double arg = (vd - vcrit) / nvt;
-            return vcrit + nvt * (1.0 + pm_log1p(arg, &hard));
+            if (PREC == SP_PREC_FP64_EXACT) {
+                const double arg = (vd - vcrit) / nvt;
+                return vcrit + nvt * (1.0 + pm_log1p(arg, &hard));
+            }
+            return vcrit + nvt * (1.0 + log1p((vd - vcrit) * inv_nvt));
         }
         return vd;
+    }
+
+    // exp of the diode: the portable correctly rounded one for the exact mode,
+    // the device's (shorter dependency chain) otherwise
+    __device__ double dexp(double v) {
+        if (PREC == SP_PREC_FP64_EXACT) return cr_exp(v / nvt, &hard);
+        return exp(v * inv_nvt);
     }
 
     // One Newton iteration of a stage on xs; writes the new iterate into xs
@@ -99,9 +182,10 @@ struct LadderWarp {
             for (int k = 1 + lane; k <= N; k += 32) {
                 const double vl1 = limit(xs[k]);
                 const double vl2 = limit(vl1);
-                const double e = cr_exp(vl2 / nvt, &hard);
+                const double e = dexp(vl2);
                 const double id = c.diode_is * (e - 1.0);
-                const double gd = fmax(c.diode_is * e / nvt, 1e-12);
+                const double gd = PREC == SP_PREC_FP64_EXACT ? fmax(c.diode_is * e / nvt, 1e-12)
+                                                             : fmax(c.diode_is * e * inv_nvt, 1e-12);
                 const double ieq_d = id - gd * vl1;
                 const double gk1 = k < N ? g[k + 1] : 0.0;
                 sdiag[k] = ((g[k] + gk1) + geq[k]) + gd;
@@ -110,8 +194,8 @@ struct LadderWarp {
                 srhs[k] = r;
             }
             __syncwarp();
-            if (lane == 0) {
-                if (PREC == SP_PREC_FP64_EXACT) {
+            if (PREC == SP_PREC_FP64_EXACT && lane == 0) {
+                {
                     scp[1] = (N > 1 ? -g[2] : 0.0) / sdiag[1];
                     sdp[1] = srhs[1] / sdiag[1];
                     for (int k = 2; k <= N; ++k) {
@@ -120,21 +204,12 @@ struct LadderWarp {
                         scp[k] = (k < N ? -g[k + 1] : 0.0) / m;
                         sdp[k] = (srhs[k] - sub * sdp[k - 1]) / m;
                     }
-                } else {
-                    double r = 1.0 / sdiag[1];
-                    scp[1] = (N > 1 ? -g[2] : 0.0) * r;
-                    sdp[1] = srhs[1] * r;
-                    for (int k = 2; k <= N; ++k) {
-                        const double sub = -g[k];
-                        r = 1.0 / (sdiag[k] - sub * scp[k - 1]);
-                        scp[k] = (k < N ? -g[k + 1] : 0.0) * r;
-                        sdp[k] = (srhs[k] - sub * sdp[k - 1]) * r;
-                    }
+                    // back substitution into srhs (the new iterate of nodes 1..N)
+                    srhs[N] = sdp[N];
+                    for (int k = N - 1; k >= 1; --k) srhs[k] = sdp[k] - scp[k] * srhs[k + 1];
                 }
-                // back substitution into srhs (the new iterate of nodes 1..N)
-                srhs[N] = sdp[N];
-                for (int k = N - 1; k >= 1; --k) srhs[k] = sdp[k] - scp[k] * srhs[k + 1];
             }
+            if (PREC != SP_PREC_FP64_EXACT) warp_partition_solve<double>(N, lane, g, sdiag, srhs, scp, sdp, sfl);
             __syncwarp();
             for (int k = 1 + lane; k <= N; k += 32) {
                 const double nw = srhs[k], old = xs[k];
@@ -153,9 +228,9 @@ struct LadderWarp {
                 const double xk = xs[k];
                 const double vl1 = limit(xk);
                 const double vl2 = limit(vl1);
-                const double e = cr_exp(vl2 / nvt, &hard);
+                const double e = dexp(vl2);
                 const double id = c.diode_is * (e - 1.0);
-                const double gd = fmax(c.diode_is * e / nvt, 1e-12);
+                const double gd = fmax(c.diode_is * e * inv_nvt, 1e-12);
                 const double xl = k == 1 ? V : xs[k - 1];
                 const double xr = k < N ? xs[k + 1] : 0.0;
                 const double gk1 = k < N ? g[k + 1] : 0.0;
@@ -165,20 +240,7 @@ struct LadderWarp {
                 jr[k] = (float)(-F);
             }
             __syncwarp();
-            if (lane == 0) {
-                float r = 1.0f / jd[1];
-                jc[1] = (N > 1 ? -(float)g[2] : 0.0f) * r;
-                jp[1] = jr[1] * r;
-                for (int k = 2; k <= N; ++k) {
-                    const float sub = -(float)g[k];
-                    r = 1.0f / (jd[k] - sub * jc[k - 1]);
-                    jc[k] = (k < N ? -(float)g[k + 1] : 0.0f) * r;
-                    jp[k] = (jr[k] - sub * jp[k - 1]) * r;
-                }
-                jr[N] = jp[N];
-                for (int k = N - 1; k >= 1; --k) jr[k] = jp[k] - jc[k] * jr[k + 1];
-            }
-            __syncwarp();
+            warp_partition_solve<float>(N, lane, g, jd, jr, jc, jp, reinterpret_cast<float*>(sfl));
             for (int k = 1 + lane; k <= N; k += 32) {
                 const double old = xs[k];
                 const double nw = old + (double)jr[k];
@@ -228,16 +290,18 @@ __global__ void __launch_bounds__(128, 2) ladder_kernel(LadderLaunch L) {
     const int slot = blockIdx.x * (blockDim.x >> 5) + wib;
     if (slot >= L.slots) return;
     const sp_ladder_config& c = L.cfg;
-    double* sm = reinterpret_cast<double*>(lsm) + (size_t)wib * 4 * L.stride;
+    double* sm = reinterpret_cast<double*>(lsm) + (size_t)wib * (4 * L.stride + 64);
     LadderWarp<PREC> W{L, c};
     for (int a = 0; a < LA_COUNT; ++a) W.A[a] = L.ws + ((size_t)slot * LA_COUNT + a) * L.stride;
     W.sdiag = sm;
     W.srhs = sm + L.stride;
     W.scp = sm + 2 * L.stride;
     W.sdp = sm + 3 * L.stride;
+    W.sfl = sm + 4 * L.stride;
     W.lane = lane;
     W.hard = 0;
     W.nvt = c.diode_n * thermal_voltage_300();
+    W.inv_nvt = 1.0 / W.nvt;
     W.vcrit = W.nvt * cr_log(W.nvt / (1.4142135623730951 * 1e-14), &W.hard);
     const double gamma = 2.0 - 1.4142135623730951;
     const int ldx = c.max_sections + 2;
