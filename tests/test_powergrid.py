@@ -55,9 +55,10 @@ def test_fp64_against_oracle(ctx):
     with oracle.math_mode("cr"):
         o = oracle.grid_solve(cfg, 1, 16)
     assert (g["status"] == 0).all() and np.array_equal(g["newton"], o["newton"])
-    # same algorithm; the dot products sum in another (fixed) order
-    assert np.abs(g["x"] - o["x"]).max() < 1e-9 * cfg.vdd + 1e-12
-    assert np.abs(g["krylov"] - o["krylov"]).max() <= 0.02 * o["krylov"].max() + 5
+    # same iteration in exact arithmetic (the GPU orthogonalises by CGS2, the
+    # oracle by MGS, and sums in other orders): agreement to the 1e-9 linear tolerance
+    assert np.abs(g["x"] - o["x"]).max() < 2e-8
+    assert np.abs(g["krylov"] - o["krylov"]).max() <= 0.1 * o["krylov"].max() + 30
     assert g["resid"].max() < 1e-7
 
 
