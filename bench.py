@@ -217,6 +217,8 @@ def main():
     ap.add_argument("--samples", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-config4", action="store_true")
+    ap.add_argument("--no-transient", action="store_true", help="skip the ladder-transient (workload 3) report")
+    ap.add_argument("--no-grid", action="store_true", help="skip the power-grid (workload 5) report")
     ap.add_argument("--train-samples", type=int, default=1 << 20)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -404,6 +406,74 @@ def main():
     if roofline is not None:
         roofline = dict(roofline, kernel=dominant)
 
+    def event_ms(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        flush.fill_(0.5)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    # workload 3: 4,096 RC-diode ladder transients (adaptive TR-BDF2), one run per precision
+    config3 = None
+    if not args.no_transient and rank == 0:
+        import oracle
+        count3 = 4096
+        config3 = {"instances": count3, "sections": "8..512", "tstop_s": 100e-9}
+        for name, prec in (("mixed", abi.SP_PREC_MIXED), ("plain_fp64", abi.SP_PREC_FP64)):
+            lc = abi.ladder_config(precision=prec, num_probe=0)
+            ld = lc.max_sections + 2
+            lx = torch.empty((count3, ld), dtype=torch.float64, device=dev)
+            li = [torch.empty(count3, dtype=torch.int32, device=dev) for _ in range(4)]
+            lst = torch.empty(count3, dtype=torch.uint8, device=dev)
+            ctx.ladder_transient_device(lc, SEED, 256, lx, *li, lst, stream=stream)  # warm-up
+            torch.cuda.synchronize()
+            ms = event_ms(lambda: ctx.ladder_transient_device(lc, SEED, count3, lx, *li, lst, stream=stream))
+            acc = li[1].cpu().numpy()
+            stages = 2.0 * float(acc.sum())
+            config3[name] = {"ms": ms, "transients_per_s": count3 / (ms / 1e3), "stage_solves_per_s": stages / (ms / 1e3),
+                             "newton_per_stage": float(li[3].cpu().numpy().sum()) / stages,
+                             "accepted_steps_mean": float(acc.mean()), "rejected_steps_mean": float(li[2].float().mean()),
+                             "converged_fraction": float((lst == 0).float().mean())}
+        sample3 = 64
+        with oracle.math_mode("cr"):
+            t0 = time.perf_counter()
+            o3 = oracle.ladder_transient(abi.ladder_config(num_probe=0), SEED, sample3)
+            dt3 = time.perf_counter() - t0
+        config3["cpu_oracle"] = {"transients_per_s": sample3 / dt3, "cores": os.cpu_count() or 1,
+                                 "sample": f"{sample3} ladders (instances 0..{sample3 - 1}), FP64, all host threads"}
+        config3["speedup_mixed_vs_plain_fp64"] = config3["mixed"]["transients_per_s"] / config3["plain_fp64"]["transients_per_s"]
+
+    # workload 5: 256 power-grid corners (Newton + GMRES(30) + Jacobi)
+    config5 = None
+    if not args.no_grid and rank == 0:
+        import oracle
+        count5 = 256
+        config5 = {"corners": count5, "mesh": "64x64 + VDD branch (4097 unknowns)", "sinks": 512}
+        for name, prec in (("mixed", abi.SP_PREC_MIXED), ("plain_fp64", abi.SP_PREC_FP64)):
+            gc = abi.grid_config(precision=prec)
+            nG = gc.rows * gc.cols + 1
+            gx = torch.empty((count5, nG), dtype=torch.float64, device=dev)
+            gnw, gkr = (torch.empty(count5, dtype=torch.int32, device=dev) for _ in range(2))
+            gst = torch.empty(count5, dtype=torch.uint8, device=dev)
+            grs = torch.empty(count5, dtype=torch.float64, device=dev)
+            ctx.grid_solve_device(gc, SEED, 8, gx, gnw, gkr, gst, grs, stream=stream)  # warm-up
+            torch.cuda.synchronize()
+            ms = event_ms(lambda: ctx.grid_solve_device(gc, SEED, count5, gx, gnw, gkr, gst, grs, stream=stream))
+            nwt = gnw.cpu().numpy()
+            config5[name] = {"ms": ms, "corners_per_s": count5 / (ms / 1e3),
+                             "newton_solves_per_s": float(nwt.sum()) / (ms / 1e3), "newton_mean": float(nwt.mean()),
+                             "krylov_mean": float(gkr.float().mean()), "max_kcl_residual_A": float(grs.max()),
+                             "converged_fraction": float((gst == 0).float().mean())}
+        sample5 = 4
+        t0 = time.perf_counter()
+        oracle.grid_solve(abi.grid_config(), SEED, sample5)
+        dt5 = time.perf_counter() - t0
+        config5["cpu_oracle"] = {"corners_per_s": sample5 / dt5, "cores": min(sample5, os.cpu_count() or 1),
+                                 "sample": f"{sample5} corners (one per host thread), FP64"}
+
     # config 4: a 10-input network (the workload's stated MLP) on 262,144 samples
     config4 = None
     if not args.no_config4 and rank == 0:
@@ -479,6 +549,8 @@ def main():
             "gpu_launches": sum(v[0] for v in head["prof"].values()),
             "clocks": head["clocks"],
             "config4": config4,
+            "config3_ladder_transient": config3,
+            "config5_power_grid": config5,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

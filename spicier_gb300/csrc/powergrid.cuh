@@ -290,14 +290,14 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_kernel(GridLaunch L) {
         int total = 0;
         bool solved = b_norm < 1e-30;
         for (int cycle = 0; !solved && cycle < c.max_krylov; ++cycle) {
-            // residual of the current solution: w = r - A sol
-            for (int p = tid; p < n; p += kGridThreads) zs[p] = (T)sol[p];
+            // residual of the current solution, r - A sol, in FP64 (an FP32
+            // difference of two nearly equal vectors would stall the restarts)
             __syncthreads();
             T loc = 0;
             for (int p = tid; p < n; p += kGridThreads) {
-                const T v = (T)r[p] - grid_apply_row<T>(c, gh, gv, dT, zs, p);
-                V[p] = v;
-                loc += v * v;
+                const double rv = r[p] - grid_apply_row<double>(c, gh, gv, diag, sol, p);
+                V[p] = (T)rv;
+                loc += (T)rv * (T)rv;
             }
             const double r_norm = sqrt((double)block_sum<T>(loc, red));
             if (r_norm / b_norm < tol) {
@@ -327,17 +327,29 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_kernel(GridLaunch L) {
                 // basis vector; in exact arithmetic the same Hessenberg column
                 // as modified Gram-Schmidt, and as well conditioned in practice
                 for (int pass = 0; pass < 2; ++pass) {
-                    for (int j = 0; j <= k; ++j) {
-                        const T* vj = V + (size_t)j * n;
-                        T loc2 = 0;
+                    // projections in chunks of 8 basis vectors: the chunk's loads
+                    // are independent, so they overlap instead of one at a time
+                    for (int j0 = 0; j0 <= k; j0 += 8) {
+                        T acc[8];
 #pragma unroll
-                        for (int q = 0; q < kGridRowsPerThread; ++q) {
-                            const int p = tid + q * kGridThreads;
-                            if (p < n) loc2 += vj[p] * w[q];
+                        for (int u = 0; u < 8; ++u) {
+                            acc[u] = 0;
+                            if (j0 + u <= k) {
+                                const T* vj = V + (size_t)(j0 + u) * n;
+#pragma unroll
+                                for (int q = 0; q < kGridRowsPerThread; ++q) {
+                                    const int p = tid + q * kGridThreads;
+                                    if (p < n) acc[u] += vj[p] * w[q];
+                                }
+                            }
                         }
 #pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) loc2 += __shfl_xor_sync(0xffffffffu, loc2, o);
-                        if ((tid & 31) == 0) proj[(tid >> 5) * (kGridMaxRestart + 1) + j] = loc2;
+                        for (int u = 0; u < 8; ++u) {
+                            T v = acc[u];
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                            if ((tid & 31) == 0 && j0 + u <= k) proj[(tid >> 5) * (kGridMaxRestart + 1) + j0 + u] = v;
+                        }
                     }
                     __syncthreads();
                     if (tid <= k) {
@@ -348,13 +360,18 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_kernel(GridLaunch L) {
                                                                           : hmat[k * (kGridMaxRestart + 1) + tid] + (double)hs;
                     }
                     __syncthreads();
-                    for (int j = 0; j <= k; ++j) {
-                        const T hij = hcol[j];
-                        const T* vj = V + (size_t)j * n;
+                    for (int j0 = 0; j0 <= k; j0 += 8) {
 #pragma unroll
-                        for (int q = 0; q < kGridRowsPerThread; ++q) {
-                            const int p = tid + q * kGridThreads;
-                            if (p < n) w[q] -= hij * vj[p];
+                        for (int u = 0; u < 8; ++u) {
+                            if (j0 + u <= k) {
+                                const T hij = hcol[j0 + u];
+                                const T* vj = V + (size_t)(j0 + u) * n;
+#pragma unroll
+                                for (int q = 0; q < kGridRowsPerThread; ++q) {
+                                    const int p = tid + q * kGridThreads;
+                                    if (p < n) w[q] -= hij * vj[p];
+                                }
+                            }
                         }
                     }
                 }
