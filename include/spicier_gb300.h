@@ -218,6 +218,29 @@ typedef struct sp_circuit {
     const double* nodeset;
 } sp_circuit;
 
+/* Histogram of column `col` of values[rows][ld] (Histogram::new,
+ * statistics.rs:243-268): num_bins bins of width (max - min) / num_bins,
+ * bin = clamp(floor((v - min) / width), 0, num_bins - 1) (NaN -> bin 0, as
+ * Rust's saturating float-to-int cast); rows whose status is not converged
+ * are skipped when d_status is given.  d_bins[num_bins] receives the counts
+ * (overwritten). */
+int sp_histogram_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld,
+                        uint32_t col, const uint8_t* d_status, double min, double max,
+                        uint32_t num_bins, uint64_t* d_bins, void* stream);
+
+/* Yield (YieldSpec / YieldAnalysis, statistics.rs:331-428): d_pass[k] = rows
+ * whose column specs[k].col lies in [lower, upper] (inclusive), d_pass[num_specs]
+ * = rows passing every spec; with d_status given, rows that did not converge
+ * pass nothing.  Yield = pass / rows. */
+typedef struct sp_yield_spec {
+    uint32_t col;
+    uint32_t reserved;
+    double lower, upper;
+} sp_yield_spec;
+int sp_yield_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld,
+                    const uint8_t* d_status, const sp_yield_spec* specs, uint32_t num_specs,
+                    uint64_t* d_pass, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* Batched nonlinear transient of RC-diode ladders (no counterpart in the  */
 /* reference, whose transient solvers are linear): every instance is a     */

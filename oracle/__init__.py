@@ -87,6 +87,8 @@ def _bind(L):
         "or_ladder_draw": (i32, [vp_, u64, u32, P(d), P(d)]),
         "or_grid_solve": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(C.c_uint8), P(d), i32]),
         "or_grid_sinks": (None, [vp_, u64, u32, P(i32), P(d)]),
+        "or_histogram": (None, [P(d), u64, u32, u32, vp_, d, d, u32, P(u64)]),
+        "or_yield": (None, [P(d), u64, u32, vp_, vp_, u32, P(u64)]),
         "or_ladder_transient": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(i32), P(i32), P(C.c_uint8),
                                        P(d), i32]),
         "or_get_math_mode": (i32, []),
@@ -214,3 +216,24 @@ def grid_solve(cfg, seed, count, first=0, threads=0):
     L.or_grid_solve(C.byref(cfg), seed, first, count, _dp(x), nw.ctypes.data_as(i32p), kr.ctypes.data_as(i32p),
                     st.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(rs), threads)
     return dict(x=x, newton=nw, krylov=kr, status=st, resid=rs)
+
+
+def histogram(values, col, min, max, num_bins, status=None):
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    bins = np.zeros(num_bins, np.uint64)
+    st = None if status is None else np.ascontiguousarray(status, dtype=np.uint8)
+    lib().or_histogram(_dp(v), v.shape[0], v.shape[1], col, None if st is None else st.ctypes.data, min, max,
+                       num_bins, bins.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return bins
+
+
+def yield_counts(values, specs, status=None):
+    """specs: [(col, lower, upper)] -> pass counts per spec and for all."""
+    from spicier_gb300 import abi
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    arr = (abi.SpYieldSpec * max(len(specs), 1))(*[abi.SpYieldSpec(c, 0, lo, hi) for c, lo, hi in specs])
+    out = np.zeros(len(specs) + 1, np.uint64)
+    st = None if status is None else np.ascontiguousarray(status, dtype=np.uint8)
+    lib().or_yield(_dp(v), v.shape[0], v.shape[1], None if st is None else st.ctypes.data, C.addressof(arr),
+                   len(specs), out.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return out

@@ -6,6 +6,7 @@
 // par_iter (crates/spicier-batched-sweep/src/parallel.rs:142-156): one
 // independent solver state per worker, samples handed out in small chunks.
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <thread>
 
@@ -202,6 +203,38 @@ void or_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t col,
         m.max = std::fmax(m.max, v);
     }
     *out = m;
+}
+
+// Histogram::new (statistics.rs:243-268) over column `col`, converged rows only
+// when status is given.  Rust's `as isize` saturates and maps NaN to 0.
+void or_histogram(const double* v, uint64_t rows, uint32_t ld, uint32_t col, const uint8_t* status, double mn,
+                  double mx, uint32_t nb, uint64_t* bins) {
+    const double width = (mx - mn) / (double)nb;
+    for (uint32_t b = 0; b < nb; ++b) bins[b] = 0;
+    for (uint64_t i = 0; i < rows; ++i) {
+        if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+        const double f = std::floor((v[i * ld + col] - mn) / width);
+        long long b = std::isnan(f) ? 0 : (f < -9.2e18 ? LLONG_MIN : (f > 9.2e18 ? LLONG_MAX : (long long)f));
+        b = std::min<long long>(std::max<long long>(b, 0), (long long)nb - 1);
+        bins[b] += 1;
+    }
+}
+
+// YieldSpec::passes / YieldAnalysis::all_pass (statistics.rs:347-428).
+void or_yield(const double* v, uint64_t rows, uint32_t ld, const uint8_t* status, const sp_yield_spec* specs,
+              uint32_t ns, uint64_t* pass) {
+    for (uint32_t k = 0; k <= ns; ++k) pass[k] = 0;
+    for (uint64_t i = 0; i < rows; ++i) {
+        if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+        bool all = true;
+        for (uint32_t k = 0; k < ns; ++k) {
+            const double x = v[i * ld + specs[k].col];
+            const bool ok = x >= specs[k].lower && x <= specs[k].upper;
+            all = all && ok;
+            pass[k] += ok ? 1 : 0;
+        }
+        pass[ns] += all ? 1 : 0;
+    }
 }
 
 // Power-grid corner instances first..first+count-1: x[count][rows*cols+1].

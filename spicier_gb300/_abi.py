@@ -215,3 +215,7 @@ def grid_config(**kw) -> SpGridConfig:
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+class SpYieldSpec(C.Structure):
+    _fields_ = [("col", C.c_uint32), ("reserved", C.c_uint32), ("lower", C.c_double), ("upper", C.c_double)]

@@ -272,6 +272,35 @@ class Context:
         check(self._ptr, load().sp_grid_solve_device(self._ptr, C.byref(cfg), seed, first, count, _vp(x),
                                                      _vp(newton), _vp(krylov), _vp(status), _vp(resid), stream))
 
+    # -- statistics ------------------------------------------------------------
+    def histogram_device(self, values, col: int, num_bins: int, min: float = None, max: float = None, status=None,
+                         stream: int = 0):
+        """Histogram of column `col` of a [rows][ld] CUDA tensor (Histogram::new; with min/max None, the
+        column's range as Histogram::from_sweep takes it, widened by 0.5 on each side if flat)."""
+        import torch
+        rows, ld = int(values.shape[0]), int(values.shape[1])
+        if min is None or max is None:
+            col_v = values[:, col] if status is None else values[:, col][(status & abi.SP_ST_MASK) == 0]
+            lo, hi = float(col_v.min()), float(col_v.max())
+            if abs(hi - lo) < np.finfo(float).eps:
+                lo, hi = lo - 0.5, hi + 0.5
+            min = lo if min is None else min
+            max = hi if max is None else max
+        bins = torch.empty(num_bins, dtype=torch.int64, device=values.device)
+        check(self._ptr, load().sp_histogram_device(self._ptr, _vp(values), rows, ld, col, _vp(status), min, max,
+                                                    num_bins, _vp(bins), stream))
+        return bins, min, max
+
+    def yield_device(self, values, specs, status=None, stream: int = 0):
+        """Pass counts of [(col, lower, upper)] specs and of all together (YieldAnalysis)."""
+        import torch
+        rows, ld = int(values.shape[0]), int(values.shape[1])
+        arr = (abi.SpYieldSpec * max(len(specs), 1))(*[abi.SpYieldSpec(c, 0, lo, hi) for c, lo, hi in specs])
+        out = torch.empty(len(specs) + 1, dtype=torch.int64, device=values.device)
+        check(self._ptr, load().sp_yield_device(self._ptr, _vp(values), rows, ld, _vp(status), C.addressof(arr),
+                                                len(specs), _vp(out), stream))
+        return out
+
     def profile_read(self) -> dict:
         """{kernel name: (launches, total_ms)} since the last read."""
         from ._lib import SpKernelTime

@@ -1008,4 +1008,45 @@ int sp_grid_solve(sp_ctx* ctx, const sp_grid_config* cfg, uint64_t seed, uint64_
     return SP_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Histogram and yield (statistics.rs)
+// ---------------------------------------------------------------------------
+int sp_histogram_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld, uint32_t col,
+                        const uint8_t* d_status, double min, double max, uint32_t num_bins, uint64_t* d_bins,
+                        void* stream) {
+    if (!ctx || !d_bins || (rows && !d_values)) return SP_ERR_INVALID_ARGUMENT;
+    if (num_bins == 0 || num_bins > 12288) return fail(ctx, SP_ERR_INVALID_DIMENSION, "num_bins must be 1..12288");
+    if (!(max > min)) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "max must be > min");
+    if (col >= ld) return fail(ctx, SP_ERR_INVALID_DIMENSION, "column outside the row");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ProfScope prof(ctx, "histogram", (cudaStream_t)stream);
+    SP_CUDA(ctx, launch_histogram(d_values, rows, ld, col, d_status, min, max, num_bins, d_bins, ctx->num_sms,
+                                  (cudaStream_t)stream),
+            "histogram launch");
+    return SP_OK;
+}
+
+int sp_yield_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld, const uint8_t* d_status,
+                    const sp_yield_spec* specs, uint32_t num_specs, uint64_t* d_pass, void* stream) {
+    if (!ctx || !d_pass || (rows && !d_values) || (num_specs && !specs)) return SP_ERR_INVALID_ARGUMENT;
+    if (num_specs > 4096) return fail(ctx, SP_ERR_INVALID_DIMENSION, "at most 4096 specifications");
+    for (uint32_t k = 0; k < num_specs; ++k)
+        if (specs[k].col >= ld) return fail(ctx, SP_ERR_INVALID_DIMENSION, "specification %u: column outside the row", k);
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    ScratchOrder order(ctx, st);
+    int rc = ensure_scratch(ctx, sizeof(sp_yield_spec) * ((size_t)num_specs + 1));
+    if (rc) return rc;
+    sp_yield_spec* d_specs = (sp_yield_spec*)ctx->scratch;
+    if (num_specs)
+        SP_CUDA(ctx, cudaMemcpyAsync(d_specs, specs, sizeof(sp_yield_spec) * num_specs, cudaMemcpyHostToDevice, st),
+                "H2D specifications");
+    ProfScope prof(ctx, "yield", st);
+    SP_CUDA(ctx, launch_yield(d_values, rows, ld, d_status, d_specs, num_specs, d_pass, ctx->num_sms, st), "yield launch");
+    return SP_OK;
+}
+
 }  // extern "C"

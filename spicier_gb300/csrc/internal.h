@@ -30,6 +30,10 @@ struct DrawLaunch {
     unsigned int* hard;   // count of draws whose rounding was undecided (or nullptr)
 };
 
+cudaError_t launch_histogram(const double* v, uint64_t rows, uint32_t ld, uint32_t col, const uint8_t* status,
+                             double mn, double mx, uint32_t nb, uint64_t* bins, int num_sms, cudaStream_t st);
+cudaError_t launch_yield(const double* v, uint64_t rows, uint32_t ld, const uint8_t* status,
+                         const sp_yield_spec* d_specs, uint32_t ns, uint64_t* pass, int num_sms, cudaStream_t st);
 struct LadderLaunch;
 struct GridLaunch;
 cudaError_t launch_grid(const GridLaunch& L, int precision, cudaStream_t st);

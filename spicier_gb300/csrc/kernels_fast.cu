@@ -359,6 +359,68 @@ cudaError_t launch_ladder_fast(const LadderLaunch& L, int precision, int grid, s
     return cudaGetLastError();
 }
 
+// Histogram: per-block shared counts, then one atomic add per bin and block
+// (integer counts: the result does not depend on the order).
+__global__ void histogram_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld, uint32_t col,
+                                 const uint8_t* __restrict__ status, double mn, double width, uint32_t nb,
+                                 unsigned long long* __restrict__ bins) {
+    extern __shared__ unsigned int hsm[];
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) hsm[b] = 0;
+    __syncthreads();
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+        const double f = floor((v[i * ld + col] - mn) / width);
+        // Rust's `as isize`: NaN -> 0, out of range saturates; then clamp
+        long long b = f != f ? 0 : (f < 0.0 ? -1 : (f >= (double)nb ? (long long)nb : (long long)f));
+        b = b < 0 ? 0 : (b > (long long)nb - 1 ? (long long)nb - 1 : b);
+        atomicAdd(&hsm[b], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x)
+        if (hsm[b]) atomicAdd(&bins[b], (unsigned long long)hsm[b]);
+}
+
+cudaError_t launch_histogram(const double* v, uint64_t rows, uint32_t ld, uint32_t col, const uint8_t* status,
+                             double mn, double mx, uint32_t nb, uint64_t* bins, int num_sms, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(bins, 0, 8 * (size_t)nb, st);
+    if (e != cudaSuccess || rows == 0) return e;
+    const unsigned grid = (unsigned)std::min<uint64_t>((rows + 255) / 256, (uint64_t)num_sms * 8);
+    histogram_kernel<<<grid, 256, 4 * (size_t)nb, st>>>(v, rows, ld, col, status, mn, (mx - mn) / (double)nb, nb,
+                                                        (unsigned long long*)bins);
+    return cudaGetLastError();
+}
+
+__global__ void yield_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
+                             const uint8_t* __restrict__ status, const sp_yield_spec* __restrict__ specs, uint32_t ns,
+                             unsigned long long* __restrict__ pass) {
+    extern __shared__ unsigned int ysm[];  // [ns + 1]
+    for (uint32_t k = threadIdx.x; k <= ns; k += blockDim.x) ysm[k] = 0;
+    __syncthreads();
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+        bool all = true;
+        for (uint32_t k = 0; k < ns; ++k) {
+            const double x = v[i * ld + specs[k].col];
+            const bool ok = x >= specs[k].lower && x <= specs[k].upper;  // YieldSpec::passes
+            all = all && ok;
+            if (ok) atomicAdd(&ysm[k], 1u);
+        }
+        if (all) atomicAdd(&ysm[ns], 1u);
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k <= ns; k += blockDim.x)
+        if (ysm[k]) atomicAdd(&pass[k], (unsigned long long)ysm[k]);
+}
+
+cudaError_t launch_yield(const double* v, uint64_t rows, uint32_t ld, const uint8_t* status, const sp_yield_spec* d_specs,
+                         uint32_t ns, uint64_t* pass, int num_sms, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(pass, 0, 8 * ((size_t)ns + 1), st);
+    if (e != cudaSuccess || rows == 0) return e;
+    const unsigned grid = (unsigned)std::min<uint64_t>((rows + 255) / 256, (uint64_t)num_sms * 8);
+    yield_kernel<<<grid, 256, 4 * ((size_t)ns + 1), st>>>(v, rows, ld, status, d_specs, ns, (unsigned long long*)pass);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_grid(const GridLaunch& L, int precision, cudaStream_t st) {
     if (precision == SP_PREC_MIXED)
         SP_KERNEL_NS::grid_kernel<SP_PREC_MIXED><<<(unsigned)L.count, kGridThreads, grid_smem_bytes(L.cfg, 4), st>>>(L);
