@@ -27,8 +27,10 @@
 //         exact; ln(1+r) by its Taylor series (15 terms, Horner, the inner
 //         8 levels in Q0.64).  Within 2^-16 of 1 the series runs in
 //         d = |x - 1| instead, relative to d (ln_near1).
-// cos t = +-cos a or +-sin a,  a = |t - k pi/2| <= pi/4,  a = j/128 + d,
-//         cos/sin(j/128) from the table, cos/sin(d) by Taylor series in d^2.
+// cos t = +-cos a or +-sin a,  a = |t - k pi/2| <= pi/4,  a = j/512 + d,
+//         cos/sin(j/512) from the table, cos/sin(d) by Taylor series in d^2
+//         (five terms each, the innermost in 64 bits), products without their
+//         low partial product (error bound 512 units of 2^-125).
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -65,11 +67,11 @@ struct ExpRow {
 
 #if defined(__CUDACC__)
 __device__ const LnRow kLnRowsDev[256] = SP_CR_LN_ROWS;
-__device__ const CosRow kCosRowsDev[102] = SP_CR_COS_ROWS;
+__device__ const CosRow kCosRowsDev[404] = SP_CR_COS_ROWS;
 __device__ const ExpRow kExpRowsDev[181] = SP_CR_EXP_ROWS;
 #endif
 static const LnRow kLnRowsHost[256] = SP_CR_LN_ROWS;
-static const CosRow kCosRowsHost[102] = SP_CR_COS_ROWS;
+static const CosRow kCosRowsHost[404] = SP_CR_COS_ROWS;
 static const ExpRow kExpRowsHost[181] = SP_CR_EXP_ROWS;
 
 SP_HD ExpRow exp_row(int i) {
@@ -146,6 +148,18 @@ SP_HD u128 mulq(u128 a, u128 b) {
     const uint64_t a0 = lo64(a), a1 = hi64(a), b0 = lo64(b), b1 = hi64(b);
     const u128 p00 = (u128)a0 * b0, p01 = (u128)a0 * b1, p10 = (u128)a1 * b0, p11 = (u128)a1 * b1;
     const u128 mid = (u128)hi64(p00) + lo64(p01) + lo64(p10);
+    const u128 top = p11 + hi64(p01) + hi64(p10) + hi64(mid);
+    constexpr int s = F - 64;
+    return (top << (64 - s)) | (lo64(mid) >> s);
+}
+
+// (a * b) >> F without the low partial product a_lo b_lo: three 64x64
+// products instead of four, at most 2^(128-F) + 1 units below the exact value.
+template <int F>
+SP_HD u128 mulq3(u128 a, u128 b) {
+    const uint64_t a0 = lo64(a), a1 = hi64(a), b0 = lo64(b), b1 = hi64(b);
+    const u128 p01 = (u128)a0 * b1, p10 = (u128)a1 * b0, p11 = (u128)a1 * b1;
+    const u128 mid = (u128)lo64(p01) + lo64(p10);
     const u128 top = p11 + hi64(p01) + hi64(p10) + hi64(mid);
     constexpr int s = F - 64;
     return (top << (64 - s)) | (lo64(mid) >> s);
@@ -283,12 +297,12 @@ SP_HD double cr_exp(double x, unsigned* hard) {
     const W2 coef[11] = SP_CR_EXP_COEF;                         // 1/2! .. 1/12!
     u128 acc = mk(coef[10]);
 #pragma unroll
-    for (int i = 9; i >= 0; --i) acc = mk(coef[i]) + mulq<126>(d, acc);
-    const u128 em1 = mulq<126>(d, ((u128)1 << 126) + mulq<126>(d, acc));  // exp(d) - 1
+    for (int i = 9; i >= 0; --i) acc = mk(coef[i]) + mulq3<126>(d, acc);
+    const u128 em1 = mulq3<126>(d, ((u128)1 << 126) + mulq3<126>(d, acc));  // exp(d) - 1
     const ExpRow row = exp_row(j + 90);
     const u128 t = mk(row.hi, row.lo);
-    const u128 v = t + mulq<126>(t, em1);
-    return round_fixed(v, 126 - k, 16 + 768 * ak, hard);
+    const u128 v = t + mulq3<126>(t, em1);
+    return round_fixed(v, 126 - k, 128 + 768 * ak, hard);  // 13 three-product multiplies: <= 5 units each
 }
 
 // log1p for a > -1 from the correctly rounded ln (Goldberg's correction):
@@ -319,32 +333,37 @@ SP_HD double cr_cos(double t, unsigned* hard) {
     const u128 kp = pio2 * (uint64_t)k;
     const bool neg = T < kp;
     const u128 a = neg ? kp - T : T - kp;
-    int j = (int)(a >> 118);
-    uint64_t err = 16;
-    if (j > 101) {  // cannot happen for |t - k pi/2| <= pi/4 + 2^-40
-        j = 101;
+    int j = (int)(a >> 116);  // floor(512 a)
+    uint64_t err = 512;
+    if (j > 403) {  // cannot happen for |t - k pi/2| <= pi/4 + 2^-40
+        j = 403;
         err = ~0ULL;
     }
-    const u128 d = a - ((u128)j << 118);
-    const u128 w = mulq<125>(d, d);
-    const W2 cc[6] = SP_CR_COS_COEF;  // 1/2!, 1/4!, ..., 1/12!
-    const W2 sc[6] = SP_CR_SIN_COEF;  // 1/3!, 1/5!, ..., 1/13!
-    u128 accc = mk(cc[5]), accs = mk(sc[5]);
-#pragma unroll
-    for (int i = 4; i >= 0; --i) {
-        accc = mk(cc[i]) - mulq<125>(w, accc);
-        accs = mk(sc[i]) - mulq<125>(w, accs);
-    }
-    const u128 cm = mulq<125>(w, accc);              // 1 - cos d
-    const u128 sd = d - mulq<125>(d, mulq<125>(w, accs));  // sin d
+    const u128 d = a - ((u128)j << 116);                    // [0, 2^-9)
+    const u128 w = mulq3<125>(d, d);                        // < 2^-18
+    const uint64_t w64 = (uint64_t)(w >> 61);               // w in Q0.64
+    const W2 cc[3] = SP_CR_COS_COEF;                        // 1/2!, 1/4!, 1/6!
+    const W2 sc[3] = SP_CR_SIN_COEF;                        // 1/3!, 1/5!, 1/7!
+    const uint64_t ct[2] = SP_CR_COS_TAIL, st[2] = SP_CR_SIN_TAIL;  // 1/8!, 1/10! and 1/9!, 1/11! (Q0.64)
+    // Horner in w: the innermost level in 64 bits (its error is scaled by w^4 <= 2^-72)
+    const uint64_t c4 = ct[0] - (uint64_t)(((u128)w64 * ct[1]) >> 64);
+    const uint64_t s4 = st[0] - (uint64_t)(((u128)w64 * st[1]) >> 64);
+    u128 accc = mk(cc[2]) - mulq3<125>(w, (u128)c4 << 61);
+    u128 accs = mk(sc[2]) - mulq3<125>(w, (u128)s4 << 61);
+    accc = mk(cc[1]) - mulq3<125>(w, accc);
+    accs = mk(sc[1]) - mulq3<125>(w, accs);
+    accc = mk(cc[0]) - mulq3<125>(w, accc);
+    accs = mk(sc[0]) - mulq3<125>(w, accs);
+    const u128 cm = mulq3<125>(w, accc);                      // 1 - cos d
+    const u128 sd = d - mulq3<125>(d, mulq3<125>(w, accs));   // sin d
     const CosRow row = cos_row(j);
     const u128 c0 = mk(row.ch, row.cl), s0 = mk(row.sh, row.sl);
     const int q = k & 3;
     u128 v;
     if ((q & 1) == 0)
-        v = c0 - mulq<125>(c0, cm) - mulq<125>(s0, sd);  // cos a
+        v = c0 - mulq3<125>(c0, cm) - mulq3<125>(s0, sd);  // cos a
     else
-        v = s0 - mulq<125>(s0, cm) + mulq<125>(c0, sd);  // sin a
+        v = s0 - mulq3<125>(s0, cm) + mulq3<125>(c0, sd);  // sin a
     // cos t = cos a, -sign(z) sin a, -cos a, sign(z) sin a for q = 0..3
     const bool negative = (q == 2) || (q == 1 && !neg) || (q == 3 && neg);
     const double r = round_fixed(v, 125, err, hard);

@@ -11,8 +11,8 @@ ln (format Q8.120, value = integer * 2^-120):
   The tail coefficients 1/j (j = 8..15) are Q0.64.
 exp (format Q2.126): exp(j/256) for j = -90..90, ln 2 (Q12.116) and 1/k!.
 cos (format Q3.125):
-  cos(j/128) and sin(j/128) for j = 0..101, pi/2, and the Taylor
-  coefficients 1/k! of the cos (k = 2..12) and sin (k = 3..13) series.
+  cos(j/512) and sin(j/512) for j = 0..403, pi/2, and the Taylor
+  coefficients 1/k! of the cos (k = 2..10) and sin (k = 3..11) series.
 """
 import os
 
@@ -67,20 +67,24 @@ def main():
     w("")
     # ---------------------------------------------------------------- cos
     rows = []
-    for j in range(102):
-        a = mp.mpf(j) / 128
+    for j in range(404):
+        a = mp.mpf(j) / 512
         rows.append(f"    {{{words(fixed(mp.cos(a), F_COS))}, {words(fixed(mp.sin(a), F_COS))}}}, ")
-    w("// cos: rows {cos(j/128) hi, lo, sin(j/128) hi, lo}, j = 0..101")
+    w("// cos: rows {cos(j/512) hi, lo, sin(j/512) hi, lo}, j = 0..403")
     w("#define SP_CR_COS_ROWS \\")
     w("    { \\")
     for r in rows:
         w(r + " \\")
     w("    }")
     w(f"#define SP_CR_PIO2 {words(fixed(mp.pi / 2, F_COS))}")
+    w("// Taylor coefficients: 1/2!, 1/4!, 1/6! and 1/3!, 1/5!, 1/7! in Q3.125; the tails 1/8!, 1/10!")
+    w("// and 1/9!, 1/11! in Q0.64")
     w("#define SP_CR_COS_COEF \\")
-    w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_COS))}}}" for k in range(2, 13, 2)) + " }")
+    w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_COS))}}}" for k in (2, 4, 6)) + " }")
     w("#define SP_CR_SIN_COEF \\")
-    w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_COS))}}}" for k in range(3, 14, 2)) + " }")
+    w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_COS))}}}" for k in (3, 5, 7)) + " }")
+    w("#define SP_CR_COS_TAIL { " + ", ".join(f"0x{fixed(1 / mp.factorial(k), 64, 64):016x}ULL" for k in (8, 10)) + " }")
+    w("#define SP_CR_SIN_TAIL { " + ", ".join(f"0x{fixed(1 / mp.factorial(k), 64, 64):016x}ULL" for k in (9, 11)) + " }")
     # ---------------------------------------------------------------- exp
     w("")
     w("// exp: rows {exp(j/256) hi, lo} for j = -90..90 (Q2.126), ln 2 in Q12.116,")
