@@ -473,6 +473,34 @@ int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_config* cfg,
                         char* err, size_t err_len);
 
 /* ---------------------------------------------------------------------- */
+/* Batched fixed-step linear transients (solve_transient, solver.rs:41-252): */
+/* the DC operating point of each sample (the Newton path, cfg as for       */
+/* sp_newton_dc), then num_steps = ceil(tstop / tstep) steps of BE, TRAP or */
+/* TR-BDF2 with the reference's companion models (companion.rs).  Circuits  */
+/* are linear (R, C, L, V, I; V and I may carry a PULSE).  Transient        */
+/* unknowns: nodes, then the V-source currents in element order.            */
+/* ---------------------------------------------------------------------- */
+enum sp_transient_method { SP_TRAN_BE = 0, SP_TRAN_TRAP = 1, SP_TRAN_TRBDF2 = 2 };
+typedef struct sp_transient_config {
+    double tstep, tstop;
+    int32_t method;     /* sp_transient_method                                   */
+    int32_t probe;      /* transient unknown recorded at every step, -1: none    */
+    int32_t precision;  /* SP_PREC_FP64 or SP_PREC_FP64_EXACT                    */
+    int32_t reserved;
+} sp_transient_config;
+
+/* x[count][nt] = state at the last step; probe[count][num_steps + 1] (when
+ * probe >= 0); status: the DC status, or SP_ST_SINGULAR when a step's solve
+ * hit a zero pivot (probe entries after it are NaN). */
+int sp_transient_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_config* dc_cfg,
+                        const sp_transient_config* tc, uint64_t seed, uint64_t first_index,
+                        uint64_t count, const double* d_table, uint32_t table_cols, double* d_x,
+                        double* d_probe, uint8_t* d_status, void* stream);
+int sp_transient(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* dc_cfg,
+                 const sp_transient_config* tc, uint64_t seed, uint64_t first_index, uint64_t count,
+                 const double* table, uint32_t table_cols, double* x, double* probe, uint8_t* status);
+
+/* ---------------------------------------------------------------------- */
 /* Learned Newton warm start (no counterpart in the reference).            */
 /* A BF16 MLP n_in -> n_layers x n_hidden (GELU) -> n_out, trained and run */
 /* on the tensor cores with FP32 accumulation; FP32 master weights + Adam. */

@@ -88,6 +88,8 @@ def _bind(L):
         "or_grid_solve": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(C.c_uint8), P(d), i32]),
         "or_grid_sinks": (None, [vp_, u64, u32, P(i32), P(d)]),
         "or_histogram": (None, [P(d), u64, u32, u32, vp_, d, d, u32, P(u64)]),
+        "or_transient": (None, [P(abi.SpCircuit), P(abi.SpNewtonConfig), u64, u64, u64, P(d), u32, i32, d, d, i32,
+                                P(d), P(d), P(C.c_uint8), i32]),
         "or_yield": (None, [P(d), u64, u32, vp_, vp_, u32, P(u64)]),
         "or_ladder_transient": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(i32), P(i32), P(C.c_uint8),
                                        P(d), i32]),
@@ -237,3 +239,21 @@ def yield_counts(values, specs, status=None):
     lib().or_yield(_dp(v), v.shape[0], v.shape[1], None if st is None else st.ctypes.data, C.addressof(arr),
                    len(specs), out.ctypes.data_as(C.POINTER(C.c_uint64)))
     return out
+
+
+def transient(circuit, cfg, seed, count, method, h, tstop, probe_idx=-1, first=0, table=None, threads=0):
+    """Oracle fixed-step linear transients: (x[count][nt], probe[count][steps+1] or None, status)."""
+    import math
+    nt = circuit.num_nodes + sum(1 for e in circuit.elements if e["kind"] == 4)
+    steps = int(math.ceil(tstop / h))
+    x = np.zeros((count, nt))
+    pr = np.zeros((count, steps + 1)) if probe_idx >= 0 else None
+    st = np.zeros(count, np.uint8)
+    cols = 0
+    if table is not None:
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        cols = table.shape[1]
+    cc = circuit.to_c()
+    lib().or_transient(C.byref(cc), C.byref(cfg), seed, first, count, _dp(table), cols, method, h, tstop, probe_idx,
+                       _dp(x), _dp(pr), st.ctypes.data_as(C.POINTER(C.c_uint8)), threads)
+    return x, pr, st

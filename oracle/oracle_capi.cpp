@@ -262,6 +262,33 @@ void or_grid_sinks(const sp_grid_config* c, uint64_t seed, uint32_t inst, int32_
     }
 }
 
+// Fixed-step linear transients of samples first..first+count-1: the DC
+// operating point by the DC pipeline, then solve_transient.  x[count][nt],
+// probe[count][steps + 1] (probe_idx < 0: none), status SP_ST_*.
+void or_transient(const sp_circuit* c, const sp_newton_config* cfg, uint64_t seed, uint64_t first, uint64_t count,
+                  const double* table, uint32_t cols, int method, double h, double tstop, int probe_idx, double* x,
+                  double* probe, uint8_t* status, int threads) {
+    const int n = c->num_nodes + c->num_branches, np = c->num_params;
+    const int nt = c->num_nodes + num_vsources(*c);
+    const long steps = (long)std::ceil(tstop / h);
+    parallel_for(count, threads, [&](int, uint64_t lo, uint64_t hi) {
+        Mna m;
+        m.init(c->num_nodes, c->num_branches);
+        std::vector<double> P(np), dc(n);
+        for (uint64_t i = lo; i < hi; ++i) {
+            const double* row = table ? table + i * cols : nullptr;
+            for (int k = 0; k < np; ++k) P[k] = draw_param(c->params[k], seed, (uint32_t)(first + i), row);
+            int it = 0;
+            uint8_t st = dc_pipeline(*c, P.data(), *cfg, nullptr, dc.data(), &it, m);
+            if ((st & SP_ST_MASK) == SP_ST_CONVERGED &&
+                !linear_transient(*c, P.data(), dc.data(), method, h, tstop, x + i * nt, probe_idx,
+                                  probe ? probe + i * (steps + 1) : nullptr))
+                st = SP_ST_SINGULAR;
+            status[i] = st;
+        }
+    });
+}
+
 // Section draws of ladder instance `inst` (R, C with room for max_sections).
 int or_ladder_draw(const sp_ladder_config* c, uint64_t seed, uint32_t inst, double* R, double* C) {
     Ladder L = ladder_draw(*c, seed, inst);

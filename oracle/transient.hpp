@@ -300,3 +300,180 @@ inline LadderOutcome ladder_transient(const sp_ladder_config& c, const Ladder& L
 }
 
 }  // namespace oracle
+
+namespace oracle {
+
+// ---------------------------------------------------------------------------
+// Fixed-step linear transient, solve_transient (solver.rs:41-252): the
+// circuit's R, V and I stamped at t = step h (stamp_at_time, element order),
+// then the capacitor and inductor companions (companion.rs, capacitors
+// first), one dense solve per step (two for TR-BDF2), the states updated with
+// the reference's own update rules (update, update_trbdf2_intermediate —
+// including the TR-BDF2 inductor update's v_prev term as written).
+// Unknowns: nodes + V-source currents (inductors carry no branch variable);
+// the capacitor voltages, inductor currents and the initial solution come
+// from the DC operating point dc[] (nodes + every DC branch, V and L).
+// ---------------------------------------------------------------------------
+struct TranState {
+    double v_prev = 0, i_prev = 0, pp = 0;  // pp: v_prev_prev (C) or i_prev_prev (L)
+};
+
+inline double wave_value(const sp_circuit& c, const sp_element& el, const double* P, double t) {
+    if (el.wave >= 0 && el.wave < c.num_pulses) return eval_pulse(c.pulses[el.wave], t);
+    return P[el.field[0]];
+}
+
+// Transient-MNA branch index of V source element e (order among V sources).
+inline int vsource_index(const sp_circuit& c, int e) {
+    int k = 0;
+    for (int i = 0; i < e; ++i) k += c.elements[i].kind == SP_EL_V;
+    return k;
+}
+
+inline int num_vsources(const sp_circuit& c) { return vsource_index(c, c.num_elements); }
+
+inline void stamp_static(const sp_circuit& c, const double* P, double t, Mna& m) {
+    for (int e = 0; e < c.num_elements; ++e) {
+        const sp_element& el = c.elements[e];
+        const int* nd = el.node;
+        if (el.kind == SP_EL_R) m.conductance(nd[0], nd[1], 1.0 / P[el.field[0]]);
+        else if (el.kind == SP_EL_V) m.voltage_source(nd[0], nd[1], vsource_index(c, e), wave_value(c, el, P, t));
+        else if (el.kind == SP_EL_I) m.current_source(nd[0], nd[1], wave_value(c, el, P, t));
+    }
+}
+
+// method: 0 BE, 1 TRAP, 2 TR-BDF2.  x[n_t] = state at tstop; probe[steps + 1]
+// = unknown `probe_idx` at every step (nullptr or probe_idx < 0: none).
+// Returns false when a solve hit a zero pivot.
+inline bool linear_transient(const sp_circuit& c, const double* P, const double* dc, int method, double h,
+                             double tstop, double* x, int probe_idx, double* probe) {
+    const int nn = c.num_nodes, nt = nn + num_vsources(c);
+    std::vector<int> cap_el, ind_el;
+    for (int e = 0; e < c.num_elements; ++e) {
+        if (c.elements[e].kind == SP_EL_C) cap_el.push_back(e);
+        if (c.elements[e].kind == SP_EL_L) ind_el.push_back(e);
+    }
+    auto node = [&](const double* v, int i) { return i >= 0 ? v[i] : 0.0; };
+    std::vector<TranState> cs(cap_el.size()), is(ind_el.size());
+    for (size_t k = 0; k < cap_el.size(); ++k) {
+        const sp_element& el = c.elements[cap_el[k]];
+        cs[k].v_prev = node(dc, el.node[0]) - node(dc, el.node[1]);
+    }
+    for (size_t k = 0; k < ind_el.size(); ++k) {
+        const sp_element& el = c.elements[ind_el[k]];
+        is[k].v_prev = node(dc, el.node[0]) - node(dc, el.node[1]);
+        is[k].i_prev = dc[nn + el.branch];
+    }
+    for (int i = 0; i < nn; ++i) x[i] = dc[i];
+    for (int e = 0; e < c.num_elements; ++e)
+        if (c.elements[e].kind == SP_EL_V) x[nn + vsource_index(c, e)] = dc[nn + c.elements[e].branch];
+    const long steps = (long)std::ceil(tstop / h);
+    if (probe && probe_idx >= 0) probe[0] = x[probe_idx];
+    Mna m;
+    m.init(nn, nt - nn);
+    const double gamma = kTrbdf2Gamma;
+    auto vc = [&](const sp_element& el, const double* s) { return node(s, el.node[0]) - node(s, el.node[1]); };
+    auto stamp_cap = [&](int kind, double hh) {  // 0 BE, 1 TRAP, 2 BDF2 stage
+        for (size_t k = 0; k < cap_el.size(); ++k) {
+            const sp_element& el = c.elements[cap_el[k]];
+            const double C = P[el.field[0]];
+            double geq, ieq;
+            if (kind == 0) {
+                geq = C / hh;
+                ieq = geq * cs[k].v_prev;
+            } else if (kind == 1) {
+                geq = 2.0 * C / hh;
+                ieq = geq * cs[k].v_prev + cs[k].i_prev;
+            } else {
+                const double h2 = (1.0 - gamma) * hh, h1 = gamma * hh, rho = h2 / h1, denom = 1.0 + 2.0 * rho;
+                const double a1 = (1.0 + rho) * (1.0 + rho) / denom, a2 = -rho * rho / denom, b0 = (1.0 + rho) / denom;
+                geq = C / (b0 * h2);
+                ieq = geq * (a1 * cs[k].v_prev + a2 * cs[k].pp);
+            }
+            m.conductance(el.node[0], el.node[1], geq);
+            m.current_source(el.node[1], el.node[0], ieq);
+        }
+        for (size_t k = 0; k < ind_el.size(); ++k) {
+            const sp_element& el = c.elements[ind_el[k]];
+            const double L = P[el.field[0]];
+            double geq, ieq;
+            if (kind == 0) {
+                geq = hh / L;
+                ieq = is[k].i_prev;
+            } else if (kind == 1) {
+                geq = hh / (2.0 * L);
+                ieq = is[k].i_prev + geq * is[k].v_prev;
+            } else {
+                const double h2 = (1.0 - gamma) * hh, h1 = gamma * hh, rho = h2 / h1, denom = 1.0 + 2.0 * rho;
+                const double a1 = (1.0 + rho) * (1.0 + rho) / denom, a2 = -rho * rho / denom, b0 = (1.0 + rho) / denom;
+                geq = b0 * h2 / L;
+                ieq = a1 * is[k].i_prev + a2 * is[k].pp;
+            }
+            m.conductance(el.node[0], el.node[1], geq);
+            m.current_source(el.node[0], el.node[1], ieq);
+        }
+    };
+    auto solve = [&](double* out) {
+        std::vector<double> A = m.A, b = m.b;
+        if (!lu_solve(nt, A.data(), b.data())) return false;
+        for (int i = 0; i < nt; ++i) out[i] = b[i];
+        return true;
+    };
+    auto update = [&](const double* s, double hh, int meth) {  // CapacitorState/InductorState::update
+        const double alpha = (1.0 - gamma) / (gamma * (2.0 - gamma));
+        for (size_t k = 0; k < cap_el.size(); ++k) {
+            const double C = P[c.elements[cap_el[k]].field[0]], v = vc(c.elements[cap_el[k]], s);
+            TranState& q = cs[k];
+            if (meth == 0) q.i_prev = C / hh * (v - q.v_prev);
+            else if (meth == 1) q.i_prev = 2.0 * C / hh * (v - q.v_prev) - q.i_prev;
+            else q.i_prev = C / hh * ((1.0 + alpha) * v - (1.0 + 2.0 * alpha) * q.v_prev + alpha * q.pp);
+            q.pp = q.v_prev;
+            q.v_prev = v;
+        }
+        for (size_t k = 0; k < ind_el.size(); ++k) {
+            const double L = P[c.elements[ind_el[k]].field[0]], v = vc(c.elements[ind_el[k]], s);
+            TranState& q = is[k];
+            if (meth == 0) q.i_prev += hh / L * v;
+            else if (meth == 1) q.i_prev += hh / (2.0 * L) * (v + q.v_prev);
+            else q.i_prev += hh / L * ((1.0 + alpha) * v - (1.0 + 2.0 * alpha) * q.v_prev + alpha * q.v_prev);
+            q.pp = q.i_prev;
+            q.v_prev = v;
+        }
+    };
+    std::vector<double> sg(nt);
+    for (long step = 1; step <= steps; ++step) {
+        const double t = (double)step * h;
+        m.clear();
+        stamp_static(c, P, t, m);
+        if (method == 2) {
+            const double hg = gamma * h;
+            stamp_cap(1, hg);
+            if (!solve(sg.data())) return false;
+            for (size_t k = 0; k < cap_el.size(); ++k) {  // update_trbdf2_intermediate
+                const double C = P[c.elements[cap_el[k]].field[0]], v = vc(c.elements[cap_el[k]], sg.data());
+                TranState& q = cs[k];
+                q.pp = q.v_prev;
+                q.i_prev = 2.0 * C / hg * (v - q.pp) - q.i_prev;
+                q.v_prev = v;
+            }
+            for (size_t k = 0; k < ind_el.size(); ++k) {
+                const double L = P[c.elements[ind_el[k]].field[0]], v = vc(c.elements[ind_el[k]], sg.data());
+                TranState& q = is[k];
+                q.pp = q.i_prev;
+                q.i_prev += hg / (2.0 * L) * (v + q.v_prev);
+                q.v_prev = v;  // solver.rs:214: ind.v_prev = v after the intermediate update
+            }
+            m.clear();
+            stamp_static(c, P, t, m);
+            stamp_cap(2, h);
+        } else {
+            stamp_cap(method, h);
+        }
+        if (!solve(x)) return false;
+        update(x, h, method);
+        if (probe && probe_idx >= 0) probe[step] = x[probe_idx];
+    }
+    return true;
+}
+
+}  // namespace oracle

@@ -168,6 +168,21 @@ def newton_config(
     return c
 
 
+SP_TRAN_BE, SP_TRAN_TRAP, SP_TRAN_TRBDF2 = 0, 1, 2
+
+
+class SpTransientConfig(C.Structure):
+    _fields_ = [("tstep", C.c_double), ("tstop", C.c_double), ("method", C.c_int32), ("probe", C.c_int32),
+                ("precision", C.c_int32), ("reserved", C.c_int32)]
+
+
+def transient_config(tstep: float, tstop: float, method: int = SP_TRAN_BE, probe: int = -1,
+                     precision: int = SP_PREC_FP64) -> SpTransientConfig:
+    """Fixed-step transient settings (TransientParams, solver.rs): step, stop time, method, the transient
+    unknown recorded at every step (-1: none) and SP_PREC_FP64 or SP_PREC_FP64_EXACT."""
+    return SpTransientConfig(tstep, tstop, method, probe, precision, 0)
+
+
 class SpLadderConfig(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("tstop", "h_init", "h_min", "h_max", "lte_reltol", "lte_abstol",
                                           "v_reltol", "v_abstol", "i_abstol", "r_lo", "r_hi", "c_lo", "c_hi",

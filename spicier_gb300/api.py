@@ -256,6 +256,35 @@ class Context:
                                                            _vp(accepted), _vp(rejected), _vp(iterations),
                                                            _vp(status), _vp(probe), stream))
 
+    # -- fixed-step linear transients -----------------------------------------
+    def transient(self, circuit: Circuit, dc_cfg: abi.SpNewtonConfig, cfg: abi.SpTransientConfig, seed: int,
+                  count: int, first: int = 0, table=None) -> dict:
+        """Host-buffer batched fixed-step transients (sp_transient, solve_transient): dict of x (state at the
+        last step, [count][nodes + V sources]), probe ([count][steps + 1] when cfg.probe >= 0), status."""
+        nv = sum(1 for e in circuit.elements if e["kind"] == abi.SP_EL_V)
+        nt = circuit.num_nodes + nv
+        steps = int(np.ceil(cfg.tstop / cfg.tstep))
+        out = dict(x=np.zeros((count, nt)), status=np.zeros(count, np.uint8),
+                   probe=np.zeros((count, steps + 1)) if cfg.probe >= 0 else None)
+        cols = 0
+        if table is not None:
+            table = np.ascontiguousarray(table, dtype=np.float64)
+            cols = table.shape[1]
+        cc = circuit.to_c()
+        check(self._ptr, load().sp_transient(self._ptr, C.byref(cc), C.byref(dc_cfg), C.byref(cfg), seed, first,
+                                             count, _vp(table), cols, _vp(out["x"]), _vp(out["probe"]),
+                                             _vp(out["status"])))
+        return out
+
+    def transient_device(self, topo: Topology, dc_cfg, cfg, seed, count, x, status, probe=None, first: int = 0,
+                         table=None, stream: int = 0):
+        """Device-buffer variant (torch CUDA tensors): x [count][nt] f64, status uint8 [count],
+        probe [count][steps + 1] f64."""
+        cols = 0 if table is None else int(table.shape[1])
+        check(self._ptr, load().sp_transient_device(self._ptr, topo._ptr, C.byref(dc_cfg), C.byref(cfg), seed,
+                                                    first, count, _vp(table), cols, _vp(x), _vp(probe),
+                                                    _vp(status), stream))
+
     # -- power-grid corners ----------------------------------------------------
     def grid_solve(self, cfg, seed: int, count: int, first: int = 0) -> dict:
         """Host-buffer power-grid corner sweep (sp_grid_solve): dict of x [count][rows*cols+1],

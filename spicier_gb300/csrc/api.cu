@@ -9,6 +9,7 @@
 
 #include "internal.h"
 #include "ladder.cuh"
+#include "transient_fixed.cuh"
 #include "powergrid.cuh"
 
 using namespace sp;
@@ -122,6 +123,7 @@ int sp_ctx_destroy(sp_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaDeviceSynchronize();
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->aux) cudaFree(ctx->aux);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
     for (auto& r : ctx->recs) {
@@ -1047,6 +1049,150 @@ int sp_yield_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t
     ProfScope prof(ctx, "yield", st);
     SP_CUDA(ctx, launch_yield(d_values, rows, ld, d_status, d_specs, num_specs, d_pass, ctx->num_sms, st), "yield launch");
     return SP_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Fixed-step linear transients (transient_fixed.cuh)
+// ---------------------------------------------------------------------------
+static int ensure_aux(sp_ctx* ctx, size_t bytes) {
+    if (bytes <= ctx->aux_bytes) return SP_OK;
+    if (ctx->aux) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronise before buffer growth");
+        cudaFree(ctx->aux);
+        ctx->aux = nullptr;
+        ctx->aux_bytes = 0;
+    }
+    const size_t want = align256(bytes + bytes / 4);
+    cudaError_t e = cudaMalloc(&ctx->aux, want);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "buffer allocation");
+    ctx->aux_bytes = want;
+    return SP_OK;
+}
+
+static int transient_locked(sp_ctx* ctx, sp_topology* t, const sp_newton_config* dc_cfg,
+                            const sp_transient_config* tc, uint64_t seed, uint64_t first, uint64_t count,
+                            const double* d_table, uint32_t cols, double* d_x, double* d_probe, uint8_t* d_status,
+                            cudaStream_t st) {
+    int nv = 0, ncap = 0, nind = 0;
+    for (const sp_element& el : t->h_elements) {
+        const int k = el.kind;
+        if (k != SP_EL_R && k != SP_EL_C && k != SP_EL_L && k != SP_EL_V && k != SP_EL_I)
+            return fail(ctx, SP_ERR_INVALID_ARGUMENT, "fixed-step transients take linear circuits (R, C, L, V, I), as "
+                                                      "solve_transient");
+        nv += k == SP_EL_V;
+        ncap += k == SP_EL_C;
+        nind += k == SP_EL_L;
+    }
+    const int nt = t->num_nodes + nv;
+    const long steps = (long)std::ceil(tc->tstop / tc->tstep);
+    const size_t words = transient_words(nt, ncap, nind);
+    int block = 128;
+    while (block > 1 && words * 8 * block > 110 * 1024) block >>= 1;
+    if (words * 8 * block > (size_t)ctx->max_smem) return fail(ctx, SP_ERR_INVALID_DIMENSION, "circuit too large");
+    const int ndc = t->n, np = t->num_params;
+    const size_t bx = align256(8 * (size_t)ndc * count), bp = align256(8 * (size_t)std::max(np, 1) * count);
+    int rc = ensure_aux(ctx, bx + bp);
+    if (rc) return rc;
+    double* x_dc = (double*)ctx->aux;
+    double* params = (double*)((char*)ctx->aux + bx);
+    sp_newton_config dcc = *dc_cfg;
+    dcc.precision = tc->precision;
+    rc = newton_dc_locked(ctx, t, &dcc, seed, first, count, d_table, cols, nullptr, x_dc, nullptr, d_status, nullptr,
+                          params, nullptr, st);
+    if (rc) return rc;
+    TransientLaunch L{};
+    L.c = t->dc;
+    L.params = params;
+    L.np = np;
+    L.x_dc = x_dc;
+    L.count = count;
+    L.method = tc->method;
+    L.h = tc->tstep;
+    L.tstop = tc->tstop;
+    L.steps = steps;
+    L.nt = nt;
+    L.num_caps = ncap;
+    L.num_inds = nind;
+    L.probe_idx = tc->probe;
+    L.x = d_x;
+    L.probe = d_probe;
+    L.status = d_status;
+    ProfScope prof(ctx, tc->precision == SP_PREC_FP64_EXACT ? "transient_fixed_exact" : "transient_fixed_fp64", st);
+    const size_t smem = words * 8 * block;
+    if (tc->precision == SP_PREC_FP64_EXACT) SP_CUDA(ctx, launch_transient_exact(L, block, smem, st), "transient launch");
+    else SP_CUDA(ctx, launch_transient_fast(L, block, smem, st), "transient launch");
+    return SP_OK;
+}
+
+static int transient_validate(sp_ctx* ctx, const sp_transient_config* tc) {
+    if (!tc) return SP_ERR_INVALID_ARGUMENT;
+    if (!(tc->tstep > 0) || !(tc->tstop > 0) || tc->tstop / tc->tstep > 1e8)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad tstep/tstop");
+    if (tc->method < SP_TRAN_BE || tc->method > SP_TRAN_TRBDF2) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "unknown method");
+    if (tc->precision != SP_PREC_FP64 && tc->precision != SP_PREC_FP64_EXACT)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "precision must be SP_PREC_FP64 or SP_PREC_FP64_EXACT");
+    return SP_OK;
+}
+
+int sp_transient_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_config* dc_cfg,
+                        const sp_transient_config* tc, uint64_t seed, uint64_t first_index, uint64_t count,
+                        const double* d_table, uint32_t table_cols, double* d_x, double* d_probe, uint8_t* d_status,
+                        void* stream) {
+    if (!ctx || !topo || !dc_cfg || !d_x || !d_status) return SP_ERR_INVALID_ARGUMENT;
+    if (topo->ctx != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "topology belongs to another context");
+    int rc = transient_validate(ctx, tc);
+    if (rc) return rc;
+    if (tc->probe >= 0 && !d_probe) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "probe requested without a buffer");
+    if (count == 0) return SP_OK;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    return transient_locked(ctx, const_cast<sp_topology*>(topo), dc_cfg, tc, seed, first_index, count, d_table,
+                            table_cols, d_x, tc->probe >= 0 ? d_probe : nullptr, d_status, (cudaStream_t)stream);
+}
+
+int sp_transient(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* dc_cfg,
+                 const sp_transient_config* tc, uint64_t seed, uint64_t first_index, uint64_t count,
+                 const double* table, uint32_t table_cols, double* x, double* probe, uint8_t* status) {
+    if (!ctx || !circuit || !dc_cfg || !x || !status) return SP_ERR_INVALID_ARGUMENT;
+    int rc = transient_validate(ctx, tc);
+    if (rc) return rc;
+    if (tc->probe >= 0 && !probe) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "probe requested without a buffer");
+    if (count == 0) return SP_OK;
+    sp_topology* t = nullptr;
+    rc = sp_topology_create(ctx, circuit, &t);
+    if (rc) return rc;
+    int nv = 0;
+    for (int e = 0; e < circuit->num_elements; ++e) nv += circuit->elements[e].kind == SP_EL_V;
+    const size_t nt = (size_t)circuit->num_nodes + nv;
+    const long steps = (long)std::ceil(tc->tstop / tc->tstep);
+    double *dx = nullptr, *dp = nullptr, *dt = nullptr;
+    uint8_t* ds = nullptr;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMalloc(&dx, 8 * nt * count);
+    if (e == cudaSuccess) e = cudaMalloc(&ds, count);
+    if (e == cudaSuccess && tc->probe >= 0) e = cudaMalloc(&dp, 8 * (size_t)(steps + 1) * count);
+    if (e == cudaSuccess && table) e = cudaMalloc(&dt, 8 * (size_t)table_cols * count);
+    if (e == cudaSuccess && table) e = cudaMemcpy(dt, table, 8 * (size_t)table_cols * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        ScratchOrder order(ctx, ctx->stream);
+        rc = transient_locked(ctx, t, dc_cfg, tc, seed, first_index, count, dt, table_cols, dx, dp, ds, ctx->stream);
+        if (rc == SP_OK) {
+            e = cudaMemcpyAsync(x, dx, 8 * nt * count, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(status, ds, count, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess && dp)
+                e = cudaMemcpyAsync(probe, dp, 8 * (size_t)(steps + 1) * count, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        }
+    }
+    for (void* p : {(void*)dx, (void*)dp, (void*)dt, (void*)ds})
+        if (p) cudaFree(p);
+    sp_topology_destroy(t);
+    if (rc) return rc;
+    return e == cudaSuccess ? SP_OK : cuda_fail(ctx, e, "transient copies");
 }
 
 }  // extern "C"

@@ -34,6 +34,9 @@ cudaError_t launch_histogram(const double* v, uint64_t rows, uint32_t ld, uint32
                              double mn, double mx, uint32_t nb, uint64_t* bins, int num_sms, cudaStream_t st);
 cudaError_t launch_yield(const double* v, uint64_t rows, uint32_t ld, const uint8_t* status,
                          const sp_yield_spec* d_specs, uint32_t ns, uint64_t* pass, int num_sms, cudaStream_t st);
+struct TransientLaunch;
+cudaError_t launch_transient_exact(const TransientLaunch& L, int block, size_t smem, cudaStream_t st);
+cudaError_t launch_transient_fast(const TransientLaunch& L, int block, size_t smem, cudaStream_t st);
 struct LadderLaunch;
 struct GridLaunch;
 cudaError_t launch_grid(const GridLaunch& L, int precision, cudaStream_t st);
@@ -107,6 +110,10 @@ struct sp_ctx {
         int nnz = 0;
     };
     std::map<std::string, Spec> spec_cache;
+    // second grow-only buffer for entry points that run the Newton path (which
+    // owns `scratch`) and keep their own data across it
+    void* aux = nullptr;
+    size_t aux_bytes = 0;
 };
 
 // Brackets one kernel launch with events when the context is profiling.

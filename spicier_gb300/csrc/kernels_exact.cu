@@ -6,6 +6,7 @@
 
 #include "rng.cuh"
 #include "ladder.cuh"
+#include "transient_fixed.cuh"
 
 namespace sp {
 
@@ -132,6 +133,12 @@ cudaError_t launch_ladder_exact(const LadderLaunch& L, int grid, size_t smem, cu
     return cudaGetLastError();
 }
 
+cudaError_t launch_transient_exact(const TransientLaunch& L, int block, size_t smem, cudaStream_t st) {
+    const unsigned grid = (unsigned)((L.count + block - 1) / block);
+    SP_KERNEL_NS::transient_fixed_kernel<<<grid, block, smem, st>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t prepare_exact_kernels(int max_smem) {
     cudaError_t e;
     e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>,
@@ -139,6 +146,8 @@ cudaError_t prepare_exact_kernels(int max_smem) {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(SP_KERNEL_NS::transient_fixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);

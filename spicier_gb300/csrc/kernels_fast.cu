@@ -8,6 +8,7 @@
 #define SP_KERNEL_NS kfast
 #include "internal.h"
 #include "ladder.cuh"
+#include "transient_fixed.cuh"
 #include "powergrid.cuh"
 #include <algorithm>
 
@@ -429,9 +430,16 @@ cudaError_t launch_grid(const GridLaunch& L, int precision, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_transient_fast(const TransientLaunch& L, int block, size_t smem, cudaStream_t st) {
+    const unsigned grid = (unsigned)((L.count + block - 1) / block);
+    SP_KERNEL_NS::transient_fixed_kernel<<<grid, block, smem, st>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t prepare_fast_kernels(int max_smem) {
     const void* fns[] = {
         (const void*)SP_KERNEL_NS::grid_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::grid_kernel<SP_PREC_FP64>,
+        (const void*)SP_KERNEL_NS::transient_fixed_kernel,
         (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_MIXED>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
