@@ -238,6 +238,22 @@ void sp_newton_config_default(sp_newton_config* c) {
 // ---------------------------------------------------------------------------
 // solve_batch
 // ---------------------------------------------------------------------------
+static int ensure_aux(sp_ctx* ctx, size_t bytes) {
+    if (bytes <= ctx->aux_bytes) return SP_OK;
+    if (ctx->aux) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronise before buffer growth");
+        cudaFree(ctx->aux);
+        ctx->aux = nullptr;
+        ctx->aux_bytes = 0;
+    }
+    const size_t want = align256(bytes + bytes / 4);
+    cudaError_t e = cudaMalloc(&ctx->aux, want);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "buffer allocation");
+    ctx->aux_bytes = want;
+    return SP_OK;
+}
+
 static int solve_batch_device_locked(sp_ctx* ctx, const double* d_m, const double* d_r, size_t n,
                                      size_t batch, double* d_x, uint8_t* d_s, int precision,
                                      int refine_steps, cudaStream_t st) {
@@ -246,9 +262,25 @@ static int solve_batch_device_locked(sp_ctx* ctx, const double* d_m, const doubl
     if (batch > ctx->cfg.max_batch_per_launch)
         return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %zu exceeds maximum %llu", batch,
                     (unsigned long long)ctx->cfg.max_batch_per_launch);
-    if (n > (size_t)kMaxDenseN)
+    if (n > (size_t)kMaxBatchLuN)
         return fail(ctx, SP_ERR_INVALID_DIMENSION, "n = %zu exceeds the batched dense LU limit %d", n,
-                    kMaxDenseN);
+                    kMaxBatchLuN);
+    if (n > (size_t)kMaxDenseN) {
+        // one CTA per system, FP64 in the reference's order (both precisions)
+        ProfScope prof(ctx, "lu_batch_cta", st);
+        double* work = nullptr;
+        int grid = (int)std::min<size_t>(batch, (size_t)ctx->num_sms * 8);
+        if (lu_batch_cta_smem((int)n) > (size_t)ctx->max_smem - 1024) {
+            const size_t per = lu_batch_cta_smem((int)n);
+            grid = (int)std::max<size_t>(1, std::min<size_t>({batch, (size_t)ctx->num_sms * 2, ((size_t)4 << 30) / per}));
+            int rc = ensure_aux(ctx, per * grid);
+            if (rc) return rc;
+            work = (double*)ctx->aux;
+        }
+        cudaError_t e = launch_lu_batch_cta(d_m, d_r, (int)n, batch, d_x, d_s, work, grid, st);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "solve_batch launch");
+        return SP_OK;
+    }
     ProfScope prof(ctx, precision == SP_PREC_MIXED ? "lu_batch_mixed" : "lu_batch_fp64", st);
     cudaError_t e = (precision == SP_PREC_MIXED)
                         ? launch_lu_batch_mixed(d_m, d_r, (int)n, batch, d_x, d_s, refine_steps, st)
@@ -265,6 +297,7 @@ int sp_solve_batch_device(sp_ctx* ctx, const double* d_matrices, const double* d
         return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null buffer");
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
     return solve_batch_device_locked(ctx, d_matrices, d_rhs, n, batch, d_solutions, d_singular_flags,
                                      precision, refine_steps, (cudaStream_t)stream);
 }
@@ -281,6 +314,7 @@ int sp_solve_batch(sp_ctx* ctx, const double* matrices, const double* rhs, size_
     size_t bm = align256(batch * n * n * 8), br = align256(batch * n * 8), bs = align256(batch);
     int rc = ensure_scratch(ctx, bm + 2 * br + bs);
     if (rc) return rc;
+    ScratchOrder order(ctx, ctx->stream);
     char* base = (char*)ctx->scratch;
     double* d_m = (double*)base;
     double* d_r = (double*)(base + bm);
@@ -447,7 +481,7 @@ struct NewtonScratch {
     double* params;
     double* derived;
     uint32_t* fail_list;
-    unsigned int* counters;  // [0] fail count, [1] undecided roundings
+    unsigned int* counters;  // [0] fail count, [1] undecided roundings, [2..3] work counter
     sp_moments* partial;
     uint32_t moment_blocks;
     double* x0;   // learned warm starts [count][n] (when requested)
@@ -518,7 +552,8 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     NewtonScratch s;
     int rc = newton_scratch(ctx, t, count, s, warm != nullptr);
     if (rc) return rc;
-    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 8, st), "clear counters");
+    // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64)
+    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 16, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
                  s.counters + 1};
     {
@@ -542,6 +577,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     L.resid = d_resid;
     L.fail_list = s.fail_list;
     L.fail_count = s.counters;
+    L.work_next = reinterpret_cast<unsigned long long*>(s.counters + 2);
     const int kprec = prec == SP_PREC_MIXED ? SP_PREC_MIXED : SP_PREC_FP64;
     size_t per = kprec == SP_PREC_MIXED ? work_bytes_per_thread<SP_PREC_MIXED>(t->n)
                                         : work_bytes_per_thread<SP_PREC_FP64>(t->n);
@@ -728,7 +764,8 @@ int sp_rng_fill_device(sp_ctx* ctx, int kind, uint64_t seed, uint64_t first_inde
 
 int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld, uint32_t cols,
                       const uint8_t* d_status, sp_moments* d_out, void* stream) {
-    if (!ctx || !d_values || !d_out) return SP_ERR_INVALID_ARGUMENT;
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    if (!d_out || (rows && !d_values)) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null buffer");
     if (cols > ld) return fail(ctx, SP_ERR_INVALID_DIMENSION, "cols > ld");
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaSetDevice(ctx->device);
@@ -1055,22 +1092,6 @@ int sp_yield_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t
 // ---------------------------------------------------------------------------
 // Fixed-step linear transients (transient_fixed.cuh)
 // ---------------------------------------------------------------------------
-static int ensure_aux(sp_ctx* ctx, size_t bytes) {
-    if (bytes <= ctx->aux_bytes) return SP_OK;
-    if (ctx->aux) {
-        cudaError_t e = cudaDeviceSynchronize();
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronise before buffer growth");
-        cudaFree(ctx->aux);
-        ctx->aux = nullptr;
-        ctx->aux_bytes = 0;
-    }
-    const size_t want = align256(bytes + bytes / 4);
-    cudaError_t e = cudaMalloc(&ctx->aux, want);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "buffer allocation");
-    ctx->aux_bytes = want;
-    return SP_OK;
-}
-
 static int transient_locked(sp_ctx* ctx, sp_topology* t, const sp_newton_config* dc_cfg,
                             const sp_transient_config* tc, uint64_t seed, uint64_t first, uint64_t count,
                             const double* d_table, uint32_t cols, double* d_x, double* d_probe, uint8_t* d_status,

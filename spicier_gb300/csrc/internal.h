@@ -55,6 +55,12 @@ cudaError_t launch_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t pa
 cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, uint64_t batch,
                                   double* sol, uint8_t* sing, cudaStream_t st);
 cudaError_t prepare_exact_kernels(int max_smem);
+// solve_batch for n > kMaxDenseN: one CTA per system (shared memory when
+// lu_batch_cta_smem(n) fits, else work = grid slices of n*n + n doubles)
+constexpr int kMaxBatchLuN = 4096;
+size_t lu_batch_cta_smem(int n);
+cudaError_t launch_lu_batch_cta(const double* mats, const double* rhs, int n, uint64_t batch, double* sol,
+                                uint8_t* sing, double* work, int grid, cudaStream_t st);
 
 // kernels_fast.cu (FMA allowed)
 cudaError_t launch_newton_fast(int prec, const NewtonLaunch& L, bool fallback, int grid, int block,
@@ -108,6 +114,7 @@ struct sp_ctx {
         cudaKernel_t kernel = nullptr;
         std::string log;
         int nnz = 0;
+        int blocks_per_sm = 1;  // resident 128-thread blocks (the persistent grid)
     };
     std::map<std::string, Spec> spec_cache;
     // second grow-only buffer for entry points that run the Newton path (which
@@ -164,6 +171,7 @@ struct sp_topology {
     cudaKernel_t spec_kernel[2] = {nullptr, nullptr};  // owned by the context's cache
     std::string spec_log[2];
     int spec_nnz[2] = {0, 0};
+    int spec_bpsm[2] = {1, 1};
 };
 
 namespace sp {

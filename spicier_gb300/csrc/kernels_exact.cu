@@ -128,6 +128,130 @@ cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, 
     return cudaGetLastError();
 }
 
+// The same solve for n beyond the one-thread-per-system limit: one CTA per
+// system.  Each step's pivot search (warp 0: first index of the largest
+// |a|, NaN never chosen, the diagonal kept when it is NaN), row swap,
+// scaling and rank-1 update touch every element in the order and with the
+// operations of lu_solve_fp64, only spread over threads, so the solution is
+// bit-identical.  A and b live in shared memory when they fit, else in a
+// per-CTA slice of global memory (work).
+__global__ void __launch_bounds__(256) lu_batch_cta_kernel(const double* __restrict__ mats,
+                                                           const double* __restrict__ rhs, int n, uint64_t batch,
+                                                           double* __restrict__ sol, uint8_t* __restrict__ sing,
+                                                           double* __restrict__ work) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_piv[2];
+    __shared__ double s_diag[2];
+    __shared__ int s_bad;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    const size_t nn = (size_t)n * n;
+    double* A = work ? work + (size_t)blockIdx.x * (nn + n) : reinterpret_cast<double*>(smem);
+    double* b = A + nn;
+    for (uint64_t s = blockIdx.x; s < batch; s += gridDim.x) {
+        const double* m = mats + s * nn;
+        for (size_t k = tid; k < nn; k += blockDim.x) A[k] = m[k];
+        for (int k = tid; k < n; k += blockDim.x) b[k] = rhs[s * n + k];
+        __syncthreads();
+        for (int i = 0; i < n; ++i) {
+            double* col = A + (size_t)i * n;  // column i: entries (r, i), r = 0..n-1
+            if (wid == 0) {
+                int piv = i;
+                if (!isnan(col[i])) {
+                    double best = -1.0;
+                    int bi = n;
+                    for (int r = i + lane; r < n; r += 32) {
+                        const double v = fabs(col[r]);
+                        if (v > best) {
+                            best = v;
+                            bi = r;
+                        }
+                    }
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) {
+                        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                        if (ob > best || (ob == best && oi < bi)) {
+                            best = ob;
+                            bi = oi;
+                        }
+                    }
+                    piv = bi;
+                }
+                if (lane == 0) {
+                    s_piv[i & 1] = piv;
+                    s_diag[i & 1] = col[piv];
+                }
+            }
+            __syncthreads();
+            const int piv = s_piv[i & 1];
+            const double diag = s_diag[i & 1];
+            if (diag == 0.0) continue;
+            if (piv != i) {
+                for (int c = tid; c < n; c += blockDim.x) {
+                    double* cc = A + (size_t)c * n;
+                    const double t = cc[i];
+                    cc[i] = cc[piv];
+                    cc[piv] = t;
+                }
+                if (tid == 0) {
+                    const double t = b[i];
+                    b[i] = b[piv];
+                    b[piv] = t;
+                }
+                __syncthreads();
+            }
+            const double inv = 1.0 / diag;
+            for (int r = i + 1 + tid; r < n; r += blockDim.x) col[r] = col[r] * inv;
+            __syncthreads();
+            for (int c = i + 1 + wid; c < n; c += nw) {
+                double* cc = A + (size_t)c * n;
+                const double p = cc[i];
+                for (int r = i + 1 + lane; r < n; r += 32) cc[r] = -p * col[r] + cc[r];
+            }
+            __syncthreads();
+        }
+        // substitutions by warp 0 (warp-synchronous)
+        if (wid == 0) {
+            for (int i = 0; i < n; ++i) {
+                const double coeff = b[i];
+                const double* col = A + (size_t)i * n;
+                for (int r = i + 1 + lane; r < n; r += 32) b[r] = -coeff * col[r] + b[r];
+                __syncwarp();
+            }
+            bool ok = true;
+            for (int i = n - 1; i >= 0; --i) {
+                const double* col = A + (size_t)i * n;
+                const double diag = col[i];
+                if (diag == 0.0) {
+                    ok = false;
+                    break;
+                }
+                const double coeff = b[i] / diag;
+                __syncwarp();
+                if (lane == 0) b[i] = coeff;
+                for (int r = lane; r < i; r += 32) b[r] = -coeff * col[r] + b[r];
+                __syncwarp();
+            }
+            if (lane == 0) s_bad = ok ? 0 : 1;
+        }
+        __syncthreads();
+        const bool bad = s_bad != 0;
+        for (int k = tid; k < n; k += blockDim.x) sol[s * n + k] = bad ? 0.0 : b[k];
+        if (tid == 0) sing[s] = bad ? 1 : 0;
+        __syncthreads();  // before the next system overwrites A and b
+    }
+}
+
+size_t lu_batch_cta_smem(int n) { return ((size_t)n * n + n) * 8; }
+
+cudaError_t launch_lu_batch_cta(const double* mats, const double* rhs, int n, uint64_t batch, double* sol,
+                                uint8_t* sing, double* work, int grid, cudaStream_t st) {
+    if (batch == 0) return cudaSuccess;
+    const size_t smem = work ? 0 : lu_batch_cta_smem(n);
+    lu_batch_cta_kernel<<<grid, 256, smem, st>>>(mats, rhs, n, batch, sol, sing, work);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ladder_exact(const LadderLaunch& L, int grid, size_t smem, cudaStream_t st) {
     SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT><<<grid, 128, smem, st>>>(L);
     return cudaGetLastError();
@@ -151,6 +275,8 @@ cudaError_t prepare_exact_kernels(int max_smem) {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(lu_batch_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - 1024);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(lu_batch_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 max_smem);

@@ -226,8 +226,16 @@ __global__ void moments_final_kernel(const sp_moments* __restrict__ partial, uin
 // (cp = cols rounded up to a power of two) over rows t / cp, t / cp + 256 / cp,
 // ... of the block's chunk, so a warp reads whole rows (coalesced); the
 // groups of a column are then merged in a fixed order, and the chunks'
-// partials by the final kernel: the result depends only on rows and cols.
-constexpr int kMomChunk = 1024;
+// partials by the tree kernel.  The chunk length is a function of rows alone
+// (about two chunks per SM), so the result depends only on rows and cols.
+constexpr int kMomChunkMin = 64;
+
+__host__ __device__ inline uint64_t moments_chunk(uint64_t rows, uint32_t max_blocks) {
+    const uint64_t target = max_blocks < 304 ? max_blocks : 304;
+    uint64_t chunk = (rows + target - 1) / target;
+    chunk = (chunk + kMomChunkMin - 1) / kMomChunkMin * kMomChunkMin;
+    return chunk < kMomChunkMin ? kMomChunkMin : chunk;
+}
 
 // Order-preserving integer key of a double (IEEE bits with the negative half
 // reflected): min/max run on the integer pipe; NaN never reaches here.
@@ -240,31 +248,43 @@ __device__ __forceinline__ double from_key(long long k) {
 }
 
 __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
-                                                           uint32_t cols, uint32_t cp,
+                                                           uint32_t cols, uint32_t cp, uint64_t chunk,
                                                            const uint8_t* __restrict__ status,
                                                            sp_moments* __restrict__ partial) {
     __shared__ sp_moments sh[256];
     const uint32_t c = threadIdx.x % cp, g = threadIdx.x / cp, groups = 256 / cp;
-    const uint64_t lo = (uint64_t)blockIdx.x * kMomChunk, hi = min(rows, lo + kMomChunk);
+    const uint64_t lo = (uint64_t)blockIdx.x * chunk, hi = min(rows, lo + chunk);
     sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
     long long kmin = order_key(CUDART_INF), kmax = order_key(-CUDART_INF);
     if (c < cols) {
-        for (uint64_t i = lo + g; i < hi; i += groups) {
-            if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
-            const double x = v[i * ld + c];
-            m.count += 1;
-            m.sum += x;
-            m.sum_sq += x * x;
-            const long long k = order_key(x);
-            kmin = k < kmin ? k : kmin;
-            kmax = k > kmax ? k : kmax;
+        // loads first (four rows in flight per thread), then the fixed-order accumulation
+        for (uint64_t i0 = lo + g; i0 < hi; i0 += 4 * (uint64_t)groups) {
+            double xs[4];
+            bool ok[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint64_t i = i0 + (uint64_t)u * groups;
+                ok[u] = i < hi && (!status || (status[i] & SP_ST_MASK) == SP_ST_CONVERGED);
+                xs[u] = ok[u] ? v[i * ld + c] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!ok[u]) continue;
+                const double x = xs[u];
+                m.count += 1;
+                m.sum += x;
+                m.sum_sq += x * x;
+                const long long k = order_key(x);
+                kmin = k < kmin ? k : kmin;
+                kmax = k > kmax ? k : kmax;
+            }
         }
     }
     m.min = from_key(kmin);
     m.max = from_key(kmax);
     sh[threadIdx.x] = m;
     __syncthreads();
-    // pairwise tree over the groups (fixed order; FP64 latency, not count, bounds this)
+    // pairwise tree over the groups (fixed order)
     for (uint32_t w = groups / 2; w >= 1; w >>= 1) {
         if (g < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w * cp]);
         __syncthreads();
@@ -293,11 +313,16 @@ cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uin
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
                            cudaStream_t st) {
     if (cols == 0) return cudaSuccess;
-    if (cols <= 32 && (rows + kMomChunk - 1) / kMomChunk <= nblocks) {
+    if (rows == 0) {  // empty accumulators (count 0, min +inf, max -inf)
+        moments_tree_kernel<<<cols, 256, 0, st>>>(partial, 0, out);
+        return cudaGetLastError();
+    }
+    const uint64_t chunk = moments_chunk(rows, nblocks);
+    if (cols <= 32 && (rows + chunk - 1) / chunk <= nblocks) {
         uint32_t cp = 1;
         while (cp < cols) cp <<= 1;
-        const uint32_t nb = (uint32_t)((rows + kMomChunk - 1) / kMomChunk);
-        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, status, partial);
+        const uint32_t nb = (uint32_t)((rows + chunk - 1) / chunk);
+        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, chunk, status, partial);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         moments_tree_kernel<<<cols, 256, 0, st>>>(partial, nb, out);

@@ -4,27 +4,30 @@
 // layer's BF16 weight matrix W[N][K] is packed once, on the device, into the
 // tensor cores' K-major 128-byte-swizzled layout (8-row x 128-byte atoms,
 // 16-byte chunks XOR-ed with the row), so a CTA fills its shared memory with
-// one linear copy.  Two teams of 256 threads each own a 128-sample tile, an activation
-// buffer in the same layout and 128 TMEM columns; a team is 8 warps, warp w
-// reading TMEM lanes 32 (w % 4).. (its sample rows) and column half w / 4:
+// one linear copy.  Up to four teams of 128 threads (four warps, warp q
+// reading TMEM lanes 32q..32q+31) each own a 128-sample tile, an activation
+// buffer in the same layout and 128 TMEM columns; thread t of a team owns
+// sample row t of its tile from input to output:
 //
-//   stage inputs  thread t of the team = sample row: centred parameters
-//                 p - in_mean in FP32 (kept in registers for the FP32 linear
-//                 term; relative error ~2^-24 / |p/in_mean - 1|), scaled to
-//                 BF16 and written as row t of the A operand;
+//   stage inputs  centred parameters p - in_mean in FP32 (kept in registers
+//                 for the FP32 linear term; relative error ~2^-24 /
+//                 |p/in_mean - 1|), scaled to BF16 and written as row t of
+//                 the A operand;
 //   per layer     one thread issues K/16 tcgen05.mma (M=128, N=layer width,
 //                 K=16, BF16 x BF16 -> FP32 in TMEM) and commits them to the
 //                 team's mbarrier; after the wait every thread reads its
-//                 TMEM lane (tcgen05.ld 32x32b), adds the bias, applies GELU
-//                 and writes the BF16 activations back as the next layer's A;
+//                 TMEM lane 32 columns at a time (tcgen05.ld 32x32b.x32),
+//                 adds the bias, applies GELU and writes the BF16
+//                 activations back as the next layer's A;
 //   output        x0[k] = out_mean[k] + out_scale[k] y[k]
 //                         + sum_j lin[k][j] (p_j - in_mean[j])    (FP32, then FP64)
 //
-// While one team runs its epilogue the other's MMAs run, so the tensor
-// cores and the CUDA cores overlap.  Every mbarrier wait is bounded: on a
-// timeout the team fills its remaining samples' x0 with NaN (the Newton
-// path then restarts those samples cold), raises the error flag, and the CTA
-// frees its TMEM before it returns.
+// With four teams a 65,536-sample sweep is one tile per team on 128 SMs: the
+// teams' MMAs, TMEM reads and epilogues interleave on the SM, and no team
+// waits for a second tile.  Every mbarrier wait is bounded: on a timeout the
+// team fills its remaining samples' x0 with NaN (the Newton path then
+// restarts those samples cold), raises the error flag, and the CTA frees
+// its TMEM before it returns.
 //
 // Scope: n_in <= 32, n_out <= 32, hidden width 64 or 128, 1..4 hidden layers;
 // the mma.sync kernel in mlp.cu serves every other shape.
@@ -39,9 +42,9 @@ namespace mlptc {
 
 namespace {
 
-constexpr int kTile = 128;     // samples per tile = MMA M
-constexpr int kTeam = 256;      // threads per tile: 8 warps, two per TMEM lane quarter
-constexpr int kThreads = 512;  // two tiles in flight
+constexpr int kTile = 128;      // samples per tile = MMA M
+constexpr int kTeam = 128;      // threads per tile: 4 warps, one per TMEM lane quarter
+constexpr int kMaxTeams = 4;    // tiles in flight per CTA (512 TMEM columns)
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -96,13 +99,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return true;
 }
 
-// Named barrier of one team (256 threads) that also ANDs a predicate across it.
+// Named barrier of one team (128 threads) that also ANDs a predicate across it.
 __device__ __forceinline__ bool team_all(int id, bool v) {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\t"
         "setp.ne.b32 q, %1, 0;\n\t"
-        "bar.red.and.pred p, %2, 256, q;\n\t"
+        "bar.red.and.pred p, %2, 128, q;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(r)
         : "r"((uint32_t)v), "r"(id)
@@ -110,26 +113,27 @@ __device__ __forceinline__ bool team_all(int id, bool v) {
     return r != 0;
 }
 
-__device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
-    uint32_t r[16];
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
+    uint32_t r[32];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr)
         : "memory");
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
-
 
 // FP64 <-> FP32 conversions on the integer pipe (GB300's FP64 pipe issues
 // conversions slowly, and the kernel converts every input and output).
@@ -188,23 +192,31 @@ struct Carve {
     uint32_t abuf, bias, lin, io, mbar, tslot, total;
 };
 
-__host__ __device__ inline Carve carve(const Args& a) {
+__host__ __device__ inline Carve carve(const Args& a, int teams) {
     Carve c;
     c.abuf = (uint32_t)a.img_bytes;                       // multiple of 1024
-    c.bias = c.abuf + 2u * kAbytes;
+    c.bias = c.abuf + (uint32_t)teams * kAbytes;
     c.lin = c.bias + 4u * (uint32_t)a.bias_total;
     c.io = c.lin + 4u * (uint32_t)(a.n_out * a.n_in);
     c.mbar = (c.io + 4u * (uint32_t)(2 * (a.n_in + a.n_out)) + 7u) & ~7u;
-    c.tslot = c.mbar + 16u;
+    c.tslot = c.mbar + 8u * kMaxTeams;
     c.total = c.tslot + 16u;
     return c;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
+constexpr uint32_t kSmemLimit = 227u * 1024u;
+
+__host__ __device__ inline int teams_for(const Args& a) {
+    for (int t = kMaxTeams; t >= 1; --t)
+        if (1024u + carve(a, t).total <= kSmemLimit) return t;
+    return 0;
+}
+
+__global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int teams) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte alignment of the swizzled operands (the dynamic window may start lower)
     unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
-    const Carve cv = carve(a);
+    const Carve cv = carve(a, teams);
     unsigned char* wimg = sm;
     float* bias_s = reinterpret_cast<float*>(sm + cv.bias);
     float* lin_s = reinterpret_cast<float*>(sm + cv.lin);
@@ -212,22 +224,25 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + cv.mbar);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + cv.tslot);
 
-    // team = tile slot (0/1); warp w of a team reads TMEM lanes 32 (w % 4)..+31
-    // (sample rows) and the column half w / 4 of every layer's output
-    const int tid = threadIdx.x, team = tid / kTeam, tt = tid % kTeam, warp = tid >> 5;
-    const int quarter = (tt >> 5) & 3, half = tt >> 7, row = quarter * 32 + (tid & 31);
-    for (int i = tid; i < a.img_bytes / 16; i += kThreads)
+    // team = tile slot; warp q of a team reads TMEM lanes 32q..32q+31 (its sample rows)
+    const int tid = threadIdx.x, nthreads = teams * kTeam, team = tid / kTeam, tt = tid % kTeam, warp = tid >> 5;
+    const int quarter = tt >> 5, row = tt;
+    for (int i = tid; i < a.img_bytes / 16; i += nthreads)
         reinterpret_cast<uint4*>(wimg)[i] = __ldg(reinterpret_cast<const uint4*>(a.img) + i);
-    for (int i = tid; i < a.bias_total; i += kThreads) bias_s[i] = a.bias[i];
-    for (int i = tid; i < a.n_out * a.n_in; i += kThreads) lin_s[i] = a.lin ? a.lin[i] : 0.f;
-    for (int i = tid; i < 2 * (a.n_in + a.n_out); i += kThreads) io_s[i] = a.io[i];
+    for (int i = tid; i < a.bias_total; i += nthreads) bias_s[i] = a.bias[i];
+    for (int i = tid; i < a.n_out * a.n_in; i += nthreads) lin_s[i] = a.lin ? a.lin[i] : 0.f;
+    // in_mean, 1 / in_scale, out_mean, out_scale
+    for (int i = tid; i < 2 * (a.n_in + a.n_out); i += nthreads)
+        io_s[i] = (i >= a.n_in && i < 2 * a.n_in) ? 1.0f / a.io[i] : a.io[i];
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
+        for (int t = 0; t < teams; ++t)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[t])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    const uint32_t tcols = teams > 2 ? 512u : (teams > 1 ? 256u : 128u);
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot))
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(tcols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -241,43 +256,39 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
     const uint32_t abuf_s = smem_u32(abuf), wimg_s = smem_u32(wimg), mb = smem_u32(&mbar[team]);
     const int bar_id = 1 + team;
     const float* in_mean = io_s;
-    const float* in_scale = io_s + a.n_in;
+    const float* in_rscale = io_s + a.n_in;
     const float* out_mean = io_s + 2 * a.n_in;
     const float* out_scale = out_mean + a.n_out;
 
     const int ntiles = (a.rows + kTile - 1) / kTile;
     uint32_t phase = 0;
     bool ok = true;
-    int tile = blockIdx.x * 2 + team;
-    for (; tile < ntiles; tile += gridDim.x * 2) {
+    int tile = blockIdx.x * teams + team;
+    for (; tile < ntiles; tile += gridDim.x * teams) {
         const int s = tile * kTile + row;
         const bool live = s < a.rows;
-        // inputs: half 0 writes chunks 0..3 of row `row` (inputs 0..31, kept in
-        // registers for the linear term), half 1 the zero chunks 4..7
+        // inputs 0..31 of row `row` (chunks 0..3, kept in registers for the
+        // linear term); chunks 4..7 of the first K-block are zero
         float pc[kMaxIn];
 #pragma unroll
         for (int j = 0; j < kMaxIn; ++j)
-            pc[j] = (half == 0 && j < a.n_in && live)
-                        ? f64_to_f32(a.params_soa[(size_t)a.slots[j] * a.stride + s]) - in_mean[j]
-                        : 0.f;
-        if (half == 0) {
+            pc[j] = (j < a.n_in && live) ? f64_to_f32(a.params_soa[(size_t)a.slots[j] * a.stride + s]) - in_mean[j]
+                                         : 0.f;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                uint32_t w[4];
+        for (int c = 0; c < 4; ++c) {
+            uint32_t w[4];
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    const int j = c * 8 + 2 * h;
-                    const float x0v = j < a.n_in ? pc[j] / in_scale[j] : 0.f;
-                    const float x1v = j + 1 < a.n_in ? pc[j + 1] / in_scale[j + 1] : 0.f;
-                    w[h] = pack2(x0v, x1v);
-                }
-                *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+            for (int h = 0; h < 4; ++h) {
+                const int j = c * 8 + 2 * h;
+                const float x0v = j < a.n_in ? pc[j] * in_rscale[j] : 0.f;
+                const float x1v = j + 1 < a.n_in ? pc[j + 1] * in_rscale[j + 1] : 0.f;
+                w[h] = pack2(x0v, x1v);
             }
-        } else {
-#pragma unroll
-            for (int c = 4; c < 8; ++c)
-                *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
+#pragma unroll
+        for (int c = 4; c < 8; ++c)
+            *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(0u, 0u, 0u, 0u);
         for (int l = 0; l < a.L; ++l) {
             const Layer& ly = a.layer[l];
             fence_async_smem();  // generic-proxy writes of A -> visible to the tensor cores
@@ -300,29 +311,27 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
             tc_after();
             const float* bias = bias_s + ly.bias_off;
             if (l + 1 < a.L) {
-                const int hw = ly.N / 2;
-                for (int c0 = half * hw; c0 < (half + 1) * hw; c0 += 16) {
-                    float v[16];
-                    tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
-                    uint32_t w[8];
+                for (int c0 = 0; c0 < ly.N; c0 += 32) {
+                    float v[32];
+                    tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
+                    uint32_t w[16];
 #pragma unroll
-                    for (int i = 0; i < 8; ++i)
+                    for (int i = 0; i < 16; ++i)
                         w[i] = pack2(act::gelu(v[2 * i] + bias[c0 + 2 * i]),
                                      act::gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
-                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8)) =
-                        make_uint4(w[0], w[1], w[2], w[3]);
-                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8 + 1)) =
-                        make_uint4(w[4], w[5], w[6], w[7]);
-                }
-            } else if (half == 0) {
-                for (int c0 = 0; c0 < a.n_out; c0 += 16) {
-                    float v[16];
-                    tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int k = c0 + i;
-                        if (k < a.n_out && live) {
-                            float x = out_mean[k] + out_scale[k] * (v[i] + bias[k]);
+                    for (int q = 0; q < 4; ++q)
+                        *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8 + q)) =
+                            make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+                }
+            } else {
+                float v[32];
+                tmem_ld32(tmem + lane_base, v);  // the output layer is 32 wide (n_out <= 32)
+                if (live) {
+#pragma unroll
+                    for (int k = 0; k < 32; ++k) {
+                        if (k < a.n_out) {
+                            float x = out_mean[k] + out_scale[k] * (v[k] + bias[k]);
 #pragma unroll
                             for (int j = 0; j < kMaxIn; ++j)
                                 if (j < a.n_in) x = fmaf(lin_s[k * a.n_in + j], pc[j], x);
@@ -338,9 +347,9 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
     if (!ok) {
         // timeout: this team's remaining samples start cold (NaN warm start)
         if (tt == 0) atomicExch(a.err, 1);
-        for (; tile < ntiles; tile += gridDim.x * 2) {
+        for (; tile < ntiles; tile += gridDim.x * teams) {
             const int s = tile * kTile + row;
-            if (s < a.rows && half == 0)
+            if (s < a.rows)
                 for (int k = 0; k < a.n_out; ++k)
                     a.x0[(size_t)s * a.n_out + k] = __longlong_as_double(0x7ff8000000000000LL);
         }
@@ -351,7 +360,8 @@ __global__ void __launch_bounds__(kThreads, 1) infer_kernel(Args a) {
     __syncthreads();
     tc_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(*tmem_slot) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tmem_slot), "r"(tcols)
+                     : "memory");
 }
 
 }  // namespace
@@ -381,7 +391,10 @@ int plan(int n_in, int n_out, int hidden, int gemm_layers, Args* a) {
     return off;
 }
 
-size_t smem_bytes(const Args& a) { return 1024 + (size_t)carve(a).total; }
+size_t smem_bytes(const Args& a) {
+    const int t = teams_for(a);
+    return t ? 1024 + (size_t)carve(a, t).total : 0;
+}
 
 cudaError_t pack(const __nv_bfloat16* wt, const size_t* woff, const Args& a, void* img, cudaStream_t st) {
     for (int l = 0; l < a.L; ++l) {
@@ -397,17 +410,19 @@ cudaError_t launch(const Args& a, int num_sms, cudaStream_t st) {
     static bool configured[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
-    const size_t smem = smem_bytes(a);
+    const int teams = teams_for(a);
+    if (teams == 0) return cudaErrorInvalidValue;
+    const size_t smem = 1024 + (size_t)carve(a, teams).total;
     if (dev < 64 && !configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
         if (e != cudaSuccess) return e;
         configured[dev] = true;
     }
     const int ntiles = (a.rows + kTile - 1) / kTile;
-    int grid = (ntiles + 1) / 2;
+    int grid = (ntiles + teams - 1) / teams;
     if (grid > num_sms) grid = num_sms;
     if (grid < 1) return cudaSuccess;
-    infer_kernel<<<grid, kThreads, smem, st>>>(a);
+    infer_kernel<<<grid, teams * kTeam, smem, st>>>(a, teams);
     return cudaGetLastError();
 }
 

@@ -281,6 +281,7 @@ struct NewtonLaunch {
     double* resid;          // [count] or nullptr
     uint32_t* fail_list;    // [count]
     unsigned int* fail_count;
+    unsigned long long* work_next = nullptr;  // zeroed work counter of the persistent kernels
 };
 
 __device__ inline void load_start(const NewtonLaunch& L, size_t s, Work& w, bool warm) {

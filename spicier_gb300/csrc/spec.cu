@@ -16,11 +16,16 @@
 //
 // The iteration is the correction form of the mixed-precision kernel: FP64
 // device currents and KCL residual F(x) (current form: each element adds
-// its current, not G*x - b), FP32 Jacobian and LU for the step, FP64 update
-// and convergence test (check_convergence, newton.rs:134-159).  With
-// precision SP_PREC_FP64 the Jacobian and LU are FP64 instead.
+// its current, not G*x - b), FP32 Jacobian (device conductances evaluated
+// from an FP32 shadow of x) and LU for the step, FP64 update, and the
+// convergence test of check_convergence (newton.rs:134-159) on the FP32 step.
+// GB300's FP64 pipe is the bound of this kernel, so nothing that does not
+// need 53 bits runs on it: the region tests are sign-bit tests and the
+// FP64 <-> FP32 conversions run on the integer pipe.  With precision
+// SP_PREC_FP64 the Jacobian, LU and test are FP64 instead.
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <sstream>
@@ -179,10 +184,38 @@ struct SpecArgs {
     double* x; int* iters; unsigned char* status; double* resid;
     unsigned int* fail_list; unsigned int* fail_count;
     double reltol, vabstol, iabstol; int max_it; int fallback_any;
+    u64* next;
 };
-__device__ __forceinline__ bool spx_fin(double v) { return fabs(v) <= 1.7976931348623157e308; }
+__device__ __forceinline__ bool spx_fin(double v) {  // not Inf / NaN, on the integer pipe
+    return ((unsigned int)(__double_as_longlong(v) >> 32) & 0x7ff00000u) != 0x7ff00000u;
+}
 __device__ __forceinline__ bool spx_bad(float p, float iv) { return !(fabsf(p) > 0.f) || !(fabsf(iv) <= 3.0e38f); }
 __device__ __forceinline__ bool spx_bad(double p, double iv) { return !(fabs(p) > 0.0) || !(fabs(iv) <= 1.0e308); }
+// FP64 <-> FP32 conversions on the integer pipe (GB300's FP64 pipe issues
+// conversions at the FP64 rate); normal numbers only, the rest take cvt.
+__device__ __forceinline__ float spx_f(double x) {
+    const u64 b = (u64)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    if (e <= 0 || e >= 255) return __double2float_rn(x);
+    const u64 m = b & ((1ULL << 52) - 1);
+    unsigned int f = ((unsigned int)(b >> 32) & 0x80000000u) | ((unsigned int)e << 23) | (unsigned int)(m >> 29);
+    const u64 rem = m & ((1ULL << 29) - 1), half = 1ULL << 28;
+    f += (rem > half || (rem == half && (f & 1))) ? 1u : 0u;
+    return __uint_as_float(f);
+}
+__device__ __forceinline__ float spx_fneg(double x) { return __uint_as_float(__float_as_uint(spx_f(x)) ^ 0x80000000u); }
+__device__ __forceinline__ double spx_d(float x) {
+    const unsigned int f = __float_as_uint(x);
+    const unsigned int e = (f >> 23) & 0xff;
+    if (e == 0 || e == 255) return (double)x;
+    return __longlong_as_double((long long)(((u64)(f & 0x80000000u) << 32) | ((u64)(e - 127 + 1023) << 52) |
+                                            ((u64)(f & 0x7fffffu) << 29)));
+}
+// v < 0 from the sign bit (integer pipe); -0 is not negative
+__device__ __forceinline__ bool spx_neg(double v) {
+    const long long b = __double_as_longlong(v);
+    return b < 0 && (b << 1) != 0;
+}
 __device__ __forceinline__ double spx_lim(double vd, double nvt, double vcrit) {
     if (vd > vcrit) { double arg = (vd - vcrit) / nvt; return vcrit + nvt * (1.0 + log1p(arg)); }
     return vd;
@@ -210,10 +243,15 @@ __device__ __forceinline__ void spx_mos(bool pmos, double vth, double beta, doub
 std::string V(int node) { return node >= 0 ? "x[" + std::to_string(node) + "]" : "0.0"; }
 
 // Element currents into F (and, when jac, conductances into J).
+// mixed: the Jacobian in FP32 — MOSFET conductances from the FP32 shadow xf
+// of x and FP32 copies of the constants, other conversions on the integer pipe.
 void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P, const std::vector<int>& doff,
-                   bool jac) {
+                   bool jac, bool mixed = false) {
     const int nn = t->num_nodes;
     auto cst = [&](int e, int k) { return "c" + std::to_string(doff[e] + k); };
+    auto cstf = [&](int e, int k) { return "cf" + std::to_string(doff[e] + k); };
+    auto VF = [&](int node) { return node >= 0 ? "xf[" + std::to_string(node) + "]" : std::string("0.f"); };
+    const char* cvt = mixed ? "spx_f" : "(JT)";
     auto J = [&](int r, int c, const std::string& expr, bool neg) {
         if (r < 0 || c < 0 || !jac) return;
         o << "    J[" << P.at(r, c) << "] " << (neg ? "-=" : "+=") << " " << expr << ";\n";
@@ -255,20 +293,49 @@ void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P
                   << "    double i = id + gd * (vd - vl);\n";
                 F(a, "i", false), F(b, "i", true);
                 if (jac) {
-                    o << "    JT g = (JT)gd;\n";
+                    o << "    JT g = " << cvt << "(gd);\n";
                     J(a, a, "g", false), J(b, b, "g", false), J(a, b, "g", true), J(b, a, "g", true);
                 }
                 break;
             case SP_EL_NMOS:
             case SP_EL_PMOS: {
                 const int d = a, g = b, s = c;
-                o << "    double ids, gds, gm;\n"
-                  << "    spx_mos(" << (el.kind == SP_EL_PMOS ? "true" : "false") << ", " << cst(e, 0) << ", "
-                  << cst(e, 1) << ", " << cst(e, 2) << ", " << V(g) << " - " << V(s) << ", " << V(d) << " - "
-                  << V(s) << ", ids, gds, gm);\n";
-                F(d, "ids", false), F(s, "ids", true);
+                const bool pm = el.kind == SP_EL_PMOS;
+                if (mixed) {
+                    // level1.rs:154-248: the drain current in FP64 (it enters F), the
+                    // region from FP64 sign tests, gds and gm in FP32
+                    const std::string ng = pm ? "-" : "";
+                    // PMOS: vgs = vs - vg, vds = vs - vd (the reference negates vg - vs; only the
+                    // sign of a zero differs, and the region tests treat -0 as 0)
+                    auto dif = [&](int p, int q) { return pm ? V(q) + " - " + V(p) : V(p) + " - " + V(q); };
+                    o << "    double vgs = " << dif(g, s) << ", vds = " << dif(d, s) << ";\n"
+                      << "    double vov = vgs - " << cst(e, 0) << ";\n"
+                      << "    bool on = !spx_neg(vov), lin = on && spx_neg(vds - vov);\n"
+                      << "    double ids = 0.0;\n"
+                      << "    if (on) { double q = 1.0 + " << cst(e, 2) << " * vds;\n"
+                      << "      ids = lin ? " << cst(e, 1) << " * (vov * vds - 0.5 * vds * vds) * q : 0.5 * "
+                      << cst(e, 1) << " * vov * vov * q; }\n";
+                    if (pm) o << "    ids = -ids;\n";
+                    F(d, "ids", false), F(s, "ids", true);
+                    o << "    float vgsf = " << ng << "(" << VF(g) << " - " << VF(s) << "), vdsf = " << ng << "("
+                      << VF(d) << " - " << VF(s) << ");\n"
+                      << "    float vovf = vgsf - " << cstf(e, 0) << ", qf = 1.f + " << cstf(e, 2) << " * vdsf;\n"
+                      << "    float gdf = 1e-12f, gmf = 0.f;\n"
+                      << "    if (lin) { gdf = " << cstf(e, 1) << " * (vovf - vdsf) * qf + " << cstf(e, 1)
+                      << " * (vovf * vdsf - 0.5f * vdsf * vdsf) * " << cstf(e, 2) << "; gmf = " << cstf(e, 1)
+                      << " * vdsf * qf; }\n"
+                      << "    else if (on) { gdf = 0.5f * " << cstf(e, 1) << " * vovf * vovf * " << cstf(e, 2)
+                      << "; gmf = " << cstf(e, 1) << " * vovf * qf; }\n"
+                      << "    gdf = fmaxf(gdf, 1e-12f);\n";
+                } else {
+                    o << "    double ids, gds, gm;\n"
+                      << "    spx_mos(" << (pm ? "true" : "false") << ", " << cst(e, 0) << ", " << cst(e, 1) << ", "
+                      << cst(e, 2) << ", " << V(g) << " - " << V(s) << ", " << V(d) << " - " << V(s)
+                      << ", ids, gds, gm);\n";
+                    F(d, "ids", false), F(s, "ids", true);
+                    if (jac) o << "    JT gdf = (JT)gds, gmf = (JT)gm;\n";
+                }
                 if (jac) {
-                    o << "    JT gdf = (JT)gds, gmf = (JT)gm;\n";
                     J(d, d, "gdf", false), J(s, s, "gdf", false), J(d, s, "gdf", true), J(s, d, "gdf", true);
                     J(d, g, "gmf", false), J(d, s, "gmf", true), J(s, g, "gmf", true), J(s, s, "gmf", false);
                 }
@@ -300,7 +367,7 @@ void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P
                   << "    double fc = ic + gm * (vbe - vbe_ieq), fb = ib + gpi * (vbe - vbe_ieq);\n";
                 F(cn, "fc", false), F(bn, "fb", false), F(en, "(fc + fb)", true);
                 if (jac) {
-                    o << "    JT gpf = (JT)gpi, gof = (JT)go, gmf = (JT)gm;\n";
+                    o << "    JT gpf = " << cvt << "(gpi), gof = " << cvt << "(go), gmf = " << cvt << "(gm);\n";
                     J(bn, bn, "gpf", false), J(en, en, "gpf", false), J(bn, en, "gpf", true), J(en, bn, "gpf", true);
                     J(cn, cn, "gof", false), J(en, en, "gof", false), J(cn, en, "gof", true), J(en, cn, "gof", true);
                     J(cn, bn, "gmf", false), J(cn, en, "gmf", true), J(en, bn, "gmf", true), J(en, en, "gmf", false);
@@ -315,14 +382,15 @@ void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P
 }
 
 // Linear (per-sample constant) Jacobian entries, J0.
-void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pattern& P, const std::vector<int>& doff) {
+void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pattern& P, const std::vector<int>& doff,
+                          bool mixed) {
     const int nn = t->num_nodes;
-    o << "  JT J0[" << P.nnz << "];\n  #pragma unroll\n  for (int k = 0; k < " << P.nnz << "; ++k) J0[k] = (JT)0;\n";
+    o << "  #pragma unroll\n  for (int k = 0; k < " << P.nnz << "; ++k) J0[k] = (JT)0;\n";
     for (int e = 0; e < t->num_elements; ++e) {
         const sp_element& el = t->h_elements[e];
         const int a = el.node[0], b = el.node[1];
         if (el.kind == SP_EL_R) {
-            o << "  { JT g = (JT)c" << doff[e] << ";\n";
+            o << "  { JT g = " << (mixed ? "spx_f(c" : "(JT)(c") << doff[e] << ");\n";
             if (a >= 0) o << "    J0[" << P.at(a, a) << "] += g;\n";
             if (b >= 0) o << "    J0[" << P.at(b, b) << "] += g;\n";
             if (a >= 0 && b >= 0) o << "    J0[" << P.at(a, b) << "] -= g; J0[" << P.at(b, a) << "] -= g;\n";
@@ -335,6 +403,12 @@ void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pat
     }
 }
 
+// The kernel is persistent: each thread iterates one sample at a time and,
+// when its sample has converged (or failed), takes the next one from a
+// global counter (warp-aggregated atomics), so lanes whose samples converge
+// early do not idle while others iterate: the warp executes about the mean
+// iteration count per sample, not the maximum over its 32 lanes.  Which
+// thread solves a sample does not change the sample's arithmetic.
 std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     const int n = t->n, nn = t->num_nodes;
     std::vector<int> doff(t->num_elements);
@@ -345,22 +419,45 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     std::ostringstream o;
     o << kPreamble << "typedef " << (fp32_jac ? "float" : "double") << " JT;\n";
     o << "extern \"C\" __global__ void __launch_bounds__(128) spec_newton(SpecArgs a) {\n"
-      << "  const u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
+      << "  const u64 nthreads = (u64)gridDim.x * blockDim.x;\n"
+      << "  u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
       << "  if (s >= a.count) return;\n"
-      << "  const double* dv = a.dv + s; const u64 st = a.stride;\n";
-    for (int k = 0; k < t->num_derived; ++k) o << "  const double c" << k << " = __ldg(dv + " << k << " * st);\n";
-    emit_linear_jacobian(o, t, P, doff);
-    o << "  double x[" << n << "];\n"
-      << "  const bool warm = a.x0 != 0;\n"
-      << "  if (warm) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n << " + i];\n"
-      << "  } else if (a.nodeset) {\n    #pragma unroll\n    for (int i = 0; i < " << n
-      << "; ++i) x[i] = a.nodeset[i];\n"
-      << "  } else {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = 0.0;\n  }\n"
-      << "  int it = 0, code = 1;\n"
-      << "  while (it < a.max_it) {\n    ++it;\n"
+      << "  const u64 st = a.stride;\n"
+      << "  const bool warm = a.x0 != 0;\n";
+    for (int k = 0; k < t->num_derived; ++k) o << "  double c" << k << ";\n";
+    std::vector<int> fcs;
+    if (fp32_jac)
+        for (int e = 0; e < t->num_elements; ++e) {
+            const int kind = t->h_elements[e].kind;
+            if (kind != SP_EL_NMOS && kind != SP_EL_PMOS) continue;
+            for (int k = 0; k < 3; ++k) {
+                fcs.push_back(doff[e] + k);
+                o << "  float cf" << doff[e] + k << ";\n";
+            }
+        }
+    o << "  JT J0[" << P.nnz << "];\n  double x[" << n << "];\n";
+    if (fp32_jac)
+        o << "  float xf[" << n << "];\n"
+          << "  const float reltolf = spx_f(a.reltol), vabstolf = spx_f(a.vabstol), iabstolf = spx_f(a.iabstol);\n";
+    o << "  int it, code;\n";
+    // per-sample set-up: constants, linear Jacobian, start point
+    std::ostringstream ld;
+    ld << "  {\n  const double* dv = a.dv + s;\n";
+    for (int k = 0; k < t->num_derived; ++k) ld << "  c" << k << " = __ldg(dv + " << k << " * st);\n";
+    for (int k : fcs) ld << "  cf" << k << " = spx_f(c" << k << ");\n";
+    emit_linear_jacobian(ld, t, P, doff, fp32_jac);
+    ld << "  if (warm) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n
+       << " + i];\n"
+       << "  } else if (a.nodeset) {\n    #pragma unroll\n    for (int i = 0; i < " << n
+       << "; ++i) x[i] = a.nodeset[i];\n"
+       << "  } else {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = 0.0;\n  }\n";
+    if (fp32_jac) ld << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) xf[i] = spx_f(x[i]);\n";
+    ld << "  it = 0; code = 1;\n  }\n";
+    o << ld.str();
+    o << "  while (true) {\n    ++it;\n"
       << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n"
       << "    JT J[" << P.nnz << "];\n    #pragma unroll\n    for (int k = 0; k < " << P.nnz << "; ++k) J[k] = J0[k];\n";
-    emit_elements(o, t, P, doff, true);
+    emit_elements(o, t, P, doff, true, fp32_jac);
     // factorisation over the static pattern
     o << "    bool sing = false;\n";
     for (int k = 0; k < n; ++k) {
@@ -377,7 +474,7 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     // forward and back substitution on -F (rows permuted)
     o << "    JT y[" << n << "];\n";
     for (int i = 0; i < n; ++i) {
-        o << "    y[" << i << "] = (JT)(-F[" << P.perm[i] << "])";
+        o << "    y[" << i << "] = " << (fp32_jac ? "spx_fneg(F[" : "(JT)(-F[") << P.perm[i] << "])";
         for (int k = 0; k < i; ++k)
             if (P.has(i, k)) o << " - J[" << P.slot[i * n + k] << "] * y[" << k << "]";
         o << ";\n";
@@ -390,25 +487,41 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     }
     o << "    bool conv = true;\n";
     for (int i = 0; i < n; ++i) {
-        o << "    { double xo = x[" << i << "], xn = xo + (double)y[" << i << "];\n"
-          << "      conv = conv && !(fabs(xn - xo) > a.reltol * fmax(fabs(xn), fabs(xo)) + "
-          << (i < nn ? "a.vabstol" : "a.iabstol") << ");\n      x[" << i << "] = xn; }\n";
+        if (fp32_jac)  // FP64 update; the test (newton.rs:134-159) on the FP32 step and shadows
+            o << "    { double xn = x[" << i << "] + spx_d(y[" << i << "]); float xnf = spx_f(xn);\n"
+              << "      conv = conv && !(fabsf(y[" << i << "]) > reltolf * fmaxf(fabsf(xnf), fabsf(xf[" << i
+              << "])) + " << (i < nn ? "vabstolf" : "iabstolf") << ");\n      x[" << i << "] = xn; xf[" << i
+              << "] = xnf; }\n";
+        else
+            o << "    { double xo = x[" << i << "], xn = xo + (double)y[" << i << "];\n"
+              << "      conv = conv && !(fabs(xn - xo) > a.reltol * fmax(fabs(xn), fabs(xo)) + "
+              << (i < nn ? "a.vabstol" : "a.iabstol") << ");\n      x[" << i << "] = xn; }\n";
     }
-    o << "    if (sing) { code = 2; break; }\n    if (conv) { code = 0; break; }\n  }\n";
-    // status, outputs, miss list, residual
-    o << "  bool fin = true;\n  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) fin = fin && spx_fin(x[i]);\n"
-      << "  unsigned char st8 = !fin ? 3 : (code == 0 ? 0 : (code == 2 ? 2 : 1));\n"
-      << "  if (warm) st8 |= 0x10;\n"
-      << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) a.x[s * " << n << " + i] = x[i];\n"
-      << "  if (a.iters) a.iters[s] = it;\n"
-      << "  if ((st8 & 15) != 0 && (warm || a.fallback_any)) {\n"
-      << "    unsigned int k = atomicAdd(a.fail_count, 1u); a.fail_list[k] = (unsigned int)s;\n"
-      << "  } else if (a.resid) {\n"
+    o << "    code = sing ? 2 : (conv ? 0 : 1);\n"
+      << "    if (sing || conv || it >= a.max_it) {\n";
+    // status, outputs, miss list, residual of sample s
+    o << "    bool fin = true;\n    #pragma unroll\n    for (int i = 0; i < " << n
+      << "; ++i) fin = fin && spx_fin(x[i]);\n"
+      << "    unsigned char st8 = !fin ? 3 : (unsigned char)code;\n"
+      << "    if (warm) st8 |= 0x10;\n"
+      << "    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) a.x[s * " << n << " + i] = x[i];\n"
+      << "    if (a.iters) a.iters[s] = it;\n"
+      << "    if ((st8 & 15) != 0 && (warm || a.fallback_any)) {\n"
+      << "      unsigned int k = atomicAdd(a.fail_count, 1u); a.fail_list[k] = (unsigned int)s;\n"
+      << "    } else if (a.resid) {\n"
       << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n";
     emit_elements(o, t, P, doff, false);
     o << "    double r = 0.0;\n";
     for (int i = 0; i < nn; ++i) o << "    r = fmax(r, fabs(F[" << i << "]));\n";
-    o << "    a.resid[s] = r;\n  }\n  if (a.status) a.status[s] = st8;\n}\n";
+    o << "    a.resid[s] = r;\n    }\n    if (a.status) a.status[s] = st8;\n";
+    // next sample: warp-aggregated fetch from the counter
+    o << "    {\n      const unsigned m = __activemask();\n      const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;\n"
+      << "      u64 base = 0;\n      if (lane == lead) base = atomicAdd(a.next, (u64)__popc(m));\n"
+      << "      base = __shfl_sync(m, base, lead);\n"
+      << "      s = nthreads + base + (u64)__popc(m & ((1u << lane) - 1u));\n    }\n"
+      << "    if (s >= a.count) break;\n";
+    o << ld.str();
+    o << "    }\n  }\n}\n";
     return o.str();
 }
 
@@ -428,6 +541,7 @@ struct SpecArgsHost {
     double reltol, vabstol, iabstol;
     int max_it;
     int fallback_any;
+    unsigned long long* next;
 };
 
 // Build (once) the specialised kernel of topology t for `prec` (MIXED: FP32
@@ -452,6 +566,7 @@ int spec_prepare(sp_topology* t, int prec, std::string& err) {
         t->spec_kernel[slot] = hit->second.kernel;
         t->spec_log[slot] = hit->second.log;
         t->spec_nnz[slot] = hit->second.nnz;
+        t->spec_bpsm[slot] = hit->second.blocks_per_sm;
         if (!t->spec_kernel[slot]) err = t->spec_log[slot];
         return t->spec_kernel[slot] ? SP_OK : SP_ERR_BACKEND;
     }
@@ -493,6 +608,10 @@ int spec_prepare(sp_topology* t, int prec, std::string& err) {
         entry.log = t->spec_log[slot] = err = std::string("module load: ") + cudaGetErrorString(e);
         return SP_ERR_BACKEND;
     }
+    int bpsm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, (const void*)k, 128, 0) != cudaSuccess || bpsm < 1)
+        bpsm = 1;
+    entry.blocks_per_sm = t->spec_bpsm[slot] = bpsm;
     entry.lib = lib;
     entry.kernel = t->spec_kernel[slot] = k;
     entry.log = t->spec_log[slot] = log;
@@ -518,8 +637,11 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     a.iabstol = L.cfg.i_abstol;
     a.max_it = L.cfg.max_iterations;
     a.fallback_any = (L.cfg.fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE)) ? 1 : 0;
+    a.next = L.work_next;
+    if (!a.next) return cudaErrorInvalidValue;
     void* args[] = {&a};
-    const unsigned grid = (unsigned)((L.count + 127) / 128);
+    const uint64_t resident = (uint64_t)t->ctx->num_sms * (uint64_t)t->spec_bpsm[slot];
+    const unsigned grid = (unsigned)std::min<uint64_t>((L.count + 127) / 128, resident);
     return cudaLaunchKernel((const void*)t->spec_kernel[slot], dim3(grid), dim3(128), args, 0, st);
 }
 

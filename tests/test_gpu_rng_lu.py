@@ -64,12 +64,33 @@ def test_f32_variants(ctx):
     assert np.max(np.abs(g - c)) < 1e-5
 
 
-@pytest.mark.parametrize("n,batch", [(1, 33), (2, 64), (6, 1000), (12, 4097), (28, 300)])
+@pytest.mark.parametrize("n,batch", [(1, 33), (2, 64), (6, 1000), (12, 4097), (28, 300), (29, 300), (64, 200),
+                                     (100, 64), (165, 9), (200, 20)])
 def test_solve_batch_matches_reference_lu(ctx, n, batch):
     rng = np.random.default_rng(n)
     A = rng.standard_normal((batch, n, n)) + 2.0 * np.eye(n)
     b = rng.standard_normal((batch, n))
     mats = np.ascontiguousarray(A.transpose(0, 2, 1)).ravel()  # column-major
+    res = ctx.solve_batch(mats, b.ravel(), n, batch)
+    sol, sing = oracle.solve_batch(mats, b.ravel(), n, batch)
+    assert res.singular_indices == [int(i) for i in np.nonzero(sing)[0]]
+    assert np.array_equal(res.solutions.view(np.uint64), sol.view(np.uint64))
+
+
+@pytest.mark.parametrize("n", [20, 48, 180])
+def test_solve_batch_pivot_edge_cases(ctx, n):
+    """Ties, zero columns, NaN and Inf entries: the same pivots and the same bits as the reference's LU."""
+    rng = np.random.default_rng(n)
+    batch = 12
+    A = rng.integers(-3, 4, (batch, n, n)).astype(float)  # many equal magnitudes (pivot ties)
+    A[1, :, 3] = 0.0              # zero column: the step is skipped, the system singular
+    A[2, 5, 5] = np.nan           # NaN on the diagonal: kept as the pivot
+    A[3, 7, 2] = np.nan           # NaN below the diagonal: never chosen
+    A[4, 9, 9] = np.inf
+    A[5] = np.eye(n)              # identity
+    A[6, :, :] = 0.0              # all zero
+    b = rng.standard_normal((batch, n))
+    mats = np.ascontiguousarray(A.transpose(0, 2, 1)).ravel()
     res = ctx.solve_batch(mats, b.ravel(), n, batch)
     sol, sing = oracle.solve_batch(mats, b.ravel(), n, batch)
     assert res.singular_indices == [int(i) for i in np.nonzero(sing)[0]]

@@ -44,3 +44,31 @@ def test_histogram_and_yield_on_gpu(ctx):
         y = ctx.yield_device(dv, specs, status=status)
         yo = oracle.yield_counts(v, specs, status=None if status is None else st)
         assert np.array_equal(y.cpu().numpy().astype(np.uint64), yo)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rows,cols", [(0, 3), (1, 1), (63, 12), (64, 12), (65, 5), (5000, 12), (100_003, 17),
+                                       (262_144, 12), (3000, 40)])
+def test_moments_device_sizes(ctx, rows, cols):
+    """StatisticsAccumulator over converged rows (statistics.rs:127-155): exact count/min/max, sums to 1e-12."""
+    import torch
+    rng = np.random.default_rng(rows + cols)
+    v = rng.normal(0.0, 1.0, (rows, cols + 2)) * 10.0 ** rng.integers(-6, 3, cols + 2)
+    st = (rng.random(rows) < 0.05).astype(np.uint8)
+    dv = torch.tensor(v, device="cuda")
+    ds = torch.tensor(st, device="cuda")
+    out = torch.zeros(max(cols, 1) * 5, dtype=torch.float64, device="cuda")
+    for status in (None, ds):
+        ctx.moments_device(dv, rows, cols + 2, cols, status, out)
+        m = out.cpu().numpy().reshape(-1, 5)[:cols]
+        cnt = m[:, 0].copy().view(np.uint64)
+        keep = np.ones(rows, bool) if status is None else st == 0
+        for c in range(cols):
+            x = v[keep, c]
+            assert cnt[c] == x.size
+            if x.size == 0:
+                assert m[c, 1] == 0.0 and m[c, 3] == np.inf and m[c, 4] == -np.inf
+                continue
+            assert m[c, 3] == x.min() and m[c, 4] == x.max()
+            assert abs(m[c, 1] - x.sum()) <= 1e-12 * np.abs(x).sum()
+            assert abs(m[c, 2] - (x * x).sum()) <= 1e-12 * (x * x).sum()
