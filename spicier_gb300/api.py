@@ -263,7 +263,7 @@ class Context:
         last step, [count][nodes + V sources]), probe ([count][steps + 1] when cfg.probe >= 0), status."""
         nv = sum(1 for e in circuit.elements if e["kind"] == abi.SP_EL_V)
         nt = circuit.num_nodes + nv
-        steps = int(np.ceil(cfg.tstop / cfg.tstep))
+        steps = int(np.ceil(cfg.tstop / cfg.tstep)) if cfg.tstep > 0 and cfg.tstop > 0 else 0  # the library rejects bad steps
         out = dict(x=np.zeros((count, nt)), status=np.zeros(count, np.uint8),
                    probe=np.zeros((count, steps + 1)) if cfg.probe >= 0 else None)
         cols = 0

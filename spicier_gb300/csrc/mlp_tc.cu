@@ -80,6 +80,18 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
                  : "memory");
 }
 
+// Bulk copy global -> shared through the TMA unit (both addresses 16-byte
+// aligned, bytes a multiple of 16), completing on mbar's transaction count.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -189,7 +201,7 @@ __global__ void pack_kernel(const __nv_bfloat16* __restrict__ wt, int N, int K, 
 
 // Shared-memory carve-up (byte offsets from the 1024-aligned base).
 struct Carve {
-    uint32_t abuf, bias, lin, io, mbar, tslot, total;
+    uint32_t abuf, bias, lin, io, slots, mbar, tslot, total;
 };
 
 __host__ __device__ inline Carve carve(const Args& a, int teams) {
@@ -198,8 +210,9 @@ __host__ __device__ inline Carve carve(const Args& a, int teams) {
     c.bias = c.abuf + (uint32_t)teams * kAbytes;
     c.lin = c.bias + 4u * (uint32_t)a.bias_total;
     c.io = c.lin + 4u * (uint32_t)(a.n_out * a.n_in);
-    c.mbar = (c.io + 4u * (uint32_t)(2 * (a.n_in + a.n_out)) + 7u) & ~7u;
-    c.tslot = c.mbar + 8u * kMaxTeams;
+    c.slots = c.io + 4u * (uint32_t)(2 * (a.n_in + a.n_out));
+    c.mbar = (c.slots + 4u * (uint32_t)a.n_in + 7u) & ~7u;  // [kMaxTeams] teams, [kMaxTeams] weights
+    c.tslot = c.mbar + 8u * (kMaxTeams + 1);
     c.total = c.tslot + 16u;
     return c;
 }
@@ -224,21 +237,29 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + cv.mbar);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + cv.tslot);
 
+    int* slots_s = reinterpret_cast<int*>(sm + cv.slots);
+    const uint32_t wbar = smem_u32(&mbar[kMaxTeams]);
+
     // team = tile slot; warp q of a team reads TMEM lanes 32q..32q+31 (its sample rows)
     const int tid = threadIdx.x, nthreads = teams * kTeam, team = tid / kTeam, tt = tid % kTeam, warp = tid >> 5;
     const int quarter = tt >> 5, row = tt;
-    for (int i = tid; i < a.img_bytes / 16; i += nthreads)
-        reinterpret_cast<uint4*>(wimg)[i] = __ldg(reinterpret_cast<const uint4*>(a.img) + i);
+    if (tid == 0) {
+        for (int t = 0; t <= kMaxTeams; ++t)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[t])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // the weight image (a.img_bytes, a multiple of 1024) by the TMA unit, 32 KB per copy
+        mbar_expect_tx(wbar, (uint32_t)a.img_bytes);
+        for (int off = 0; off < a.img_bytes; off += 32768) {
+            const int len = a.img_bytes - off < 32768 ? a.img_bytes - off : 32768;
+            bulk_g2s(smem_u32(wimg + off), static_cast<const unsigned char*>(a.img) + off, (uint32_t)len, wbar);
+        }
+    }
     for (int i = tid; i < a.bias_total; i += nthreads) bias_s[i] = a.bias[i];
     for (int i = tid; i < a.n_out * a.n_in; i += nthreads) lin_s[i] = a.lin ? a.lin[i] : 0.f;
     // in_mean, 1 / in_scale, out_mean, out_scale
     for (int i = tid; i < 2 * (a.n_in + a.n_out); i += nthreads)
         io_s[i] = (i >= a.n_in && i < 2 * a.n_in) ? 1.0f / a.io[i] : a.io[i];
-    if (tid == 0) {
-        for (int t = 0; t < teams; ++t)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[t])) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
+    for (int i = tid; i < a.n_in; i += nthreads) slots_s[i] = a.slots[i];
     const uint32_t tcols = teams > 2 ? 512u : (teams > 1 ? 256u : 128u);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -246,7 +267,6 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    fence_async_smem();
     tc_before();
     __syncthreads();
     tc_after();
@@ -262,7 +282,7 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
 
     const int ntiles = (a.rows + kTile - 1) / kTile;
     uint32_t phase = 0;
-    bool ok = true;
+    bool ok = true, weights = false;
     int tile = blockIdx.x * teams + team;
     for (; tile < ntiles; tile += gridDim.x * teams) {
         const int s = tile * kTile + row;
@@ -272,7 +292,7 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
         float pc[kMaxIn];
 #pragma unroll
         for (int j = 0; j < kMaxIn; ++j)
-            pc[j] = (j < a.n_in && live) ? f64_to_f32(a.params_soa[(size_t)a.slots[j] * a.stride + s]) - in_mean[j]
+            pc[j] = (j < a.n_in && live) ? f64_to_f32(a.params_soa[(size_t)slots_s[j] * a.stride + s]) - in_mean[j]
                                          : 0.f;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -295,6 +315,11 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
             tc_before();
             team_sync(bar_id);
             tc_after();
+            if (!weights) {  // the TMA copy of the weights (issued at the start) has landed
+                ok = team_all(bar_id, mbar_wait(wbar, 0));
+                weights = true;
+                if (!ok) break;
+            }
             if (tt == 0) {
                 const uint32_t id = idesc_bf16(ly.N);
                 const uint32_t wb = wimg_s + (uint32_t)ly.img_off;

@@ -191,25 +191,39 @@ __device__ __forceinline__ bool spx_fin(double v) {  // not Inf / NaN, on the in
 }
 __device__ __forceinline__ bool spx_bad(float p, float iv) { return !(fabsf(p) > 0.f) || !(fabsf(iv) <= 3.0e38f); }
 __device__ __forceinline__ bool spx_bad(double p, double iv) { return !(fabs(p) > 0.0) || !(fabs(iv) <= 1.0e308); }
-// FP64 <-> FP32 conversions on the integer pipe (GB300's FP64 pipe issues
-// conversions at the FP64 rate); normal numbers only, the rest take cvt.
+// FP64 <-> FP32 conversions entirely on the integer pipe (GB300's FP64 pipe
+// issues conversions at the FP64 rate), round to nearest even, with zeros,
+// subnormals, overflow, Inf and NaN handled by integer code too: a fallback
+// to the hardware conversion would be if-converted into every call.
 __device__ __forceinline__ float spx_f(double x) {
     const u64 b = (u64)__double_as_longlong(x);
-    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
-    if (e <= 0 || e >= 255) return __double2float_rn(x);
-    const u64 m = b & ((1ULL << 52) - 1);
-    unsigned int f = ((unsigned int)(b >> 32) & 0x80000000u) | ((unsigned int)e << 23) | (unsigned int)(m >> 29);
-    const u64 rem = m & ((1ULL << 29) - 1), half = 1ULL << 28;
-    f += (rem > half || (rem == half && (f & 1))) ? 1u : 0u;
-    return __uint_as_float(f);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const int ex = (int)((b >> 52) & 0x7ff);
+    const u64 m = (b & ((1ULL << 52) - 1)) | (ex ? (1ULL << 52) : 0ULL);  // 53-bit significand
+    const int e = ex - 1023 + 127;                                         // biased float exponent
+    // normal results keep 24 bits (drop 29); subnormal ones drop 29 + 1 - e
+    int sh = e >= 1 ? 29 : 30 - e;
+    sh = sh > 63 ? 63 : sh;
+    const u64 q = m >> sh, rem = m & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+    unsigned int f = (unsigned int)q + (unsigned int)(rem > half || (rem == half && (q & 1)));
+    // f counts in units of the result's last place: for normal results add the
+    // exponent field minus the implicit bit (a carry rounds into the exponent)
+    f = e >= 1 ? f + ((unsigned int)(e - 1) << 23) : f;
+    f = (e >= 255 || f >= 0x7f800000u) ? 0x7f800000u : f;                   // overflow -> Inf
+    f = ex == 0x7ff ? (0x7f800000u | (unsigned int)(m >> 29) | ((b & ((1ULL << 52) - 1)) ? 0x400000u : 0u)) : f;
+    return __uint_as_float(sign | f);
 }
 __device__ __forceinline__ float spx_fneg(double x) { return __uint_as_float(__float_as_uint(spx_f(x)) ^ 0x80000000u); }
 __device__ __forceinline__ double spx_d(float x) {
     const unsigned int f = __float_as_uint(x);
-    const unsigned int e = (f >> 23) & 0xff;
-    if (e == 0 || e == 255) return (double)x;
-    return __longlong_as_double((long long)(((u64)(f & 0x80000000u) << 32) | ((u64)(e - 127 + 1023) << 52) |
-                                            ((u64)(f & 0x7fffffu) << 29)));
+    const u64 sign = (u64)(f & 0x80000000u) << 32;
+    const unsigned int e = (f >> 23) & 0xff, m = f & 0x7fffffu;
+    // subnormal floats: normalise the 23-bit significand (m != 0); zero stays zero
+    const int lz = __clz(m) - 8;  // m < 2^23: shift that brings its top bit to bit 23
+    const u64 sub = m ? ((u64)(1023 - 126 - lz) << 52) | ((u64)((m << lz) & 0x7fffffu) << 29) : 0ULL;
+    const u64 nrm = ((u64)(e - 127 + 1023) << 52) | ((u64)m << 29);
+    const u64 inf = (0x7ffULL << 52) | ((u64)m << 29);
+    return __longlong_as_double((long long)(sign | (e == 0 ? sub : (e == 255 ? inf : nrm))));
 }
 // v < 0 from the sign bit (integer pipe); -0 is not negative
 __device__ __forceinline__ bool spx_neg(double v) {
@@ -268,7 +282,7 @@ void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P
             case SP_EL_R:
                 o << "    double i = " << cst(e, 0) << " * (" << V(a) << " - " << V(b) << ");\n";
                 F(a, "i", false), F(b, "i", true);
-                break;  // linear J in J0
+                break;  // linear J: emit_linear_jacobian
             case SP_EL_V:
             case SP_EL_L: {
                 const int br = nn + el.branch;
@@ -302,25 +316,24 @@ void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P
                 const int d = a, g = b, s = c;
                 const bool pm = el.kind == SP_EL_PMOS;
                 if (mixed) {
-                    // level1.rs:154-248: the drain current in FP64 (it enters F), the
-                    // region from FP64 sign tests, gds and gm in FP32
-                    const std::string ng = pm ? "-" : "";
-                    // PMOS: vgs = vs - vg, vds = vs - vd (the reference negates vg - vs; only the
-                    // sign of a zero differs, and the region tests treat -0 as 0)
+                    // level1.rs:154-248 with the drain current in FP64 (it enters F) and
+                    // gds, gm in FP32 from the shadow of x.  The region comes from the
+                    // FP32 voltages: ids is continuous across both region boundaries
+                    // (a misread region changes it by O(delta^2)), and one formula
+                    // serves both conducting regions: ids = beta u (vov - u/2) q with
+                    // u = vds in the linear region and u = vov in saturation.
                     auto dif = [&](int p, int q) { return pm ? V(q) + " - " + V(p) : V(p) + " - " + V(q); };
-                    o << "    double vgs = " << dif(g, s) << ", vds = " << dif(d, s) << ";\n"
-                      << "    double vov = vgs - " << cst(e, 0) << ";\n"
-                      << "    bool on = !spx_neg(vov), lin = on && spx_neg(vds - vov);\n"
-                      << "    double ids = 0.0;\n"
-                      << "    if (on) { double q = 1.0 + " << cst(e, 2) << " * vds;\n"
-                      << "      ids = lin ? " << cst(e, 1) << " * (vov * vds - 0.5 * vds * vds) * q : 0.5 * "
-                      << cst(e, 1) << " * vov * vov * q; }\n";
+                    auto diff = [&](int p, int q) { return pm ? VF(q) + " - " + VF(p) : VF(p) + " - " + VF(q); };
+                    o << "    float vgsf = " << diff(g, s) << ", vdsf = " << diff(d, s) << ";\n"
+                      << "    float vovf = vgsf - " << cstf(e, 0) << ", qf = 1.f + " << cstf(e, 2) << " * vdsf;\n"
+                      << "    bool on = vovf >= 0.f, lin = on && vdsf < vovf;\n"
+                      << "    double vds = " << dif(d, s) << ", vov = (" << dif(g, s) << ") - " << cst(e, 0) << ";\n"
+                      << "    double u = lin ? vds : vov;\n"
+                      << "    double ids = on ? " << cst(e, 1) << " * u * fma(-0.5, u, vov) * fma(" << cst(e, 2)
+                      << ", vds, 1.0) : 0.0;\n";
                     if (pm) o << "    ids = -ids;\n";
                     F(d, "ids", false), F(s, "ids", true);
-                    o << "    float vgsf = " << ng << "(" << VF(g) << " - " << VF(s) << "), vdsf = " << ng << "("
-                      << VF(d) << " - " << VF(s) << ");\n"
-                      << "    float vovf = vgsf - " << cstf(e, 0) << ", qf = 1.f + " << cstf(e, 2) << " * vdsf;\n"
-                      << "    float gdf = 1e-12f, gmf = 0.f;\n"
+                    o << "    float gdf = 1e-12f, gmf = 0.f;\n"
                       << "    if (lin) { gdf = " << cstf(e, 1) << " * (vovf - vdsf) * qf + " << cstf(e, 1)
                       << " * (vovf * vdsf - 0.5f * vdsf * vdsf) * " << cstf(e, 2) << "; gmf = " << cstf(e, 1)
                       << " * vdsf * qf; }\n"
@@ -381,24 +394,25 @@ void emit_elements(std::ostringstream& o, const sp_topology* t, const Pattern& P
     }
 }
 
-// Linear (per-sample constant) Jacobian entries, J0.
-void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pattern& P, const std::vector<int>& doff,
-                          bool mixed) {
+// Linear (per-sample constant) Jacobian entries, stamped into J at the start
+// of every iteration: the +-1 entries of sources and inductors are literals
+// the compiler folds, and only the resistor conductances (g<e>, converted
+// once per sample) occupy registers.
+void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pattern& P) {
     const int nn = t->num_nodes;
-    o << "  #pragma unroll\n  for (int k = 0; k < " << P.nnz << "; ++k) J0[k] = (JT)0;\n";
+    o << "    #pragma unroll\n    for (int k = 0; k < " << P.nnz << "; ++k) J[k] = (JT)0;\n";
     for (int e = 0; e < t->num_elements; ++e) {
         const sp_element& el = t->h_elements[e];
         const int a = el.node[0], b = el.node[1];
         if (el.kind == SP_EL_R) {
-            o << "  { JT g = " << (mixed ? "spx_f(c" : "(JT)(c") << doff[e] << ");\n";
-            if (a >= 0) o << "    J0[" << P.at(a, a) << "] += g;\n";
-            if (b >= 0) o << "    J0[" << P.at(b, b) << "] += g;\n";
-            if (a >= 0 && b >= 0) o << "    J0[" << P.at(a, b) << "] -= g; J0[" << P.at(b, a) << "] -= g;\n";
-            o << "  }\n";
+            const std::string g = "g" + std::to_string(e);
+            if (a >= 0) o << "    J[" << P.at(a, a) << "] += " << g << ";\n";
+            if (b >= 0) o << "    J[" << P.at(b, b) << "] += " << g << ";\n";
+            if (a >= 0 && b >= 0) o << "    J[" << P.at(a, b) << "] -= " << g << "; J[" << P.at(b, a) << "] -= " << g << ";\n";
         } else if (el.kind == SP_EL_V || el.kind == SP_EL_L) {
             const int br = nn + el.branch;
-            if (a >= 0) o << "  J0[" << P.at(a, br) << "] += (JT)1; J0[" << P.at(br, a) << "] += (JT)1;\n";
-            if (b >= 0) o << "  J0[" << P.at(b, br) << "] -= (JT)1; J0[" << P.at(br, b) << "] -= (JT)1;\n";
+            if (a >= 0) o << "    J[" << P.at(a, br) << "] += (JT)1; J[" << P.at(br, a) << "] += (JT)1;\n";
+            if (b >= 0) o << "    J[" << P.at(b, br) << "] -= (JT)1; J[" << P.at(br, b) << "] -= (JT)1;\n";
         }
     }
 }
@@ -409,6 +423,17 @@ void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pat
 // early do not idle while others iterate: the warp executes about the mean
 // iteration count per sample, not the maximum over its 32 lanes.  Which
 // thread solves a sample does not change the sample's arithmetic.
+// Per-thread shared memory of the per-sample constants (0: they stay in
+// registers).  Shared memory frees ~3 registers per constant, so more warps
+// stay resident to hide the latency of the next sample's loads.
+size_t spec_smem_bytes(const sp_topology* t, bool fp32_jac) {
+    int nfc = 0;
+    if (fp32_jac)
+        for (const sp_element& el : t->h_elements) nfc += (el.kind == SP_EL_NMOS || el.kind == SP_EL_PMOS) ? 3 : 0;
+    const size_t bytes = ((size_t)t->num_derived * 8 + (size_t)nfc * 4) * 128;
+    return bytes <= 48 * 1024 ? bytes : 0;
+}
+
 std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     const int n = t->n, nn = t->num_nodes;
     std::vector<int> doff(t->num_elements);
@@ -416,26 +441,38 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
         doff[e] = o;
         o += derived_count(t->h_elements[e].kind);
     }
-    std::ostringstream o;
-    o << kPreamble << "typedef " << (fp32_jac ? "float" : "double") << " JT;\n";
-    o << "extern \"C\" __global__ void __launch_bounds__(128) spec_newton(SpecArgs a) {\n"
-      << "  const u64 nthreads = (u64)gridDim.x * blockDim.x;\n"
-      << "  u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
-      << "  if (s >= a.count) return;\n"
-      << "  const u64 st = a.stride;\n"
-      << "  const bool warm = a.x0 != 0;\n";
-    for (int k = 0; k < t->num_derived; ++k) o << "  double c" << k << ";\n";
+    const bool sm = spec_smem_bytes(t, fp32_jac) > 0;
     std::vector<int> fcs;
     if (fp32_jac)
         for (int e = 0; e < t->num_elements; ++e) {
             const int kind = t->h_elements[e].kind;
             if (kind != SP_EL_NMOS && kind != SP_EL_PMOS) continue;
-            for (int k = 0; k < 3; ++k) {
-                fcs.push_back(doff[e] + k);
-                o << "  float cf" << doff[e] + k << ";\n";
-            }
+            for (int k = 0; k < 3; ++k) fcs.push_back(doff[e] + k);
         }
-    o << "  JT J0[" << P.nnz << "];\n  double x[" << n << "];\n";
+    std::ostringstream o;
+    o << kPreamble << "typedef " << (fp32_jac ? "float" : "double") << " JT;\n";
+    if (sm) {  // constant k of this thread at [k][threadIdx.x]; volatile keeps them out of registers
+        for (int k = 0; k < t->num_derived; ++k) o << "#define c" << k << " (spx_cd[" << k << " * 128])\n";
+        for (size_t j = 0; j < fcs.size(); ++j) o << "#define cf" << fcs[j] << " (spx_cf[" << j << " * 128])\n";
+    }
+    o << "extern \"C\" __global__ void __launch_bounds__(128, " << (sm ? (fp32_jac ? 3 : 2) : 1) << ") spec_newton(SpecArgs a) {\n"
+      << "  const u64 nthreads = (u64)gridDim.x * blockDim.x;\n"
+      << "  u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
+      << "  if (s >= a.count) return;\n"
+      << "  const u64 st = a.stride;\n"
+      << "  const bool warm = a.x0 != 0;\n";
+    if (sm) {
+        o << "  extern __shared__ __align__(16) unsigned char spx_smem[];\n"
+          << "  volatile double* const spx_cd = reinterpret_cast<volatile double*>(spx_smem) + threadIdx.x;\n"
+          << "  volatile float* const spx_cf = reinterpret_cast<volatile float*>(spx_smem + " << t->num_derived * 8 * 128
+          << ") + threadIdx.x;\n";
+    } else {
+        for (int k = 0; k < t->num_derived; ++k) o << "  double c" << k << ";\n";
+        for (int k : fcs) o << "  float cf" << k << ";\n";
+    }
+    for (int e = 0; e < t->num_elements; ++e)
+        if (t->h_elements[e].kind == SP_EL_R) o << "  JT g" << e << ";\n";
+    o << "  double x[" << n << "];\n";
     if (fp32_jac)
         o << "  float xf[" << n << "];\n"
           << "  const float reltolf = spx_f(a.reltol), vabstolf = spx_f(a.vabstol), iabstolf = spx_f(a.iabstol);\n";
@@ -445,7 +482,9 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     ld << "  {\n  const double* dv = a.dv + s;\n";
     for (int k = 0; k < t->num_derived; ++k) ld << "  c" << k << " = __ldg(dv + " << k << " * st);\n";
     for (int k : fcs) ld << "  cf" << k << " = spx_f(c" << k << ");\n";
-    emit_linear_jacobian(ld, t, P, doff, fp32_jac);
+    for (int e = 0; e < t->num_elements; ++e)
+        if (t->h_elements[e].kind == SP_EL_R)
+            ld << "  g" << e << " = " << (fp32_jac ? "spx_f(c" : "(JT)(c") << doff[e] << ");\n";
     ld << "  if (warm) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n
        << " + i];\n"
        << "  } else if (a.nodeset) {\n    #pragma unroll\n    for (int i = 0; i < " << n
@@ -456,7 +495,8 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     o << ld.str();
     o << "  while (true) {\n    ++it;\n"
       << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n"
-      << "    JT J[" << P.nnz << "];\n    #pragma unroll\n    for (int k = 0; k < " << P.nnz << "; ++k) J[k] = J0[k];\n";
+      << "    JT J[" << P.nnz << "];\n";
+    emit_linear_jacobian(o, t, P);
     emit_elements(o, t, P, doff, true, fp32_jac);
     // factorisation over the static pattern
     o << "    bool sing = false;\n";
@@ -609,7 +649,8 @@ int spec_prepare(sp_topology* t, int prec, std::string& err) {
         return SP_ERR_BACKEND;
     }
     int bpsm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, (const void*)k, 128, 0) != cudaSuccess || bpsm < 1)
+    const size_t smem = spec_smem_bytes(t, prec == SP_PREC_MIXED);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, (const void*)k, 128, smem) != cudaSuccess || bpsm < 1)
         bpsm = 1;
     entry.blocks_per_sm = t->spec_bpsm[slot] = bpsm;
     entry.lib = lib;
@@ -642,7 +683,8 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     void* args[] = {&a};
     const uint64_t resident = (uint64_t)t->ctx->num_sms * (uint64_t)t->spec_bpsm[slot];
     const unsigned grid = (unsigned)std::min<uint64_t>((L.count + 127) / 128, resident);
-    return cudaLaunchKernel((const void*)t->spec_kernel[slot], dim3(grid), dim3(128), args, 0, st);
+    return cudaLaunchKernel((const void*)t->spec_kernel[slot], dim3(grid), dim3(128), args,
+                            spec_smem_bytes(t, prec == SP_PREC_MIXED), st);
 }
 
 void spec_release_all(sp_ctx* ctx) {
