@@ -99,6 +99,10 @@ def _bind(L):
         "or_cr_log_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
         "or_cr_cos_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
         "or_cr_exp_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
+        "or_cr_log_full_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
+        "or_cr_cos_full_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
+        "or_cr_fast_misses": (u64, [i32, P(d), u64]),
+        "or_ieee_int_mismatches": (u64, [u64, u64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -64,6 +64,45 @@ void or_cr_cos_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
 void or_cr_exp_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
     for (uint64_t i = 0; i < n; ++i) y[i] = sp::cr_exp(x[i], hard);
 }
+// the 128-bit evaluations alone (no 64-bit fast path), to check the fast paths against
+void or_cr_log_full_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
+    for (uint64_t i = 0; i < n; ++i) y[i] = sp::cr_log_impl(x[i], hard, false);
+}
+void or_cr_cos_full_batch(const double* x, uint64_t n, double* y, unsigned* hard) {
+    for (uint64_t i = 0; i < n; ++i) y[i] = sp::cr_cos_impl(x[i], hard, false);
+}
+// the integer multiply / divide / square root of cr_math.cuh against the
+// host's IEEE operators on n random normal operands (mismatches returned)
+uint64_t or_ieee_int_mismatches(uint64_t seed, uint64_t n) {
+    uint64_t st = seed, bad = 0;
+    auto next = [&]() { st = oracle::splitmix64(st); return st; };
+    auto rnd = [&](int elo, int ehi) {
+        const uint64_t m = next() & ((1ULL << 52) - 1);
+        const int e = elo + (int)(next() % (uint64_t)(ehi - elo + 1));
+        return sp::cr::bdouble(((uint64_t)(e + 1023) << 52) | m);
+    };
+    for (uint64_t i = 0; i < n; ++i) {
+        const double a = rnd(-400, 400), b = rnd(-400, 400), sa = (next() & 1) ? -a : a;
+        bad += sp::cr::dbits(sp::cr::mul_rn(sa, b)) != sp::cr::dbits(sa * b);
+        bad += sp::cr::dbits(sp::cr::div_pos(a, b)) != sp::cr::dbits(a / b);
+        bad += sp::cr::dbits(sp::cr::sqrt_pos(a)) != sp::cr::dbits(std::sqrt(a));
+    }
+    return bad;
+}
+
+// how often the ln fast path hands over to the 128-bit evaluation
+uint64_t or_cr_fast_misses(int fn, const double* x, uint64_t n) {
+    uint64_t miss = 0;
+    for (uint64_t i = 0; i < n && fn == 0; ++i) {
+        double r;
+        const uint64_t b = sp::cr::dbits(x[i]);
+        const int bexp = (int)(b >> 52);
+        if (bexp < 1023 - 360 || bexp > 1023 + 359) continue;
+        if (b > 0x3FEFFFE000000000ULL && b < 0x3FF0001000000000ULL) continue;
+        miss += sp::cr::ln_fast(bexp - 1023, b & ((1ULL << 52) - 1), &r) ? 0 : 1;
+    }
+    return miss;
+}
 
 // kind: 0 uniform, 1 gaussian, 2 uniform_f32, 3 gaussian_f32 (sp_rng_fill_device).
 void or_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t param, uint64_t count,

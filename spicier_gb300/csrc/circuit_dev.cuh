@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include "../../include/spicier_gb300.h"
+#include "cr_math.cuh"
 
 namespace sp {
 
@@ -99,7 +100,7 @@ template <class PF, class OF>
 __host__ __device__ inline void derive_element(const sp_element& el, PF P, OF out) {
     const double vt = thermal_voltage_300();
     switch (el.kind) {
-        case SP_EL_R: out(0, 1.0 / P(el.field[0])); break;  // passive.rs:48-50
+        case SP_EL_R: out(0, ieee_div(1.0, P(el.field[0]))); break;  // passive.rs:48-50
         case SP_EL_D: {
             double nvt = P(el.field[1]) * vt;
             out(0, P(el.field[0]));
@@ -112,7 +113,7 @@ __host__ __device__ inline void derive_element(const sp_element& el, PF P, OF ou
             // vth = |VTO| (level1.rs:164); beta = kp * nf * w / l (level1.rs:68-70)
             double kp = P(el.field[1]), w = P(el.field[3]), l = P(el.field[4]), nf = P(el.field[5]);
             out(0, fabs(P(el.field[0])));
-            out(1, kp * nf * w / l);
+            out(1, ieee_div(ieee_mul(ieee_mul(kp, nf), w), l));  // ((kp nf) w) / l
             out(2, P(el.field[2]));
             break;
         }

@@ -33,6 +33,7 @@
 //         low partial product (error bound 512 units of 2^-125).
 #pragma once
 #include <math.h>
+#include <cmath>
 #include <stdint.h>
 #include <string.h>
 
@@ -225,6 +226,136 @@ SP_HD double ln_near1(uint64_t xb, unsigned* hard) {
     return below ? -r : r;
 }
 
+// IEEE-exact (round to nearest even) multiply, divide and square root of
+// finite positive-normal doubles whose results are normal, by integer
+// operations: GB300's FP64 pipe issues at a small fraction of the integer
+// rate, and the results are the IEEE ones bit for bit (a correctly rounded
+// result is unique).  Callers check the domain.
+
+// a b for normal a, b (either sign) with a normal product.
+SP_HD double mul_rn(double a, double b) {
+    const uint64_t ba = dbits(a), bb = dbits(b);
+    const uint64_t ma = (ba & ((1ULL << 52) - 1)) | (1ULL << 52), mb = (bb & ((1ULL << 52) - 1)) | (1ULL << 52);
+    const int ea = (int)((ba >> 52) & 0x7ff), eb = (int)((bb >> 52) & 0x7ff);
+    const u128 p = (u128)ma * mb;  // [2^104, 2^106)
+    const int top = (int)(p >> 105);  // 1 when the product has 106 bits
+    const int sh = 52 + top;
+    uint64_t q = (uint64_t)(p >> sh);
+    const uint64_t rem = (uint64_t)p & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+    q += (rem > half || (rem == half && (q & 1))) ? 1 : 0;  // q = 2^53 carries into the exponent below
+    const uint64_t e = (uint64_t)(ea + eb - 1023 + top);
+    return bdouble(((ba ^ bb) & (1ULL << 63)) | ((e << 52) + (q - (1ULL << 52))));
+}
+
+// a / b for positive normal a, b with a normal quotient.
+SP_HD double div_pos(double a, double b) {
+    const uint64_t ba = dbits(a), bb = dbits(b);
+    const uint64_t ma = (ba & ((1ULL << 52) - 1)) | (1ULL << 52), mb = (bb & ((1ULL << 52) - 1)) | (1ULL << 52);
+    int e = (int)(ba >> 52) - (int)(bb >> 52) + 1023;
+    // quotient mantissa: floor(ma 2^s / mb) with 53 significant bits, s = 52 or 53
+    const int s = ma >= mb ? 52 : 53;
+    e -= s - 52;
+    const u128 num = (u128)ma << s;
+    // R ~ 2^115 / mb in (2^62, 2^63]: an FP32 reciprocal, then two Newton steps
+#if defined(__CUDA_ARCH__)
+    const float rf = __frcp_rn((float)(uint32_t)(mb >> 29));  // mb 2^-29 in [2^23, 2^24)
+#else
+    const float rf = 1.0f / (float)(uint32_t)(mb >> 29);
+#endif
+    uint64_t R = (uint64_t)(uint32_t)(rf * 0x1p54f) << 32;  // rf 2^86
+    for (int it = 0; it < 2; ++it) {
+        const u128 mr = (u128)mb * R;                                    // ~2^115
+        const uint64_t corr = (uint64_t)((((u128)1 << 116) - mr) >> 52);  // (2 - mb R 2^-115) 2^63
+        R = (uint64_t)(((u128)R * corr) >> 63);
+    }
+    uint64_t q = (uint64_t)(((num >> 52) * (u128)R) >> 63);  // ~ num / mb
+    // exact correction: rem = num - q mb in [0, mb)
+    for (int it = 0; it < 3 && (u128)q * mb > num; ++it) --q;
+    for (int it = 0; it < 3 && (u128)(q + 1) * mb <= num; ++it) ++q;
+    const uint64_t rem = (uint64_t)(num - (u128)q * mb);
+    q += (2 * (u128)rem > mb || (2 * (u128)rem == mb && (q & 1))) ? 1 : 0;
+    return bdouble(((uint64_t)e << 52) + (q - (1ULL << 52)));
+}
+
+// sqrt(x) for positive normal x.
+SP_HD double sqrt_pos(double x) {
+    const uint64_t b = dbits(x);
+    int E = (int)(b >> 52) - 1023;
+    uint64_t M = (b & ((1ULL << 52) - 1)) | (1ULL << 52);
+    if (E & 1) {
+        M <<= 1;
+        E -= 1;
+    }
+    // r = floor(sqrt(M 2^52)), M 2^52 in [2^104, 2^106): r in [2^52, 2^53)
+    const uint64_t U = M << 10;  // u = M 2^-52 in [1, 4), as u 2^62
+    const float uf = (float)(uint32_t)(M >> 30) * 0x1p-22f;
+#if defined(__CUDA_ARCH__)
+    const float gf = rsqrtf(uf);
+#else
+    const float gf = 1.0f / std::sqrt(uf);
+#endif
+    uint64_t G = (uint64_t)(uint32_t)(gf * 0x1p31f) << 32;  // g = 1/sqrt(u), as g 2^63
+    for (int it = 0; it < 2; ++it) {
+        const uint64_t A = (uint64_t)(((u128)G * G) >> 64);          // g^2 2^62
+        const uint64_t B = (uint64_t)(((u128)U * A) >> 64);          // u g^2 2^60
+        const uint64_t T = (3ULL << 60) - B;                          // (3 - u g^2) 2^60
+        G = (uint64_t)(((u128)G * T) >> 64) << 3;                     // g (3 - u g^2)/2 2^63
+    }
+    uint64_t r = (uint64_t)(((u128)U * G) >> 64) >> 9;  // sqrt(u) 2^52
+    const u128 N = (u128)M << 52;
+    for (int it = 0; it < 3 && (u128)r * r > N; ++it) --r;
+    for (int it = 0; it < 3 && (u128)(r + 1) * (r + 1) <= N; ++it) ++r;
+    r += (N - (u128)r * r > r) ? 1 : 0;  // round to nearest (no ties: N is an integer)
+    return bdouble(((uint64_t)(E / 2 + 1023) << 52) + (r - (1ULL << 52)));
+}
+
+}  // namespace cr
+
+// IEEE multiply / divide / square root that run on the integer pipe on the
+// device for operands and results in the normal range, and in hardware
+// otherwise (a call the compiler does not speculate); plain operators on the
+// host.  Bit-identical to the operators everywhere.
+#if defined(__CUDA_ARCH__)
+__device__ __noinline__ static double hw_mul(double a, double b) { return a * b; }
+__device__ __noinline__ static double hw_div(double a, double b) { return a / b; }
+__device__ __noinline__ static double hw_sqrt(double a) { return sqrt(a); }
+#endif
+
+SP_HD double ieee_mul(double a, double b) {
+#if defined(__CUDA_ARCH__)
+    const int ea = (int)((cr::dbits(a) >> 52) & 0x7ff), eb = (int)((cr::dbits(b) >> 52) & 0x7ff);
+    const int e = ea + eb - 1023;
+    if (ea != 0 && eb != 0 && ea != 0x7ff && eb != 0x7ff && e >= 2 && e <= 2045) return cr::mul_rn(a, b);
+    return hw_mul(a, b);
+#else
+    return a * b;
+#endif
+}
+
+SP_HD double ieee_div(double a, double b) {
+#if defined(__CUDA_ARCH__)
+    const uint64_t ba = cr::dbits(a), bb = cr::dbits(b);
+    const int ea = (int)(ba >> 52), eb = (int)(bb >> 52);  // sign bit included: negative operands fail below
+    const int e = ea - eb + 1023;
+    if (ea > 0 && ea < 0x7ff && eb > 0 && eb < 0x7ff && e >= 2 && e <= 2045) return cr::div_pos(a, b);
+    return hw_div(a, b);
+#else
+    return a / b;
+#endif
+}
+
+SP_HD double ieee_sqrt(double a) {
+#if defined(__CUDA_ARCH__)
+    const int ea = (int)(cr::dbits(a) >> 52);  // sign bit included
+    if (ea > 0 && ea < 0x7ff) return cr::sqrt_pos(a);
+    return hw_sqrt(a);
+#else
+    return sqrt(a);
+#endif
+}
+
+namespace cr {
+
 // D 2^-53 as a double for an integer D < 2^53 (exact), by integer operations.
 SP_HD double u53_to_double(uint64_t m) {
     if (m == 0) return 0.0;
@@ -239,8 +370,83 @@ SP_HD double out_of_domain(unsigned* hard) {
 
 }  // namespace cr
 
-// Correctly rounded natural logarithm (see the header comment for the domain).
-SP_HD double cr_log(double x, unsigned* hard) {
+namespace cr {
+
+SP_HD uint64_t mulhi64(uint64_t a, uint64_t b) { return (uint64_t)(((u128)a * b) >> 64); }
+
+// Fast path of ln for x = m 2^e outside (1 - 2^-16, 1 + 2^-16): the same
+// reduction as the full path, ln(1 + r) = r - r^2 P(r) with P in 64-bit
+// Horner (r^2 P < 2^-15.6, so its 64-bit relative accuracy is about 2^-77
+// absolute), summed with the 128-bit table value and e ln 2.  Returns false
+// when the error bound (2^44 units of 2^-120) does not decide the rounding.
+SP_HD bool ln_fast(int e, uint64_t frac, double* out) {
+    const LnRow row = ln_row((int)(frac >> 44));
+    const uint64_t r0 = ((1ULL << 52) | frac) * row.c;  // r 2^68, exact
+    const uint64_t r64 = r0 >> 4;                       // r 2^64
+    const uint64_t cf[8] = SP_CR_LN_FAST;               // 1/2 .. 1/9
+    uint64_t h = cf[7];
+#pragma unroll
+    for (int j = 6; j >= 0; --j) h = cf[j] - mulhi64(r64, h);  // P(r) 2^64
+    const uint64_t R2 = (uint64_t)(((u128)r0 * r0) >> 58);     // r^2 2^78
+    const uint64_t q = mulhi64(R2, h);                           // r^2 P 2^78
+    const u128 lnm = mk(row.th, row.tl) + ((u128)r0 << 52) - ((u128)q << 42);
+    const W2 ln2w = {SP_CR_LN2};
+    const uint64_t ae = (uint64_t)(e < 0 ? -e : e);
+    const u128 eln2 = mk(ln2w) * ae;
+    const uint64_t err = (1ULL << 44) + 8 + ae;
+    unsigned undecided = 0;
+    const double r = e >= 0 ? round_fixed(eln2 + lnm, 120, err, &undecided)
+                            : -round_fixed(eln2 - lnm, 120, err, &undecided);
+    *out = r;
+    return undecided == 0;
+}
+
+// Fast path of cos: the full path's reduction a = |t - k pi/2| = j/512 + d,
+// then 1 - cos d = w Pc(w) and sin d = d - d w Ps(w) in 64-bit Horner, the
+// products with the table's cos/sin(j/512) in 64 bits except y d, formed
+// from the 128-bit table value and d to a few units of 2^-125.  Error bound
+// 2^47 units of 2^-125; returns false when that does not decide the rounding.
+SP_HD bool cos_fast(u128 a, int k, bool neg, double* out) {
+    const int j = (int)(a >> 116);  // floor(512 a)
+    if (j > 403) return false;
+    const u128 d = a - ((u128)j << 116);                   // d 2^125, d < 2^-9
+    const uint64_t dh = (uint64_t)(d >> 52);               // d 2^73 (truncated)
+    const uint64_t dl = (uint64_t)d & ((1ULL << 52) - 1);  // the rest, units of 2^-125
+    const uint64_t W = mulhi64(dh, dh);                    // w = d^2, 2^82
+    const uint64_t w64 = W >> 18;                          // w 2^64
+    const uint64_t cc[4] = SP_CR_COS_FAST, sc[4] = SP_CR_SIN_FAST;
+    uint64_t pc = cc[2] - mulhi64(w64, cc[3]);
+    pc = cc[1] - mulhi64(w64, pc);
+    pc = cc[0] - mulhi64(w64, pc);  // Pc 2^64
+    uint64_t ps = sc[2] - mulhi64(w64, sc[3]);
+    ps = sc[1] - mulhi64(w64, ps);
+    ps = sc[0] - mulhi64(w64, ps);  // Ps 2^64
+    const uint64_t CM = mulhi64(W, pc);               // 1 - cos d, 2^82
+    const uint64_t SDC = mulhi64(mulhi64(dh, W), ps);  // d w Ps, 2^91
+    const CosRow row = cos_row(j);
+    const int q = k & 3;
+    const bool odd = (q & 1) != 0;
+    // cos a = C - C (1 - cos d) - S sin d;  sin a = S - S (1 - cos d) + C sin d
+    const u128 X = odd ? mk(row.sh, row.sl) : mk(row.ch, row.cl);  // 2^125
+    const u128 Y = odd ? mk(row.ch, row.cl) : mk(row.sh, row.sl);
+    const uint64_t X63 = (uint64_t)(X >> 62), Y63 = (uint64_t)(Y >> 62);  // 2^63
+    const u128 yd = (((u128)hi64(Y) * dh + hi64((u128)lo64(Y) * dh)) >> 9) + (((u128)Y63 * dl) >> 63);  // y d
+    const u128 xcm = (u128)mulhi64(X63, CM) << 44;    // x (1 - cos d)
+    const u128 ysdc = (u128)mulhi64(Y63, SDC) << 35;  // y d w Ps
+    const u128 v = odd ? (X + yd) - (xcm + ysdc) : (X + ysdc) - (xcm + yd);
+    unsigned undecided = 0;
+    const double r = round_fixed(v, 125, 1ULL << 47, &undecided);
+    const bool negative = (q == 2) || (q == 1 && !neg) || (q == 3 && neg);
+    *out = negative ? -r : r;
+    return undecided == 0;
+}
+
+}  // namespace cr
+
+// Correctly rounded natural logarithm (see the header comment for the domain):
+// the 64-bit fast path (fast = true), and the 128-bit evaluation wherever it
+// cannot decide the rounding (or always, fast = false).
+SP_HD double cr_log_impl(double x, unsigned* hard, bool fast) {
     using namespace cr;
     const uint64_t b = dbits(x);
     const int bexp = (int)(b >> 52);  // sign bit included: negative x lands above 2047
@@ -248,6 +454,10 @@ SP_HD double cr_log(double x, unsigned* hard) {
     // x in (1 - 2^-16, 1 + 2^-16): positive doubles order like their bit patterns
     if (b > 0x3FEFFFE000000000ULL && b < 0x3FF0001000000000ULL) return b == 0x3FF0000000000000ULL ? 0.0 : ln_near1(b, hard);
     const int e = bexp - 1023;
+    if (fast) {
+        double r;
+        if (ln_fast(e, b & ((1ULL << 52) - 1), &r)) return r;
+    }
     const uint64_t frac = b & ((1ULL << 52) - 1);
     const LnRow row = ln_row((int)(frac >> 44));
     const uint64_t r0 = ((1ULL << 52) | frac) * row.c;  // m c_i 2^68 - 2^68, exact (< 2^61)
@@ -270,6 +480,8 @@ SP_HD double cr_log(double x, unsigned* hard) {
     if (e >= 0) return round_fixed(eln2 + lnm, 120, err, hard);
     return -round_fixed(eln2 - lnm, 120, err, hard);
 }
+
+SP_HD double cr_log(double x, unsigned* hard) { return cr_log_impl(x, hard, true); }
 
 // Correctly rounded exponential (subnormal results and overflow to +Inf
 // included); |x| < 2^-54 returns 1, x < -746 returns 0, x > 710 +Inf, NaN
@@ -315,8 +527,9 @@ SP_HD double pm_log1p(double a, unsigned* hard) {
     return cr_log(u, hard) * (a / (u - 1.0));
 }
 
-// Correctly rounded cosine (see the header comment for the domain).
-SP_HD double cr_cos(double t, unsigned* hard) {
+// Correctly rounded cosine (see the header comment for the domain): the
+// 64-bit fast path (fast = true), else the 128-bit evaluation.
+SP_HD double cr_cos_impl(double t, unsigned* hard, bool fast) {
     using namespace cr;
     const uint64_t b = dbits(t) & ~(1ULL << 63);  // cos is even
     const int bexp = (int)(b >> 52);
@@ -333,6 +546,10 @@ SP_HD double cr_cos(double t, unsigned* hard) {
     const u128 kp = pio2 * (uint64_t)k;
     const bool neg = T < kp;
     const u128 a = neg ? kp - T : T - kp;
+    if (fast) {
+        double r;
+        if (cos_fast(a, k, neg, &r)) return r;
+    }
     int j = (int)(a >> 116);  // floor(512 a)
     uint64_t err = 512;
     if (j > 403) {  // cannot happen for |t - k pi/2| <= pi/4 + 2^-40
@@ -369,5 +586,7 @@ SP_HD double cr_cos(double t, unsigned* hard) {
     const double r = round_fixed(v, 125, err, hard);
     return negative ? -r : r;
 }
+
+SP_HD double cr_cos(double t, unsigned* hard) { return cr_cos_impl(t, hard, true); }
 
 }  // namespace sp

@@ -13,6 +13,8 @@ exp (format Q2.126): exp(j/256) for j = -90..90, ln 2 (Q12.116) and 1/k!.
 cos (format Q3.125):
   cos(j/512) and sin(j/512) for j = 0..403, pi/2, and the Taylor
   coefficients 1/k! of the cos (k = 2..10) and sin (k = 3..11) series.
+fast paths (Q0.64): 1/j (j = 2..9) for ln; 1/k! (k = 2, 4, 6, 8) and
+  (k = 3, 5, 7, 9) for cos and sin.
 """
 import os
 
@@ -85,6 +87,14 @@ def main():
     w("    { " + ", ".join(f"{{{words(fixed(1 / mp.factorial(k), F_COS))}}}" for k in (3, 5, 7)) + " }")
     w("#define SP_CR_COS_TAIL { " + ", ".join(f"0x{fixed(1 / mp.factorial(k), 64, 64):016x}ULL" for k in (8, 10)) + " }")
     w("#define SP_CR_SIN_TAIL { " + ", ".join(f"0x{fixed(1 / mp.factorial(k), 64, 64):016x}ULL" for k in (9, 11)) + " }")
+    # ------------------------------------------------- fast paths (Q0.64)
+    w("")
+    w("// fast paths (64-bit Horner, Q0.64): ln(1+r) = r - r^2 P(r), P = 1/2 - r/3 + ... - r^7/9;")
+    w("// 1 - cos d = w Pc(w), Pc = 1/2! - w/4! + w^2/6! - w^3/8!; sin d = d - d w Ps(w),")
+    w("// Ps = 1/3! - w/5! + w^2/7! - w^3/9!  (w = d^2)")
+    w("#define SP_CR_LN_FAST { " + ", ".join(f"0x{fixed(mp.mpf(1) / j, 64, 64):016x}ULL" for j in range(2, 10)) + " }")
+    w("#define SP_CR_COS_FAST { " + ", ".join(f"0x{fixed(1 / mp.factorial(k), 64, 64):016x}ULL" for k in (2, 4, 6, 8)) + " }")
+    w("#define SP_CR_SIN_FAST { " + ", ".join(f"0x{fixed(1 / mp.factorial(k), 64, 64):016x}ULL" for k in (3, 5, 7, 9)) + " }")
     # ---------------------------------------------------------------- exp
     w("")
     w("// exp: rows {exp(j/256) hi, lo} for j = -90..90 (Q2.126), ln 2 in Q12.116,")

@@ -118,3 +118,41 @@ def test_gaussian_host_libm_agreement(rng_gold):
     assert np.mean(got == want) > 0.98
     scale = np.spacing(np.maximum(np.abs(want), 1.0))
     assert np.all(np.abs(got - want) <= 8 * scale)
+
+
+def _batch(fn, x):
+    import ctypes as C
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    hard = C.c_uint(0)
+    getattr(oracle.lib(), f"or_cr_{fn}_batch")(oracle._dp(x), x.size, oracle._dp(y), C.byref(hard))
+    return y, hard.value
+
+
+def test_fast_paths_equal_full_evaluation():
+    """The 64-bit fast paths of ln and cos return the 128-bit evaluation's bits wherever they decide."""
+    rng = np.random.default_rng(11)
+    n = 1 << 19
+    u = (rng.integers(1, 1 << 53, n, dtype=np.uint64) >> np.uint64(0)).astype(np.float64) * 2.0 ** -53
+    x_cases = [np.maximum(u, 1e-10), np.exp(rng.uniform(-240, 240, n)),
+               1.0 + rng.uniform(-2.0 ** -7, 2.0 ** -7, n // 4)]
+    for x in x_cases:
+        f, hf = _batch("log", x)
+        g, hg = _batch("log_full", x)
+        assert hf == hg == 0
+        assert np.array_equal(f.view(np.uint64), g.view(np.uint64))
+    miss = oracle.lib().or_cr_fast_misses(0, oracle._dp(x_cases[0]), x_cases[0].size)
+    assert miss < n * 1e-4  # the fast path decides nearly every Box-Muller ln
+    base = np.pi / 2 * np.arange(1, 5)
+    near = np.concatenate([b * (1 + rng.uniform(-1e-9, 1e-9, 4000)) for b in base]
+                          + [np.nextafter(base, base + 1), np.nextafter(base, base - 1)])
+    for t in (6.283185307179586 * u, rng.uniform(-7.99, 7.99, n), near):
+        f, hf = _batch("cos", t)
+        g, hg = _batch("cos_full", t)
+        assert hf == hg
+        assert np.array_equal(f.view(np.uint64), g.view(np.uint64))
+
+
+def test_integer_ieee_operations():
+    """cr::mul_rn, div_pos and sqrt_pos (the device's integer-pipe IEEE operations) equal the host operators."""
+    assert oracle.lib().or_ieee_int_mismatches(3, 1 << 20) == 0
