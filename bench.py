@@ -221,6 +221,8 @@ def main():
     ap.add_argument("--no-grid", action="store_true", help="skip the power-grid (workload 5) report")
     ap.add_argument("--train-samples", type=int, default=1 << 20)
     ap.add_argument("--no-ablations", action="store_true", help="skip the mixed-from-nodeset and FP64-specialised arms")
+    ap.add_argument("--mlp-hidden", type=int, default=128, help="hidden width of the warm-start network")
+    ap.add_argument("--mlp-layers", type=int, default=3, help="hidden layers of the warm-start network")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -264,7 +266,8 @@ def main():
     t0 = time.perf_counter()
     ctx.specialize(topo, abi.SP_PREC_MIXED, True)
     spec_s = time.perf_counter() - t0
-    ws = WarmStart(ctx, circ, n_inputs=len(random_slots(circ)), seed=3)
+    ws = WarmStart(ctx, circ, n_inputs=len(random_slots(circ)), n_hidden=args.mlp_hidden, n_layers=args.mlp_layers,
+                   seed=3)
     rep = ws.train(topo, seed=TRAIN_SEED, samples=args.train_samples, epochs=16, batch=4096, lr=2e-3)
 
     cfg_plain = abi.newton_config(precision=abi.SP_PREC_FP64)

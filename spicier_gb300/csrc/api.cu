@@ -552,8 +552,8 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     NewtonScratch s;
     int rc = newton_scratch(ctx, t, count, s, warm != nullptr);
     if (rc) return rc;
-    // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64)
-    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 16, st), "clear counters");
+    // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64), [4] moments ticket
+    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 20, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
                  s.counters + 1};
     {
@@ -620,7 +620,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (d_moments) {
         ProfScope prof(ctx, "moments", st);
         e = launch_moments(d_x, count, (uint32_t)t->n, (uint32_t)t->n, d_status, s.partial, s.moment_blocks,
-                           d_moments, st);
+                           d_moments, s.counters + 4, st);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "moments launch");
     }
     return SP_OK;
@@ -770,10 +770,13 @@ int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaSetDevice(ctx->device);
     uint32_t mb = (uint32_t)std::max<uint64_t>(256, (rows + 511) / 512);  // partials per column
-    int rc = ensure_scratch(ctx, align256(sizeof(sp_moments) * mb * (size_t)cols));
+    const size_t bpart = align256(sizeof(sp_moments) * mb * (size_t)cols);
+    int rc = ensure_scratch(ctx, bpart + 256);
     if (rc) return rc;
     ScratchOrder order(ctx, (cudaStream_t)stream);
-    SP_CUDA(ctx, launch_moments(d_values, rows, ld, cols, d_status, (sp_moments*)ctx->scratch, mb, d_out,
+    unsigned int* ticket = (unsigned int*)((char*)ctx->scratch + bpart);
+    SP_CUDA(ctx, cudaMemsetAsync(ticket, 0, 4, (cudaStream_t)stream), "clear ticket");
+    SP_CUDA(ctx, launch_moments(d_values, rows, ld, cols, d_status, (sp_moments*)ctx->scratch, mb, d_out, ticket,
                                 (cudaStream_t)stream),
             "moments launch");
     return SP_OK;

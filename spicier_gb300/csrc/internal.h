@@ -68,8 +68,8 @@ cudaError_t launch_newton_fast(int prec, const NewtonLaunch& L, bool fallback, i
 cudaError_t launch_lu_batch_mixed(const double* mats, const double* rhs, int n, uint64_t batch,
                                   double* sol, uint8_t* sing, int refine_steps, cudaStream_t st);
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
-                           const uint8_t* status, sp_moments* partial, uint32_t nblocks,
-                           sp_moments* out, cudaStream_t st);
+                           const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
+                           unsigned int* ticket, cudaStream_t st);  // ticket: a zeroed counter
 cudaError_t prepare_fast_kernels(int max_smem);
 
 // Largest dense size of the thread-per-sample Newton kernels.

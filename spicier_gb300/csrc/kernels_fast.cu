@@ -250,7 +250,8 @@ __device__ __forceinline__ double from_key(long long k) {
 __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
                                                            uint32_t cols, uint32_t cp, uint64_t chunk,
                                                            const uint8_t* __restrict__ status,
-                                                           sp_moments* __restrict__ partial) {
+                                                           sp_moments* __restrict__ partial, unsigned int* ticket,
+                                                           sp_moments* __restrict__ out) {
     __shared__ sp_moments sh[256];
     const uint32_t c = threadIdx.x % cp, g = threadIdx.x / cp, groups = 256 / cp;
     const uint64_t lo = (uint64_t)blockIdx.x * chunk, hi = min(rows, lo + chunk);
@@ -290,6 +291,27 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
         __syncthreads();
     }
     if (threadIdx.x < cols) partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
+    // the last block to finish merges the partials: thread t works on column
+    // t % cp, merging partials t / cp, t / cp + groups, ... in order, then a
+    // pairwise tree over the groups (a fixed order for given rows and cols)
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    sp_moments f{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+    if (c < cols)
+        for (uint32_t b = g; b < gridDim.x; b += groups) mom_merge(f, partial[(size_t)c * gridDim.x + b]);
+    sh[threadIdx.x] = f;
+    __syncthreads();
+    for (uint32_t w = groups / 2; w >= 1; w >>= 1) {
+        if (g < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w * cp]);
+        __syncthreads();
+    }
+    if (threadIdx.x < cols) out[threadIdx.x] = sh[threadIdx.x];
+    if (threadIdx.x == 0) *ticket = 0;  // ready for the next launch on this buffer
 }
 
 // One block per column: each thread merges partials t, t + 256, ... in order,
@@ -311,7 +333,7 @@ __global__ void __launch_bounds__(256) moments_tree_kernel(const sp_moments* __r
 
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
-                           cudaStream_t st) {
+                           unsigned int* ticket, cudaStream_t st) {
     if (cols == 0) return cudaSuccess;
     if (rows == 0) {  // empty accumulators (count 0, min +inf, max -inf)
         moments_tree_kernel<<<cols, 256, 0, st>>>(partial, 0, out);
@@ -322,10 +344,7 @@ cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uin
         uint32_t cp = 1;
         while (cp < cols) cp <<= 1;
         const uint32_t nb = (uint32_t)((rows + chunk - 1) / chunk);
-        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, chunk, status, partial);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        moments_tree_kernel<<<cols, 256, 0, st>>>(partial, nb, out);
+        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, chunk, status, partial, ticket, out);
         return cudaGetLastError();
     }
     nblocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(nblocks, 256), std::max<uint64_t>(1, rows / 1024));
