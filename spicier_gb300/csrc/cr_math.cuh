@@ -252,28 +252,44 @@ SP_HD double div_pos(double a, double b) {
     const uint64_t ba = dbits(a), bb = dbits(b);
     const uint64_t ma = (ba & ((1ULL << 52) - 1)) | (1ULL << 52), mb = (bb & ((1ULL << 52) - 1)) | (1ULL << 52);
     int e = (int)(ba >> 52) - (int)(bb >> 52) + 1023;
-    // quotient mantissa: floor(ma 2^s / mb) with 53 significant bits, s = 52 or 53
+    // quotient mantissa q = floor(ma 2^s / mb) has 53 bits with s = 52 or 53
     const int s = ma >= mb ? 52 : 53;
     e -= s - 52;
-    const u128 num = (u128)ma << s;
-    // R ~ 2^115 / mb in (2^62, 2^63]: an FP32 reciprocal, then two Newton steps
+    // reciprocal 2^63 / (mb 2^-52) ~ R in (2^62, 2^63]: FP32 estimate, one
+    // 32-bit Newton step, one 64-bit step
 #if defined(__CUDA_ARCH__)
     const float rf = __frcp_rn((float)(uint32_t)(mb >> 29));  // mb 2^-29 in [2^23, 2^24)
 #else
     const float rf = 1.0f / (float)(uint32_t)(mb >> 29);
 #endif
-    uint64_t R = (uint64_t)(uint32_t)(rf * 0x1p54f) << 32;  // rf 2^86
-    for (int it = 0; it < 2; ++it) {
-        const u128 mr = (u128)mb * R;                                    // ~2^115
+    uint32_t r32 = (uint32_t)(rf * 0x1p54f);  // 2^31 / (mb 2^-52), in (2^30, 2^31]
+    {
+        const uint32_t m32 = (uint32_t)(mb >> 21);                        // mb 2^-21 in [2^31, 2^32)
+        const uint64_t e32 = (uint64_t)m32 * r32;                         // ~2^62
+        const uint32_t c32 = (uint32_t)(((1ULL << 63) - e32) >> 31) ;     // (2 - e) 2^31 ~ 2^32
+        r32 = (uint32_t)(((uint64_t)r32 * c32) >> 32) << 1;               // refined, ~2^31
+    }
+    uint64_t R = (uint64_t)r32 << 32;  // ~2^63 / (mb 2^-52)
+    {
+        const u128 mr = (u128)mb * R;                                     // ~2^115
         const uint64_t corr = (uint64_t)((((u128)1 << 116) - mr) >> 52);  // (2 - mb R 2^-115) 2^63
         R = (uint64_t)(((u128)R * corr) >> 63);
     }
-    uint64_t q = (uint64_t)(((num >> 52) * (u128)R) >> 63);  // ~ num / mb
-    // exact correction: rem = num - q mb in [0, mb)
-    for (int it = 0; it < 3 && (u128)q * mb > num; ++it) --q;
-    for (int it = 0; it < 3 && (u128)(q + 1) * mb <= num; ++it) ++q;
-    const uint64_t rem = (uint64_t)(num - (u128)q * mb);
-    q += (2 * (u128)rem > mb || (2 * (u128)rem == mb && (q & 1))) ? 1 : 0;
+    const uint64_t a54 = ma << (s - 52);  // num = a54 2^52
+    uint64_t q = (uint64_t)(((u128)a54 * R) >> 63);  // ~ num / mb, within a few units
+    // exact remainder of num = q mb + rem, then at most two corrections each way
+    const u128 num = (u128)a54 << 52;
+    __int128 rem = (__int128)(num - (u128)q * mb);
+    for (int it = 0; it < 2 && rem < 0; ++it) {
+        --q;
+        rem += mb;
+    }
+    for (int it = 0; it < 2 && rem >= (__int128)mb; ++it) {
+        ++q;
+        rem -= mb;
+    }
+    const uint64_t r = (uint64_t)rem;
+    q += (2 * r > mb || (2 * r == mb && (q & 1))) ? 1 : 0;
     return bdouble(((uint64_t)e << 52) + (q - (1ULL << 52)));
 }
 
@@ -294,18 +310,34 @@ SP_HD double sqrt_pos(double x) {
 #else
     const float gf = 1.0f / std::sqrt(uf);
 #endif
-    uint64_t G = (uint64_t)(uint32_t)(gf * 0x1p31f) << 32;  // g = 1/sqrt(u), as g 2^63
-    for (int it = 0; it < 2; ++it) {
-        const uint64_t A = (uint64_t)(((u128)G * G) >> 64);          // g^2 2^62
-        const uint64_t B = (uint64_t)(((u128)U * A) >> 64);          // u g^2 2^60
-        const uint64_t T = (3ULL << 60) - B;                          // (3 - u g^2) 2^60
-        G = (uint64_t)(((u128)G * T) >> 64) << 3;                     // g (3 - u g^2)/2 2^63
+    // g = 1/sqrt(u): one 32-bit Newton step (g 2^31), one 64-bit step (g 2^63)
+    uint32_t g32 = (uint32_t)(gf * 0x1p31f);
+    {
+        const uint32_t u32 = (uint32_t)(U >> 32);                        // u 2^30
+        const uint32_t a = (uint32_t)(((uint64_t)g32 * g32) >> 32);      // g^2 2^30
+        const uint32_t bb = (uint32_t)(((uint64_t)u32 * a) >> 32);       // u g^2 2^28
+        const uint32_t t = (3u << 28) - bb;                              // (3 - u g^2) 2^28
+        g32 = (uint32_t)(((uint64_t)g32 * t) >> 29);                     // g (3 - u g^2)/2 2^31
     }
-    uint64_t r = (uint64_t)(((u128)U * G) >> 64) >> 9;  // sqrt(u) 2^52
+    uint64_t G = (uint64_t)g32 << 32;
+    {
+        const uint64_t A = (uint64_t)(((u128)G * G) >> 64);  // g^2 2^62
+        const uint64_t B = (uint64_t)(((u128)U * A) >> 64);  // u g^2 2^60
+        const uint64_t T = (3ULL << 60) - B;                  // (3 - u g^2) 2^60
+        G = (uint64_t)(((u128)G * T) >> 64) << 3;             // 2^63
+    }
+    uint64_t r = (uint64_t)(((u128)U * G) >> 64) >> 9;  // sqrt(u) 2^52, within a few units
     const u128 N = (u128)M << 52;
-    for (int it = 0; it < 3 && (u128)r * r > N; ++it) --r;
-    for (int it = 0; it < 3 && (u128)(r + 1) * (r + 1) <= N; ++it) ++r;
-    r += (N - (u128)r * r > r) ? 1 : 0;  // round to nearest (no ties: N is an integer)
+    __int128 rem = (__int128)(N - (u128)r * r);  // N - r^2
+    for (int it = 0; it < 2 && rem < 0; ++it) {
+        --r;
+        rem += 2 * (__int128)r + 1;
+    }
+    for (int it = 0; it < 2 && rem > 2 * (__int128)r; ++it) {
+        rem -= 2 * (__int128)r + 1;
+        ++r;
+    }
+    r += rem > (__int128)r ? 1 : 0;  // round to nearest (no ties: N is an integer)
     return bdouble(((uint64_t)(E / 2 + 1023) << 52) + (r - (1ULL << 52)));
 }
 
@@ -323,6 +355,7 @@ __device__ __noinline__ static double hw_sqrt(double a) { return sqrt(a); }
 
 SP_HD double ieee_mul(double a, double b) {
 #if defined(__CUDA_ARCH__)
+    if (cr::dbits(b) == 0x3FF0000000000000ULL) return a;  // a * 1 = a for every non-signalling a
     const int ea = (int)((cr::dbits(a) >> 52) & 0x7ff), eb = (int)((cr::dbits(b) >> 52) & 0x7ff);
     const int e = ea + eb - 1023;
     if (ea != 0 && eb != 0 && ea != 0x7ff && eb != 0x7ff && e >= 2 && e <= 2045) return cr::mul_rn(a, b);

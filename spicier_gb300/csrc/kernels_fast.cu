@@ -302,8 +302,21 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
     if (!last) return;
     __threadfence();
     sp_moments f{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
-    if (c < cols)
-        for (uint32_t b = g; b < gridDim.x; b += groups) mom_merge(f, partial[(size_t)c * gridDim.x + b]);
+    if (c < cols) {
+        // four partials in flight per thread, merged in order
+        const sp_moments* pc = partial + (size_t)c * gridDim.x;
+        for (uint32_t b0 = g; b0 < gridDim.x; b0 += 4 * groups) {
+            sp_moments q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t b = b0 + (uint32_t)u * groups;
+                q[u] = b < gridDim.x ? pc[b] : sp_moments{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (b0 + (uint32_t)u * groups < gridDim.x) mom_merge(f, q[u]);
+        }
+    }
     sh[threadIdx.x] = f;
     __syncthreads();
     for (uint32_t w = groups / 2; w >= 1; w >>= 1) {

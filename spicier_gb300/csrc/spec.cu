@@ -455,7 +455,7 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
         for (int k = 0; k < t->num_derived; ++k) o << "#define c" << k << " (spx_cd[" << k << " * 128])\n";
         for (size_t j = 0; j < fcs.size(); ++j) o << "#define cf" << fcs[j] << " (spx_cf[" << j << " * 128])\n";
     }
-    o << "extern \"C\" __global__ void __launch_bounds__(128, " << (sm ? (fp32_jac ? 3 : 2) : 1) << ") spec_newton(SpecArgs a) {\n"
+    o << "extern \"C\" __global__ void __launch_bounds__(128, " << (sm ? (fp32_jac ? 4 : 2) : 1) << ") spec_newton(SpecArgs a) {\n"
       << "  const u64 nthreads = (u64)gridDim.x * blockDim.x;\n"
       << "  u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
       << "  if (s >= a.count) return;\n"
