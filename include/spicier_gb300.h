@@ -501,6 +501,40 @@ int sp_transient(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
                  const double* table, uint32_t table_cols, double* x, double* probe, uint8_t* status);
 
 /* ---------------------------------------------------------------------- */
+/* Batched AC small-signal sweeps (solve_ac, ac.rs:357-400, with the netlist */
+/* AC stamper of crates/spicier-cli/src/stampers.rs): per sample the DC      */
+/* operating point (the Newton path, cfg as for sp_newton_dc), the devices'  */
+/* small-signal conductances there (ac_info_at), and at every frequency the */
+/* complex MNA solve with the reference's dense LU.  Unknowns: nodes, then  */
+/* the branch currents (V sources and inductors) as in the DC path.         */
+/* ---------------------------------------------------------------------- */
+enum sp_ac_sweep_type { SP_AC_LIN = 0, SP_AC_DEC = 1, SP_AC_OCT = 2 };
+typedef struct sp_ac_config {
+    double fstart, fstop;
+    int32_t num_points;  /* total (linear) or per decade / octave              */
+    int32_t sweep;       /* sp_ac_sweep_type                                   */
+    int32_t source;      /* -1: every V source at AC magnitude 1 (ac_info's   */
+                         /* default); else the element index of the stimulus */
+    int32_t num_probe;   /* 1..8 unknowns recorded                             */
+    int32_t probe[8];
+} sp_ac_config;
+
+/* The frequency grid (generate_frequencies, ac.rs:258-287): writes up to cap
+ * values to freqs (may be NULL) and returns the number of frequencies. */
+int sp_ac_frequencies(const sp_ac_config* cfg, double* freqs, int cap);
+/* probe[count][nf][num_probe] complex values as (re, im) double pairs;
+ * status: the DC status, or SP_ST_SINGULAR when a frequency's matrix was
+ * singular (that frequency's probes NaN).  Samples whose DC point did not
+ * converge get NaN probes. */
+int sp_ac_sweep_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_config* dc_cfg,
+                       const sp_ac_config* ac, uint64_t seed, uint64_t first_index, uint64_t count,
+                       const double* d_table, uint32_t table_cols, double* d_probe, uint8_t* d_status,
+                       void* stream);
+int sp_ac_sweep(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* dc_cfg, const sp_ac_config* ac,
+                uint64_t seed, uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
+                double* probe, uint8_t* status);
+
+/* ---------------------------------------------------------------------- */
 /* Learned Newton warm start (no counterpart in the reference).            */
 /* A BF16 MLP n_in -> n_layers x n_hidden (GELU) -> n_out, trained and run */
 /* on the tensor cores with FP32 accumulation; FP32 master weights + Adam. */

@@ -103,6 +103,9 @@ def _bind(L):
         "or_cr_cos_full_batch": (None, [P(d), u64, P(d), P(C.c_uint)]),
         "or_cr_fast_misses": (u64, [i32, P(d), u64]),
         "or_ieee_int_mismatches": (u64, [u64, u64]),
+        "or_ac_frequencies": (i32, [d, d, i32, i32, P(d), i32]),
+        "or_ac_sweep": (i32, [vp_, vp_, u64, u64, u64, P(d), u32, P(d), i32, i32, P(C.c_int), i32, P(d),
+                              P(C.c_uint8), i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -261,3 +264,29 @@ def transient(circuit, cfg, seed, count, method, h, tstop, probe_idx=-1, first=0
     lib().or_transient(C.byref(cc), C.byref(cfg), seed, first, count, _dp(table), cols, method, h, tstop, probe_idx,
                        _dp(x), _dp(pr), st.ctypes.data_as(C.POINTER(C.c_uint8)), threads)
     return x, pr, st
+
+
+def ac_frequencies(fstart, fstop, num_points, sweep):
+    """AC frequency grid (generate_frequencies): sweep 0 linear, 1 decade, 2 octave."""
+    n = lib().or_ac_frequencies(fstart, fstop, num_points, sweep, None, 0)
+    out = np.zeros(max(n, 1))
+    lib().or_ac_frequencies(fstart, fstop, num_points, sweep, _dp(out), n)
+    return out[:n]
+
+
+def ac_sweep(circuit, cfg, seed, count, freqs, probes, source=-1, first=0, table=None, threads=0):
+    """Oracle batched AC sweep: (probe[count][nf][np] complex, status[count])."""
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    pr = np.ascontiguousarray(probes, dtype=np.int32)
+    out = np.zeros((count, freqs.size, pr.size, 2))
+    st = np.zeros(count, np.uint8)
+    cols = 0
+    if table is not None:
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        cols = table.shape[1]
+    cc = circuit.to_c()
+    lib().or_ac_sweep(C.cast(C.pointer(cc), C.c_void_p), C.cast(C.pointer(cfg), C.c_void_p), seed, first, count,
+                      _dp(table), cols, _dp(freqs), freqs.size, source, pr.ctypes.data_as(C.POINTER(C.c_int)),
+                      pr.size, _dp(out), st.ctypes.data_as(C.POINTER(C.c_uint8)), threads)
+    return out[..., 0] + 1j * out[..., 1], st
+

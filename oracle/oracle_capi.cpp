@@ -12,6 +12,7 @@
 
 #include "oracle_core.hpp"
 #include "transient.hpp"
+#include "ac.hpp"
 #include "powergrid.hpp"
 
 
@@ -222,6 +223,55 @@ int or_newton_dc(const sp_circuit* c, const sp_newton_config* cfg, uint64_t seed
             uint8_t st = dc_pipeline(*c, P.data(), *cfg, x0 ? x0 + i * n : nullptr, x + i * n, &it, m);
             if (iters) iters[i] = it;
             if (status) status[i] = st;
+        }
+    });
+    return 0;
+}
+
+// AC frequency grid (ac.rs:258-287): writes up to cap values, returns the count.
+int or_ac_frequencies(double fstart, double fstop, int num_points, int sweep, double* out, int cap) {
+    const std::vector<double> f = ac_frequencies(fstart, fstop, num_points, sweep);
+    for (int i = 0; i < (int)f.size() && i < cap; ++i) out[i] = f[i];
+    return (int)f.size();
+}
+
+// Batched AC sweep: per sample the draws, the DC pipeline, then the complex
+// solve at every frequency; probe[count][nf][np] complex (re, im) values of
+// the given unknowns; status: the DC status, or SP_ST_SINGULAR when a
+// frequency's matrix was singular (its probes NaN).
+int or_ac_sweep(const sp_circuit* c, const sp_newton_config* cfg, uint64_t seed, uint64_t first, uint64_t count,
+                const double* table, uint32_t cols, const double* freqs, int nf, int source, const int* probes,
+                int np, double* probe, uint8_t* status, int threads) {
+    const int n = c->num_nodes + c->num_branches;
+    const int npar = c->num_params;
+    parallel_for(count, threads, [&](int, uint64_t lo, uint64_t hi) {
+        Mna m;
+        m.init(c->num_nodes, c->num_branches);
+        std::vector<double> P(npar), x(n);
+        std::vector<Cx> A((size_t)n * n), b(n);
+        for (uint64_t i = lo; i < hi; ++i) {
+            const double* row = table ? table + i * cols : nullptr;
+            for (int k = 0; k < npar; ++k) P[k] = draw_param(c->params[k], seed, (uint32_t)(first + i), row);
+            int it = 0;
+            uint8_t st = dc_pipeline(*c, P.data(), *cfg, nullptr, x.data(), &it, m);
+            double* out = probe + i * (size_t)nf * np * 2;
+            if ((st & SP_ST_MASK) != SP_ST_CONVERGED) {
+                for (size_t k = 0; k < (size_t)nf * np * 2; ++k) out[k] = NAN;
+                status[i] = st;
+                continue;
+            }
+            const AcLinear L = ac_linearise(*c, P.data(), x.data(), source);
+            for (int f = 0; f < nf; ++f) {
+                const double w = 2.0 * 3.141592653589793 * freqs[f];
+                ac_matrix(*c, P.data(), L, w, A.data(), b.data());
+                const bool ok = lu_solve_complex(n, A.data(), b.data());
+                if (!ok) st = (uint8_t)((st & ~SP_ST_MASK) | SP_ST_SINGULAR);
+                for (int k = 0; k < np; ++k) {
+                    out[((size_t)f * np + k) * 2] = ok ? b[probes[k]].re : NAN;
+                    out[((size_t)f * np + k) * 2 + 1] = ok ? b[probes[k]].im : NAN;
+                }
+            }
+            status[i] = st;
         }
     });
     return 0;

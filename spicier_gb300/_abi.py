@@ -183,6 +183,27 @@ def transient_config(tstep: float, tstop: float, method: int = SP_TRAN_BE, probe
     return SpTransientConfig(tstep, tstop, method, probe, precision, 0)
 
 
+SP_AC_LIN, SP_AC_DEC, SP_AC_OCT = 0, 1, 2
+
+
+class SpAcConfig(C.Structure):
+    _fields_ = [("fstart", C.c_double), ("fstop", C.c_double), ("num_points", C.c_int32), ("sweep", C.c_int32),
+                ("source", C.c_int32), ("num_probe", C.c_int32), ("probe", C.c_int32 * 8)]
+
+
+def ac_config(fstart: float, fstop: float, num_points: int, sweep: int = SP_AC_DEC, probes=(0,),
+              source: int = -1) -> SpAcConfig:
+    """AC sweep settings (AcParams, ac.rs:30-40): frequency range and points (total for SP_AC_LIN, per decade or
+    octave otherwise), the recorded unknowns (1..8) and the stimulus (-1: every V source at AC magnitude 1, as
+    the reference's ac_info default; else the element index of the one source)."""
+    c = SpAcConfig()
+    c.fstart, c.fstop, c.num_points, c.sweep, c.source = fstart, fstop, num_points, sweep, source
+    c.num_probe = len(probes)
+    for k, p in enumerate(probes):
+        c.probe[k] = p
+    return c
+
+
 class SpLadderConfig(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("tstop", "h_init", "h_min", "h_max", "lte_reltol", "lte_abstol",
                                           "v_reltol", "v_abstol", "i_abstol", "r_lo", "r_hi", "c_lo", "c_hi",

@@ -103,6 +103,11 @@ def _bind(L):
                                        vp, vp, vp, vp, vp]),
         "sp_topology_specialize": (i32, [vp, vp, i32, i32, C.c_char_p, C.c_size_t]),
         "sp_specialize_source": (i32, [P(abi.SpCircuit), i32, i32, C.c_char_p, C.c_size_t, P(i32)]),
+        "sp_ac_frequencies": (i32, [P(abi.SpAcConfig), vp, i32]),
+        "sp_ac_sweep_device": (i32, [vp, vp, P(abi.SpNewtonConfig), P(abi.SpAcConfig), u64, u64, u64, vp, u32, vp, vp,
+                                     vp]),
+        "sp_ac_sweep": (i32, [vp, P(abi.SpCircuit), P(abi.SpNewtonConfig), P(abi.SpAcConfig), u64, u64, u64, vp, u32,
+                              vp, vp]),
         "sp_transient_device": (i32, [vp, vp, P(abi.SpNewtonConfig), P(abi.SpTransientConfig), u64, u64, u64, vp,
                                       u32, vp, vp, vp, vp]),
         "sp_transient": (i32, [vp, P(abi.SpCircuit), P(abi.SpNewtonConfig), P(abi.SpTransientConfig), u64, u64, u64, vp, u32, vp,

@@ -256,6 +256,37 @@ class Context:
                                                            _vp(accepted), _vp(rejected), _vp(iterations),
                                                            _vp(status), _vp(probe), stream))
 
+    # -- AC small-signal sweeps ------------------------------------------------
+    @staticmethod
+    def ac_frequencies(cfg: abi.SpAcConfig) -> np.ndarray:
+        """The frequency grid of an AC sweep (generate_frequencies)."""
+        n = load().sp_ac_frequencies(C.byref(cfg), None, 0)
+        out = np.zeros(max(n, 1))
+        load().sp_ac_frequencies(C.byref(cfg), _vp(out), n)
+        return out[:n]
+
+    def ac_sweep(self, circuit: Circuit, dc_cfg: abi.SpNewtonConfig, cfg: abi.SpAcConfig, seed: int, count: int,
+                 first: int = 0, table=None):
+        """Host-buffer batched AC sweep (sp_ac_sweep): (probe [count][nf][num_probe] complex, status [count])."""
+        nf = len(self.ac_frequencies(cfg))
+        out = np.zeros((count, nf, cfg.num_probe, 2))
+        st = np.zeros(count, np.uint8)
+        cols = 0
+        if table is not None:
+            table = np.ascontiguousarray(table, dtype=np.float64)
+            cols = table.shape[1]
+        cc = circuit.to_c()
+        check(self._ptr, load().sp_ac_sweep(self._ptr, C.byref(cc), C.byref(dc_cfg), C.byref(cfg), seed, first, count,
+                                            _vp(table), cols, _vp(out), _vp(st)))
+        return out[..., 0] + 1j * out[..., 1], st
+
+    def ac_sweep_device(self, topo: Topology, dc_cfg, cfg, seed, count, probe, status, first: int = 0, table=None,
+                        stream: int = 0):
+        """Device-buffer variant: probe [count][nf][num_probe][2] f64, status uint8 [count] (torch CUDA tensors)."""
+        cols = 0 if table is None else int(table.shape[1])
+        check(self._ptr, load().sp_ac_sweep_device(self._ptr, topo._ptr, C.byref(dc_cfg), C.byref(cfg), seed, first,
+                                                   count, _vp(table), cols, _vp(probe), _vp(status), stream))
+
     # -- fixed-step linear transients -----------------------------------------
     def transient(self, circuit: Circuit, dc_cfg: abi.SpNewtonConfig, cfg: abi.SpTransientConfig, seed: int,
                   count: int, first: int = 0, table=None) -> dict:

@@ -1,0 +1,283 @@
+// Batched AC small-signal sweep: one thread per (sample, frequency).
+//
+// From each sample's DC operating point (the Newton path's output), the
+// devices' small-signal conductances (ac_info_at: diode.rs:202-220,
+// mosfet/level1.rs:307-331, bjt.rs:404-427) and the reactive terms at
+// w = 2 pi f are stamped into a complex MNA matrix exactly as the netlist AC
+// stamper does (crates/spicier-cli/src/stampers.rs:94-330, ComplexMna in
+// crates/spicier-solver/src/ac.rs:121-240), then solved by the dense complex
+// LU of solve_complex (nalgebra LU on num_complex numbers, linear.rs:557-583):
+// pivot = first maximum of |re| + |im| in the column, num_complex's operation
+// order for products and quotients.  In the exact build (no FMA contraction)
+// the result is the oracle's bit for bit wherever the DC point is.
+//
+// Real contributions accumulate in element order, then the imaginary ones
+// (capacitors, inductors) in element order: each component's sum has the
+// order of the reference's triplet sum.  The matrix and right-hand side live
+// interleaved per thread ([element][thread]) in shared memory, or in a global
+// work buffer with the same layout when n is too large for shared memory.
+#pragma once
+#include "circuit_dev.cuh"
+#include "internal.h"
+
+namespace sp {
+
+struct AcLaunch {
+    DevCircuit c;
+    const double* params;  // [count][np] the DC pass's drawn parameters
+    int np;
+    const double* x_dc;     // [count][n]
+    const uint8_t* dc_status;
+    uint64_t count;
+    const double* freqs;    // [nf]
+    int nf;
+    int source;             // -1: every V source at magnitude 1; else the element index of the stimulus
+    int num_probe;
+    int probe[8];
+    double* out;            // [count][nf][num_probe][2]
+    unsigned int* singular; // [count] set when a frequency's matrix was singular
+    double* work;           // global interleaved work area ([2 (n^2 + n)][grid threads]), or nullptr
+};
+
+#ifdef SP_AC_KERNELS  // the kernels: only in the translation unit that builds them (no FMA contraction)
+// complex number stored at p[0], p[stride] (re, im) of an interleaved array
+struct CxRef {
+    double* p;
+    int64_t stride;
+    __device__ double& re() const { return p[0]; }
+    __device__ double& im() const { return p[stride]; }
+};
+
+struct CxArr {
+    double* base;
+    int64_t stride;  // distance between consecutive doubles of one thread
+    __device__ CxRef operator[](int k) const { return CxRef{base + (int64_t)(2 * k) * stride, stride}; }
+};
+
+__device__ inline void ac_add_re(CxArr A, int n, int r, int c, double v) {
+    if (r >= 0 && c >= 0) A[c * n + r].re() += v;
+}
+__device__ inline void ac_add_im(CxArr A, int n, int r, int c, double v) {
+    if (r >= 0 && c >= 0) A[c * n + r].im() += v;
+}
+
+// nalgebra LU + solve on the interleaved complex matrix (column-major), b -> x.
+__device__ inline bool ac_lu_solve(int n, CxArr A, CxArr b, int8_t* swap_with) {
+    for (int i = 0; i < n; ++i) {
+        int piv = i;
+        double best = fabs(A[i * n + i].re()) + fabs(A[i * n + i].im());
+        for (int r = i + 1; r < n; ++r) {
+            const double v = fabs(A[i * n + r].re()) + fabs(A[i * n + r].im());
+            if (v > best) {
+                best = v;
+                piv = r;
+            }
+        }
+        swap_with[i] = -1;
+        const double dre = A[i * n + piv].re(), dim = A[i * n + piv].im();
+        if (dre == 0.0 && dim == 0.0) continue;
+        if (piv != i) {
+            swap_with[i] = (int8_t)piv;
+            for (int c = 0; c < n; ++c) {
+                const double tr = A[c * n + i].re(), ti = A[c * n + i].im();
+                A[c * n + i].re() = A[c * n + piv].re();
+                A[c * n + i].im() = A[c * n + piv].im();
+                A[c * n + piv].re() = tr;
+                A[c * n + piv].im() = ti;
+            }
+        }
+        // inv = 1 / diag (num_complex: (1 re + 0 im) / d)
+        const double ns = dre * dre + dim * dim;
+        const double ire = (1.0 * dre + 0.0 * dim) / ns, iim = (0.0 * dre - 1.0 * dim) / ns;
+        for (int r = i + 1; r < n; ++r) {
+            const double ar = A[i * n + r].re(), ai = A[i * n + r].im();
+            A[i * n + r].re() = ar * ire - ai * iim;
+            A[i * n + r].im() = ar * iim + ai * ire;
+        }
+        for (int c = i + 1; c < n; ++c) {
+            const double pr = -A[c * n + i].re(), pi = -A[c * n + i].im();
+            for (int r = i + 1; r < n; ++r) {
+                const double ar = A[i * n + r].re(), ai = A[i * n + r].im();
+                const double mr = pr * ar - pi * ai, mi = pr * ai + pi * ar;
+                A[c * n + r].re() = mr + A[c * n + r].re();
+                A[c * n + r].im() = mi + A[c * n + r].im();
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        const int p = swap_with[i];
+        if (p >= 0) {
+            const double tr = b[i].re(), ti = b[i].im();
+            b[i].re() = b[p].re();
+            b[i].im() = b[p].im();
+            b[p].re() = tr;
+            b[p].im() = ti;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        const double cr = -b[i].re(), ci = -b[i].im();
+        for (int r = i + 1; r < n; ++r) {
+            const double ar = A[i * n + r].re(), ai = A[i * n + r].im();
+            const double mr = cr * ar - ci * ai, mi = cr * ai + ci * ar;
+            b[r].re() = mr + b[r].re();
+            b[r].im() = mi + b[r].im();
+        }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        const double dr = A[i * n + i].re(), di = A[i * n + i].im();
+        if (dr == 0.0 && di == 0.0) return false;
+        const double ns = dr * dr + di * di;
+        const double br = b[i].re(), bi = b[i].im();
+        const double qr = (br * dr + bi * di) / ns, qi = (bi * dr - br * di) / ns;
+        b[i].re() = qr;
+        b[i].im() = qi;
+        const double cr = -qr, ci = -qi;
+        for (int r = 0; r < i; ++r) {
+            const double ar = A[i * n + r].re(), ai = A[i * n + r].im();
+            const double mr = cr * ar - ci * ai, mi = cr * ai + ci * ar;
+            b[r].re() = mr + b[r].re();
+            b[r].im() = mi + b[r].im();
+        }
+    }
+    return true;
+}
+
+// bjt.rs:176-259 evaluate at (vbe, vce): o[3..5] = gm, gpi, go (floored at 1e-12).
+__device__ inline void bjt_eval_ac(bool pnp, double is, double bf, double br, double nf_vt, double nr_vt, double vaf,
+                                   double vbe, double vce, double o[6]) {
+    if (pnp) {
+        vbe = -vbe;
+        vce = -vce;
+    }
+    const double vbc = vbe - vce;
+    const double vbe_l = limit_voltage(vbe, nf_vt, diode_vcrit(nf_vt));
+    const double vbc_l = limit_voltage(vbc, nr_vt, diode_vcrit(nr_vt));
+    const double exp_be = exp(vbe_l / nf_vt), exp_bc = exp(vbc_l / nr_vt);
+    const double i_f = is * (exp_be - 1.0), i_r = is * (exp_bc - 1.0);
+    const bool vfin = isfinite(vaf) && vaf > 0.0;
+    const double early = (vfin && vce > 0.0) ? 1.0 + vce / vaf : 1.0;
+    const double ic = (i_f - i_r / br) * early;
+    const double gm = (i_f > 1e-20) ? (is * exp_be / nf_vt) * early : 1e-12;
+    const double gpi = gm / bf;
+    const double go_early = (vfin && fabs(ic) > 1e-20) ? fabs(ic) / vaf : 0.0;
+    const double go = fmax(go_early + is * exp_bc / nr_vt / br * early, 1e-12);
+    o[3] = fmax(gm, 1e-12);
+    o[4] = fmax(gpi, 1e-12);
+    o[5] = fmax(go, 1e-12);
+}
+
+// One (sample, frequency) unit u = s * nf + f with the work area A.
+__device__ inline void ac_unit(const AcLaunch& L, uint64_t u, CxArr A) {
+    const uint64_t s = u / (uint64_t)L.nf;
+    const int f = (int)(u % (uint64_t)L.nf);
+    const DevCircuit& c = L.c;
+    const int n = c.n, nn = c.num_nodes;
+    double* out = L.out + (u * (uint64_t)L.num_probe) * 2;
+    if ((L.dc_status[s] & SP_ST_MASK) != SP_ST_CONVERGED) {
+        for (int k = 0; k < 2 * L.num_probe; ++k) out[k] = CUDART_NAN;
+        return;
+    }
+    const CxArr b{A.base + (int64_t)(2 * n * n) * A.stride, A.stride};
+    for (int k = 0; k < n * n; ++k) A[k].re() = 0.0, A[k].im() = 0.0;
+    for (int k = 0; k < n; ++k) b[k].re() = 0.0, b[k].im() = 0.0;
+    const double* P = L.params + s * (uint64_t)L.np;
+    const double* x = L.x_dc + s * (uint64_t)n;
+    auto V = [&](int i) { return i >= 0 ? x[i] : 0.0; };
+    auto cond = [&](int i, int j, double g) {
+        ac_add_re(A, n, i, i, g), ac_add_re(A, n, j, j, g), ac_add_re(A, n, i, j, -g), ac_add_re(A, n, j, i, -g);
+    };
+    auto vccs = [&](int op, int on, int cp, int cn, double gm) {
+        ac_add_re(A, n, op, cp, gm), ac_add_re(A, n, op, cn, -gm), ac_add_re(A, n, on, cp, -gm),
+            ac_add_re(A, n, on, cn, gm);
+    };
+    const double vt = thermal_voltage_300();
+    for (int e = 0; e < c.num_elements; ++e) {
+        const sp_element el = c.el[e];
+        const int a0 = el.node[0], a1 = el.node[1], a2 = el.node[2];
+        switch (el.kind) {
+            case SP_EL_R: cond(a0, a1, 1.0 / P[el.field[0]]); break;
+            case SP_EL_V:
+            case SP_EL_L: {
+                const int br = nn + el.branch;
+                ac_add_re(A, n, a0, br, 1.0), ac_add_re(A, n, br, a0, 1.0);
+                ac_add_re(A, n, a1, br, -1.0), ac_add_re(A, n, br, a1, -1.0);
+                if (el.kind == SP_EL_V && (L.source < 0 || L.source == e)) b[br].re() += 1.0;
+                break;
+            }
+            case SP_EL_D: {  // diode.rs evaluate at vd (it limits once)
+                const double nvt = P[el.field[1]] * vt;
+                const double vd = V(a0) - V(a1);
+                const double vl = limit_voltage(vd, nvt, diode_vcrit(nvt));
+                const double g = P[el.field[0]] * exp(vl / nvt) / nvt;
+                cond(a0, a1, fmax(g, 1e-12));
+                break;
+            }
+            case SP_EL_NMOS:
+            case SP_EL_PMOS: {
+                const double kp = P[el.field[1]], w = P[el.field[3]], l = P[el.field[4]], nf = P[el.field[5]];
+                double ids, gds, gm;
+                mos_eval(el.kind == SP_EL_PMOS, fabs(P[el.field[0]]), kp * nf * w / l, P[el.field[2]],
+                         V(a1) - V(a2), V(a0) - V(a2), ids, gds, gm);
+                cond(a0, a2, gds);
+                vccs(a0, a2, a1, a2, gm);
+                break;
+            }
+            case SP_EL_NPN:
+            case SP_EL_PNP: {
+                double o[6];
+                bjt_eval_ac(el.kind == SP_EL_PNP, P[el.field[0]], P[el.field[1]], P[el.field[2]],
+                            P[el.field[3]] * vt, P[el.field[4]] * vt, P[el.field[5]], V(a1) - V(a2),
+                            V(a0) - V(a2), o);
+                cond(a1, a2, o[4]);
+                cond(a0, a2, o[5]);
+                vccs(a0, a2, a1, a2, o[3]);
+                break;
+            }
+            default:
+                break;
+        }
+    }
+    const double wv = 2.0 * 3.141592653589793 * L.freqs[f];
+    for (int e = 0; e < c.num_elements; ++e) {
+        const sp_element el = c.el[e];
+        if (el.kind == SP_EL_C) {
+            const double y = wv * P[el.field[0]];
+            const int i = el.node[0], j = el.node[1];
+            ac_add_im(A, n, i, i, y), ac_add_im(A, n, j, j, y), ac_add_im(A, n, i, j, -y), ac_add_im(A, n, j, i, -y);
+        } else if (el.kind == SP_EL_L) {
+            const int br = nn + el.branch;
+            A[br * n + br].im() -= wv * P[el.field[0]];
+        }
+    }
+    int8_t swap_with[64];
+    const bool ok = ac_lu_solve(n, A, b, swap_with);
+    if (!ok) atomicOr(L.singular + s, 1u);
+    for (int k = 0; k < L.num_probe; ++k) {
+        out[2 * k] = ok ? b[L.probe[k]].re() : CUDART_NAN;
+        out[2 * k + 1] = ok ? b[L.probe[k]].im() : CUDART_NAN;
+    }
+}
+
+// Grid-stride over the units; thread t's work area is column t of the
+// interleaved shared (blockDim threads) or global (gridDim * blockDim) array.
+__global__ void __launch_bounds__(128) ac_kernel(AcLaunch L) {
+    extern __shared__ __align__(16) unsigned char ac_smem[];
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    const CxArr A = L.work ? CxArr{L.work + t, (int64_t)nthreads}
+                           : CxArr{reinterpret_cast<double*>(ac_smem) + threadIdx.x, (int64_t)blockDim.x};
+    const uint64_t total = L.count * (uint64_t)L.nf;
+    for (uint64_t u = t; u < total; u += nthreads) ac_unit(L, u, A);
+}
+
+__global__ void ac_status_kernel(uint64_t count, const uint8_t* dc_status, const unsigned int* singular,
+                                 uint8_t* status) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= count) return;
+    const uint8_t st = dc_status[s];
+    status[s] = singular[s] ? (uint8_t)((st & ~SP_ST_MASK) | SP_ST_SINGULAR) : st;
+}
+
+#endif  // SP_AC_KERNELS
+
+}  // namespace sp

@@ -10,6 +10,7 @@
 #include "internal.h"
 #include "ladder.cuh"
 #include "transient_fixed.cuh"
+#include "ac.cuh"
 #include "powergrid.cuh"
 
 using namespace sp;
@@ -494,7 +495,7 @@ static int newton_scratch(sp_ctx* ctx, const sp_topology* t, uint64_t count, New
     size_t bd = align256(8 * (size_t)t->num_derived * count);
     size_t bl = align256(4 * count);
     size_t bc = 256;
-    uint32_t mb = (uint32_t)std::max<uint64_t>(256, (count + 511) / 512);  // partials per column
+    uint32_t mb = (uint32_t)std::max<uint64_t>(1216, (count + 511) / 512);  // partials per column
     size_t bm = align256(sizeof(sp_moments) * mb * (size_t)t->n);
     size_t bx = want_x0 ? align256(8 * (size_t)t->n * count) : 0;
     int rc = ensure_scratch(ctx, bp + bd + bl + bc + bm + bx);
@@ -552,8 +553,8 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     NewtonScratch s;
     int rc = newton_scratch(ctx, t, count, s, warm != nullptr);
     if (rc) return rc;
-    // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64), [4] moments ticket
-    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 20, st), "clear counters");
+    // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64)
+    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 16, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
                  s.counters + 1};
     {
@@ -620,7 +621,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (d_moments) {
         ProfScope prof(ctx, "moments", st);
         e = launch_moments(d_x, count, (uint32_t)t->n, (uint32_t)t->n, d_status, s.partial, s.moment_blocks,
-                           d_moments, s.counters + 4, st);
+                           d_moments, st);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "moments launch");
     }
     return SP_OK;
@@ -769,14 +770,11 @@ int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32
     if (cols > ld) return fail(ctx, SP_ERR_INVALID_DIMENSION, "cols > ld");
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaSetDevice(ctx->device);
-    uint32_t mb = (uint32_t)std::max<uint64_t>(256, (rows + 511) / 512);  // partials per column
-    const size_t bpart = align256(sizeof(sp_moments) * mb * (size_t)cols);
-    int rc = ensure_scratch(ctx, bpart + 256);
+    uint32_t mb = (uint32_t)std::max<uint64_t>(1216, (rows + 511) / 512);  // partials per column
+    int rc = ensure_scratch(ctx, align256(sizeof(sp_moments) * mb * (size_t)cols));
     if (rc) return rc;
     ScratchOrder order(ctx, (cudaStream_t)stream);
-    unsigned int* ticket = (unsigned int*)((char*)ctx->scratch + bpart);
-    SP_CUDA(ctx, cudaMemsetAsync(ticket, 0, 4, (cudaStream_t)stream), "clear ticket");
-    SP_CUDA(ctx, launch_moments(d_values, rows, ld, cols, d_status, (sp_moments*)ctx->scratch, mb, d_out, ticket,
+    SP_CUDA(ctx, launch_moments(d_values, rows, ld, cols, d_status, (sp_moments*)ctx->scratch, mb, d_out,
                                 (cudaStream_t)stream),
             "moments launch");
     return SP_OK;
@@ -1217,6 +1215,149 @@ int sp_transient(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
     sp_topology_destroy(t);
     if (rc) return rc;
     return e == cudaSuccess ? SP_OK : cuda_fail(ctx, e, "transient copies");
+}
+
+
+// ---------------------------------------------------------------------------
+// AC small-signal sweeps (ac.cuh)
+// ---------------------------------------------------------------------------
+static std::vector<double> ac_grid(const sp_ac_config* c) {
+    std::vector<double> f;
+    if (c->sweep == SP_AC_LIN) {
+        if (c->num_points <= 1) return {c->fstart};
+        const double step = (c->fstop - c->fstart) / ((double)c->num_points - 1.0);
+        for (int i = 0; i < c->num_points; ++i) f.push_back(c->fstart + step * (double)i);
+        return f;
+    }
+    const double base = c->sweep == SP_AC_DEC ? 10.0 : 2.0;
+    const double span = c->sweep == SP_AC_DEC ? std::log10(c->fstop / c->fstart) : std::log2(c->fstop / c->fstart);
+    const long total = (long)std::ceil((double)c->num_points * span) + 1;
+    for (long i = 0; i < total && i < (1L << 20); ++i) {
+        const double v = c->fstart * std::pow(base, (double)i / (double)c->num_points);
+        if (v <= c->fstop * 1.001) f.push_back(v);
+    }
+    return f;
+}
+
+static int ac_validate(sp_ctx* ctx, const sp_ac_config* c, int n, int num_elements) {
+    if (!c) return SP_ERR_INVALID_ARGUMENT;
+    if (c->sweep < SP_AC_LIN || c->sweep > SP_AC_OCT) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "unknown sweep type");
+    if (!(c->fstart > 0) || !(c->fstop >= c->fstart) || c->num_points < 1)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "need 0 < fstart <= fstop and num_points >= 1");
+    if (c->num_probe < 1 || c->num_probe > 8) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "num_probe must be 1..8");
+    for (int k = 0; k < c->num_probe; ++k)
+        if (c->probe[k] < 0 || c->probe[k] >= n) return fail(ctx, SP_ERR_INVALID_DIMENSION, "probe %d out of range", k);
+    if (c->source < -1 || c->source >= num_elements) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad AC source");
+    return SP_OK;
+}
+
+int sp_ac_frequencies(const sp_ac_config* cfg, double* freqs, int cap) {
+    if (!cfg) return SP_ERR_INVALID_ARGUMENT;
+    const std::vector<double> f = ac_grid(cfg);
+    for (int i = 0; i < (int)f.size() && i < cap && freqs; ++i) freqs[i] = f[i];
+    return (int)f.size();
+}
+
+static int ac_locked(sp_ctx* ctx, sp_topology* t, const sp_newton_config* dc_cfg, const sp_ac_config* ac, uint64_t seed,
+                     uint64_t first, uint64_t count, const double* d_table, uint32_t cols, double* d_probe,
+                     uint8_t* d_status, cudaStream_t st) {
+    const std::vector<double> freqs = ac_grid(ac);
+    const int nf = (int)freqs.size();
+    if (nf < 1) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "empty frequency grid");
+    const int n = t->n, np = std::max(t->num_params, 1);
+    const size_t per = (size_t)16 * ((size_t)n * n + n);  // complex matrix + rhs per thread
+    int block = 128;
+    while (block > 32 && per * block > 110 * 1024) block >>= 1;
+    const bool shared = per * block <= 110 * 1024;
+    const uint64_t units = count * (uint64_t)nf;
+    int grid = (int)std::min<uint64_t>((units + block - 1) / block,
+                                       (uint64_t)ctx->num_sms * (shared ? std::max<size_t>(1, (200 * 1024) / (per * block)) : 2));
+    grid = std::max(grid, 1);
+    const size_t bx = align256(8 * (size_t)n * count), bp = align256(8 * (size_t)np * count),
+                 bf = align256(8 * (size_t)nf), bs = align256(4 * count),
+                 bw = shared ? 0 : align256(per * (size_t)grid * block);
+    int rc = ensure_aux(ctx, bx + bp + bf + bs + bw);
+    if (rc) return rc;
+    char* base = (char*)ctx->aux;
+    double* x_dc = (double*)base;
+    double* params = (double*)(base + bx);
+    double* d_freqs = (double*)(base + bx + bp);
+    unsigned int* singular = (unsigned int*)(base + bx + bp + bf);
+    double* work = shared ? nullptr : (double*)(base + bx + bp + bf + bs);
+    SP_CUDA(ctx, cudaMemcpyAsync(d_freqs, freqs.data(), 8 * (size_t)nf, cudaMemcpyHostToDevice, st), "H2D freqs");
+    SP_CUDA(ctx, cudaMemsetAsync(singular, 0, 4 * count, st), "clear flags");
+    rc = newton_dc_locked(ctx, t, dc_cfg, seed, first, count, d_table, cols, nullptr, x_dc, nullptr, d_status,
+                          nullptr, params, nullptr, st);
+    if (rc) return rc;
+    AcLaunch L{};
+    L.c = t->dc;
+    L.params = params;
+    L.np = t->num_params;
+    L.x_dc = x_dc;
+    L.dc_status = d_status;
+    L.count = count;
+    L.freqs = d_freqs;
+    L.nf = nf;
+    L.source = ac->source;
+    L.num_probe = ac->num_probe;
+    for (int k = 0; k < 8; ++k) L.probe[k] = k < ac->num_probe ? ac->probe[k] : 0;
+    L.out = d_probe;
+    L.singular = singular;
+    L.work = work;
+    ProfScope prof(ctx, "ac_sweep", st);
+    SP_CUDA(ctx, launch_ac(L, grid, block, shared ? per * block : 0, st), "AC launch");
+    return SP_OK;
+}
+
+int sp_ac_sweep_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_config* dc_cfg, const sp_ac_config* ac,
+                       uint64_t seed, uint64_t first_index, uint64_t count, const double* d_table,
+                       uint32_t table_cols, double* d_probe, uint8_t* d_status, void* stream) {
+    if (!ctx || !topo || !dc_cfg || !d_probe || !d_status) return SP_ERR_INVALID_ARGUMENT;
+    if (topo->ctx != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "topology belongs to another context");
+    int rc = ac_validate(ctx, ac, topo->n, topo->num_elements);
+    if (rc) return rc;
+    if (count == 0) return SP_OK;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    return ac_locked(ctx, const_cast<sp_topology*>(topo), dc_cfg, ac, seed, first_index, count, d_table, table_cols,
+                     d_probe, d_status, (cudaStream_t)stream);
+}
+
+int sp_ac_sweep(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* dc_cfg, const sp_ac_config* ac,
+                uint64_t seed, uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
+                double* probe, uint8_t* status) {
+    if (!ctx || !circuit || !dc_cfg || !probe || !status) return SP_ERR_INVALID_ARGUMENT;
+    int rc = ac_validate(ctx, ac, circuit->num_nodes + circuit->num_branches, circuit->num_elements);
+    if (rc) return rc;
+    if (count == 0) return SP_OK;
+    sp_topology* t = nullptr;
+    rc = sp_topology_create(ctx, circuit, &t);
+    if (rc) return rc;
+    const size_t nf = ac_grid(ac).size();
+    const size_t pbytes = 16 * nf * (size_t)ac->num_probe * count;
+    double *dp = nullptr, *dt = nullptr;
+    uint8_t* ds = nullptr;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMalloc(&dp, pbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&ds, count);
+    if (e == cudaSuccess && table) e = cudaMalloc(&dt, 8 * (size_t)table_cols * count);
+    if (e == cudaSuccess && table) e = cudaMemcpy(dt, table, 8 * (size_t)table_cols * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        ScratchOrder order(ctx, ctx->stream);
+        rc = ac_locked(ctx, t, dc_cfg, ac, seed, first_index, count, dt, table_cols, dp, ds, ctx->stream);
+        if (rc == SP_OK) {
+            e = cudaMemcpyAsync(probe, dp, pbytes, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(status, ds, count, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        }
+    }
+    for (void* p : {(void*)dp, (void*)dt, (void*)ds})
+        if (p) cudaFree(p);
+    sp_topology_destroy(t);
+    if (rc) return rc;
+    return e == cudaSuccess ? SP_OK : cuda_fail(ctx, e, "AC copies");
 }
 
 }  // extern "C"

@@ -55,6 +55,8 @@ cudaError_t launch_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t pa
 cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, uint64_t batch,
                                   double* sol, uint8_t* sing, cudaStream_t st);
 cudaError_t prepare_exact_kernels(int max_smem);
+struct AcLaunch;
+cudaError_t launch_ac(const AcLaunch& L, int grid, int block, size_t smem, cudaStream_t st);
 // solve_batch for n > kMaxDenseN: one CTA per system (shared memory when
 // lu_batch_cta_smem(n) fits, else work = grid slices of n*n + n doubles)
 constexpr int kMaxBatchLuN = 4096;
@@ -69,7 +71,7 @@ cudaError_t launch_lu_batch_mixed(const double* mats, const double* rhs, int n, 
                                   double* sol, uint8_t* sing, int refine_steps, cudaStream_t st);
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
-                           unsigned int* ticket, cudaStream_t st);  // ticket: a zeroed counter
+                           cudaStream_t st);
 cudaError_t prepare_fast_kernels(int max_smem);
 
 // Largest dense size of the thread-per-sample Newton kernels.

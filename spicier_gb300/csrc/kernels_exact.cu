@@ -7,6 +7,8 @@
 #include "rng.cuh"
 #include "ladder.cuh"
 #include "transient_fixed.cuh"
+#define SP_AC_KERNELS
+#include "ac.cuh"
 
 namespace sp {
 
@@ -252,6 +254,15 @@ cudaError_t launch_lu_batch_cta(const double* mats, const double* rhs, int n, ui
     return cudaGetLastError();
 }
 
+cudaError_t launch_ac(const AcLaunch& L, int grid, int block, size_t smem, cudaStream_t st) {
+    ac_kernel<<<grid, block, smem, st>>>(L);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    ac_status_kernel<<<(unsigned)((L.count + 255) / 256), 256, 0, st>>>(L.count, L.dc_status, L.singular,
+                                                                       const_cast<uint8_t*>(L.dc_status));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ladder_exact(const LadderLaunch& L, int grid, size_t smem, cudaStream_t st) {
     SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT><<<grid, 128, smem, st>>>(L);
     return cudaGetLastError();
@@ -275,6 +286,8 @@ cudaError_t prepare_exact_kernels(int max_smem) {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(ac_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(lu_batch_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - 1024);
     if (e != cudaSuccess) return e;

@@ -227,11 +227,12 @@ __global__ void moments_final_kernel(const sp_moments* __restrict__ partial, uin
 // ... of the block's chunk, so a warp reads whole rows (coalesced); the
 // groups of a column are then merged in a fixed order, and the chunks'
 // partials by the tree kernel.  The chunk length is a function of rows alone
-// (about two chunks per SM), so the result depends only on rows and cols.
+// (about eight chunks per SM, one batch of loads per thread), so the result
+// depends only on rows and cols.
 constexpr int kMomChunkMin = 64;
 
 __host__ __device__ inline uint64_t moments_chunk(uint64_t rows, uint32_t max_blocks) {
-    const uint64_t target = max_blocks < 304 ? max_blocks : 304;
+    const uint64_t target = max_blocks < 1216 ? max_blocks : 1216;  // about eight blocks per SM
     uint64_t chunk = (rows + target - 1) / target;
     chunk = (chunk + kMomChunkMin - 1) / kMomChunkMin * kMomChunkMin;
     return chunk < kMomChunkMin ? kMomChunkMin : chunk;
@@ -250,8 +251,7 @@ __device__ __forceinline__ double from_key(long long k) {
 __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
                                                            uint32_t cols, uint32_t cp, uint64_t chunk,
                                                            const uint8_t* __restrict__ status,
-                                                           sp_moments* __restrict__ partial, unsigned int* ticket,
-                                                           sp_moments* __restrict__ out) {
+                                                           sp_moments* __restrict__ partial) {
     __shared__ sp_moments sh[256];
     const uint32_t c = threadIdx.x % cp, g = threadIdx.x / cp, groups = 256 / cp;
     const uint64_t lo = (uint64_t)blockIdx.x * chunk, hi = min(rows, lo + chunk);
@@ -291,40 +291,6 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
         __syncthreads();
     }
     if (threadIdx.x < cols) partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
-    // the last block to finish merges the partials: thread t works on column
-    // t % cp, merging partials t / cp, t / cp + groups, ... in order, then a
-    // pairwise tree over the groups (a fixed order for given rows and cols)
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    sp_moments f{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
-    if (c < cols) {
-        // four partials in flight per thread, merged in order
-        const sp_moments* pc = partial + (size_t)c * gridDim.x;
-        for (uint32_t b0 = g; b0 < gridDim.x; b0 += 4 * groups) {
-            sp_moments q[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint32_t b = b0 + (uint32_t)u * groups;
-                q[u] = b < gridDim.x ? pc[b] : sp_moments{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (b0 + (uint32_t)u * groups < gridDim.x) mom_merge(f, q[u]);
-        }
-    }
-    sh[threadIdx.x] = f;
-    __syncthreads();
-    for (uint32_t w = groups / 2; w >= 1; w >>= 1) {
-        if (g < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w * cp]);
-        __syncthreads();
-    }
-    if (threadIdx.x < cols) out[threadIdx.x] = sh[threadIdx.x];
-    if (threadIdx.x == 0) *ticket = 0;  // ready for the next launch on this buffer
 }
 
 // One block per column: each thread merges partials t, t + 256, ... in order,
@@ -334,7 +300,17 @@ __global__ void __launch_bounds__(256) moments_tree_kernel(const sp_moments* __r
     __shared__ sp_moments sh[256];
     const uint32_t col = blockIdx.x;
     sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
-    for (uint32_t b = threadIdx.x; b < nblocks; b += 256) mom_merge(m, partial[(size_t)col * nblocks + b]);
+    for (uint32_t b0 = threadIdx.x; b0 < nblocks; b0 += 4 * 256) {  // four partials in flight, merged in order
+        sp_moments q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t b = b0 + (uint32_t)u * 256;
+            q[u] = b < nblocks ? partial[(size_t)col * nblocks + b] : sp_moments{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (b0 + (uint32_t)u * 256 < nblocks) mom_merge(m, q[u]);
+    }
     sh[threadIdx.x] = m;
     __syncthreads();
     for (int w = 128; w >= 1; w >>= 1) {
@@ -346,7 +322,7 @@ __global__ void __launch_bounds__(256) moments_tree_kernel(const sp_moments* __r
 
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
-                           unsigned int* ticket, cudaStream_t st) {
+                           cudaStream_t st) {
     if (cols == 0) return cudaSuccess;
     if (rows == 0) {  // empty accumulators (count 0, min +inf, max -inf)
         moments_tree_kernel<<<cols, 256, 0, st>>>(partial, 0, out);
@@ -357,7 +333,10 @@ cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uin
         uint32_t cp = 1;
         while (cp < cols) cp <<= 1;
         const uint32_t nb = (uint32_t)((rows + chunk - 1) / chunk);
-        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, chunk, status, partial, ticket, out);
+        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, chunk, status, partial);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        moments_tree_kernel<<<cols, 256, 0, st>>>(partial, nb, out);
         return cudaGetLastError();
     }
     nblocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(nblocks, 256), std::max<uint64_t>(1, rows / 1024));
