@@ -195,21 +195,36 @@ __global__ void splitk_reduce(const float* __restrict__ part, int splits, int co
     out[i] = s;
 }
 
-// Bias gradient: db[n] = sum over rows of dZ[row][n] (rows in a fixed order).
-__global__ void bias_grad(const bf16* __restrict__ d, int rows, int cols, int ld, float* __restrict__ db) {
+// Bias gradient: db[n] = sum over rows of dZ[row][n], in a fixed order: block
+// (x, y) sums rows [y chunk, (y + 1) chunk) of columns 32x.. into part[y][n]
+// (eight row lanes, then the lanes in order); bias_grad_final adds the
+// chunks in order.  kBiasChunks chunks keep the whole GPU busy.
+constexpr int kBiasChunks = 64;
+
+__global__ void bias_grad(const bf16* __restrict__ d, int rows, int cols, int ld, float* __restrict__ part) {
     __shared__ float sh[8][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int col = blockIdx.x * 32 + tx;
+    const int chunk = (rows + gridDim.y - 1) / gridDim.y;
+    const int r0 = blockIdx.y * chunk, r1 = min(rows, r0 + chunk);
     float s = 0.f;
     if (col < cols)
-        for (int r = ty; r < rows; r += 8) s += __bfloat162float(d[(size_t)r * ld + col]);
+        for (int r = r0 + ty; r < r1; r += 8) s += __bfloat162float(d[(size_t)r * ld + col]);
     sh[ty][tx] = s;
     __syncthreads();
     if (ty == 0 && col < cols) {
         float t = 0.f;
         for (int k = 0; k < 8; ++k) t += sh[k][tx];
-        db[col] = t;
+        part[(size_t)blockIdx.y * cols + col] = t;
     }
+}
+
+__global__ void bias_grad_final(const float* __restrict__ part, int chunks, int cols, float* __restrict__ db) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= cols) return;
+    float t = 0.f;
+    for (int y = 0; y < chunks; ++y) t += part[(size_t)y * cols + col];
+    db[col] = t;
 }
 
 // Mean-squared-error gradient of the output layer (first n_real columns),
@@ -678,8 +693,14 @@ cudaError_t backward(sp_mlp* m, int rows_pad, const float* targets, int ldt_in, 
         const int cnt = width * in_w;
         splitk_reduce<<<(cnt + 255) / 256, 256, 0, st>>>(m->part, splits, cnt, m->grads + m->woff[l]);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        bias_grad<<<(width + 31) / 32, 256, 0, st>>>(dcur, rows_pad, width, width, m->grads + m->boff[l]);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        {
+            const int chunks = (int)std::max<size_t>(
+                1, std::min<size_t>({(size_t)kBiasChunks, (size_t)rows_pad / 64, m->part_elems / (size_t)width}));
+            bias_grad<<<dim3((width + 31) / 32, chunks), 256, 0, st>>>(dcur, rows_pad, width, width, m->part);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            bias_grad_final<<<(width + 127) / 128, 128, 0, st>>>(m->part, chunks, width, m->grads + m->boff[l]);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
         if (l == 0) break;
         // input gradient through the GELU: dZ_{l-1} = (dZ_l * W_l) .* gelu'(Z_{l-1})
         bf16* dn = toggle ? m->dB : m->dA;
