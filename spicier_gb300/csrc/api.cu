@@ -612,7 +612,9 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (e != cudaSuccess) return cuda_fail(ctx, e, "newton launch");
     const bool any_fallback = d_x0 || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE));
     if (any_fallback) {
-        int fgrid = std::min(grid, std::max(1, ctx->num_sms * 2));
+        // one wave of blocks: the miss list is usually empty or short, and a
+        // second wave of large-shared-memory blocks costs a few microseconds
+        int fgrid = std::min(grid, std::max(1, ctx->num_sms));
         ProfScope prof(ctx, fname[prec], st);
         e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, true, fgrid, block, smem, st)
                                        : launch_newton_fast(kprec, L, true, fgrid, block, smem, st);

@@ -178,12 +178,19 @@ cudaError_t launch_lu_batch_mixed(const double* mats, const double* rhs, int n, 
 // statistics.rs:127-155).  Pass 1: each block reduces a contiguous row range
 // per column in a fixed tree order; pass 2: one block merges the partials in
 // block order.  The order is fixed, so reruns are bit-identical.
+// min / max by the order-preserving integer keys of the doubles (integer pipe;
+// no NaN reaches the accumulators)
+__device__ __forceinline__ long long mom_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (long long)(0x8000000000000000ULL - (unsigned long long)b) - 1;
+}
+
 __device__ inline void mom_merge(sp_moments& a, const sp_moments& b) {
     a.count += b.count;
     a.sum += b.sum;
     a.sum_sq += b.sum_sq;
-    a.min = fmin(a.min, b.min);
-    a.max = fmax(a.max, b.max);
+    a.min = mom_key(b.min) < mom_key(a.min) ? b.min : a.min;
+    a.max = mom_key(b.max) > mom_key(a.max) ? b.max : a.max;
 }
 
 __global__ void moments_partial_kernel(const double* __restrict__ v, uint64_t rows, uint32_t ld,
