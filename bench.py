@@ -219,6 +219,7 @@ def main():
     ap.add_argument("--no-config4", action="store_true")
     ap.add_argument("--no-transient", action="store_true", help="skip the ladder-transient (workload 3) report")
     ap.add_argument("--no-grid", action="store_true", help="skip the power-grid (workload 5) report")
+    ap.add_argument("--no-ac", action="store_true", help="skip the AC small-signal sweep report")
     ap.add_argument("--train-samples", type=int, default=1 << 20)
     ap.add_argument("--no-ablations", action="store_true", help="skip the mixed-from-nodeset and FP64-specialised arms")
     ap.add_argument("--mlp-hidden", type=int, default=128, help="hidden width of the warm-start network")
@@ -465,6 +466,24 @@ def main():
                                  "sample": f"{sample3} ladders (instances 0..{sample3 - 1}), FP64, all host threads"}
         config3["speedup_mixed_vs_plain_fp64"] = config3["mixed"]["transients_per_s"] / config3["plain_fp64"]["transients_per_s"]
 
+    # AC small-signal sweep of the op-amp Monte Carlo (the next row after the DC sweep)
+    ac_report = None
+    if not args.no_ac and rank == 0:
+        from spicier_gb300.api import Context as _Ctx
+        acfg = {}
+        for name, prec in (("mixed", abi.SP_PREC_MIXED), ("fp64", abi.SP_PREC_FP64)):
+            cfg_ac = abi.ac_config(10.0, 1e9, 10, abi.SP_AC_DEC, [circ.node("out")], precision=prec)
+            nf = len(_Ctx.ac_frequencies(cfg_ac))
+            pd = torch.empty((N, nf, 1, 2), dtype=torch.float64, device=dev)
+            sd = torch.empty(N, dtype=torch.uint8, device=dev)
+            run_ac = lambda: ctx.ac_sweep_device(topo, cfg_mixed, cfg_ac, SEED, N, pd, sd, stream=stream)
+            run_ac()
+            ms = min(event_ms(run_ac) for _ in range(3))
+            ok = float(((sd & 0x0F) == 0).float().mean().item())
+            acfg[name] = {"ms": ms, "complex_solves_per_s": N * nf / (ms * 1e-3), "converged_fraction": ok}
+        ac_report = {"samples": N, "frequencies": nf, "sweep": "10 Hz .. 1 GHz, 10 per decade",
+                     "probe": "out", "dc": "mixed + nodeset, inside the timed call", **acfg}
+
     # workload 5: 256 power-grid corners (Newton + GMRES(30) + Jacobi)
     config5 = None
     if not args.no_grid and rank == 0:
@@ -570,6 +589,7 @@ def main():
             "config4": config4,
             "config3_ladder_transient": config3,
             "config5_power_grid": config5,
+            "ac_sweep": ac_report,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -517,6 +517,9 @@ typedef struct sp_ac_config {
                          /* default); else the element index of the stimulus */
     int32_t num_probe;   /* 1..8 unknowns recorded                             */
     int32_t probe[8];
+    int32_t precision;   /* SP_PREC_FP64: the reference's FP64 LU order;       */
+                         /* SP_PREC_MIXED: FP32 complex LU + FP64 refinement  */
+    int32_t refine;      /* mixed: residual refinement steps (0 -> 3)          */
 } sp_ac_config;
 
 /* The frequency grid (generate_frequencies, ac.rs:258-287): writes up to cap

@@ -188,16 +188,19 @@ SP_AC_LIN, SP_AC_DEC, SP_AC_OCT = 0, 1, 2
 
 class SpAcConfig(C.Structure):
     _fields_ = [("fstart", C.c_double), ("fstop", C.c_double), ("num_points", C.c_int32), ("sweep", C.c_int32),
-                ("source", C.c_int32), ("num_probe", C.c_int32), ("probe", C.c_int32 * 8)]
+                ("source", C.c_int32), ("num_probe", C.c_int32), ("probe", C.c_int32 * 8), ("precision", C.c_int32),
+                ("refine", C.c_int32)]
 
 
 def ac_config(fstart: float, fstop: float, num_points: int, sweep: int = SP_AC_DEC, probes=(0,),
-              source: int = -1) -> SpAcConfig:
+              source: int = -1, precision: int = SP_PREC_FP64, refine: int = 0) -> SpAcConfig:
     """AC sweep settings (AcParams, ac.rs:30-40): frequency range and points (total for SP_AC_LIN, per decade or
-    octave otherwise), the recorded unknowns (1..8) and the stimulus (-1: every V source at AC magnitude 1, as
-    the reference's ac_info default; else the element index of the one source)."""
+    octave otherwise), the recorded unknowns (1..8), the stimulus (-1: every V source at AC magnitude 1, as
+    the reference's ac_info default; else the element index of the one source), and the precision
+    (SP_PREC_FP64: the reference's LU order; SP_PREC_MIXED: FP32 LU with `refine` FP64 refinement steps)."""
     c = SpAcConfig()
     c.fstart, c.fstop, c.num_points, c.sweep, c.source = fstart, fstop, num_points, sweep, source
+    c.precision, c.refine = precision, refine
     c.num_probe = len(probes)
     for k, p in enumerate(probes):
         c.probe[k] = p

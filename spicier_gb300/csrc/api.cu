@@ -1250,6 +1250,9 @@ static int ac_validate(sp_ctx* ctx, const sp_ac_config* c, int n, int num_elemen
     for (int k = 0; k < c->num_probe; ++k)
         if (c->probe[k] < 0 || c->probe[k] >= n) return fail(ctx, SP_ERR_INVALID_DIMENSION, "probe %d out of range", k);
     if (c->source < -1 || c->source >= num_elements) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad AC source");
+    if (c->precision != SP_PREC_FP64 && c->precision != SP_PREC_MIXED)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "AC precision must be SP_PREC_FP64 or SP_PREC_MIXED");
+    if (c->refine < 0 || c->refine > 8) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "refine must be 0..8");
     return SP_OK;
 }
 
@@ -1267,13 +1270,14 @@ static int ac_locked(sp_ctx* ctx, sp_topology* t, const sp_newton_config* dc_cfg
     const int nf = (int)freqs.size();
     if (nf < 1) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "empty frequency grid");
     const int n = t->n, np = std::max(t->num_params, 1);
-    const size_t per = (size_t)16 * ((size_t)n * n + n);  // complex matrix + rhs per thread
+    const bool mixed = ac->precision == SP_PREC_MIXED;
+    const size_t per = ac_work_bytes(n, mixed);  // per-thread work area
     int block = 128;
     while (block > 32 && per * block > 110 * 1024) block >>= 1;
     const bool shared = per * block <= 110 * 1024;
     const uint64_t units = count * (uint64_t)nf;
     int grid = (int)std::min<uint64_t>((units + block - 1) / block,
-                                       (uint64_t)ctx->num_sms * (shared ? std::max<size_t>(1, (200 * 1024) / (per * block)) : 2));
+                                       (uint64_t)ctx->num_sms * (shared ? std::max<size_t>(1, (220 * 1024) / (per * block)) : 2));
     grid = std::max(grid, 1);
     const size_t bx = align256(8 * (size_t)n * count), bp = align256(8 * (size_t)np * count),
                  bf = align256(8 * (size_t)nf), bs = align256(4 * count),
@@ -1306,8 +1310,10 @@ static int ac_locked(sp_ctx* ctx, sp_topology* t, const sp_newton_config* dc_cfg
     L.out = d_probe;
     L.singular = singular;
     L.work = work;
-    ProfScope prof(ctx, "ac_sweep", st);
-    SP_CUDA(ctx, launch_ac(L, grid, block, shared ? per * block : 0, st), "AC launch");
+    L.refine = ac->refine > 0 ? ac->refine : 3;
+    ProfScope prof(ctx, mixed ? "ac_sweep_mixed" : "ac_sweep_fp64", st);
+    if (mixed) SP_CUDA(ctx, launch_ac_mixed(L, grid, block, shared ? per * block : 0, st), "AC launch");
+    else SP_CUDA(ctx, launch_ac(L, grid, block, shared ? per * block : 0, st), "AC launch");
     return SP_OK;
 }
 

@@ -57,6 +57,7 @@ cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, 
 cudaError_t prepare_exact_kernels(int max_smem);
 struct AcLaunch;
 cudaError_t launch_ac(const AcLaunch& L, int grid, int block, size_t smem, cudaStream_t st);
+cudaError_t launch_ac_mixed(const AcLaunch& L, int grid, int block, size_t smem, cudaStream_t st);
 // solve_batch for n > kMaxDenseN: one CTA per system (shared memory when
 // lu_batch_cta_smem(n) fits, else work = grid slices of n*n + n doubles)
 constexpr int kMaxBatchLuN = 4096;

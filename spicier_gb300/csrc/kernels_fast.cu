@@ -7,6 +7,8 @@
 
 #define SP_KERNEL_NS kfast
 #include "internal.h"
+#define SP_AC_MIXED_KERNELS
+#include "ac.cuh"
 #include "ladder.cuh"
 #include "transient_fixed.cuh"
 #include "powergrid.cuh"
@@ -327,6 +329,21 @@ __global__ void __launch_bounds__(256) moments_tree_kernel(const sp_moments* __r
     if (threadIdx.x == 0) out[col] = sh[0];
 }
 
+__global__ void ac_status_kernel_fast(uint64_t count, const unsigned int* singular, uint8_t* status) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= count || !singular[s]) return;
+    status[s] = (uint8_t)((status[s] & ~SP_ST_MASK) | SP_ST_SINGULAR);
+}
+
+cudaError_t launch_ac_mixed(const AcLaunch& L, int grid, int block, size_t smem, cudaStream_t st) {
+    ac_mixed_kernel<<<grid, block, smem, st>>>(L);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    ac_status_kernel_fast<<<(unsigned)((L.count + 255) / 256), 256, 0, st>>>(L.count, L.singular,
+                                                                            const_cast<uint8_t*>(L.dc_status));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
                            cudaStream_t st) {
@@ -482,7 +499,7 @@ cudaError_t launch_transient_fast(const TransientLaunch& L, int block, size_t sm
 cudaError_t prepare_fast_kernels(int max_smem) {
     const void* fns[] = {
         (const void*)SP_KERNEL_NS::grid_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::grid_kernel<SP_PREC_FP64>,
-        (const void*)SP_KERNEL_NS::transient_fixed_kernel,
+        (const void*)SP_KERNEL_NS::transient_fixed_kernel, (const void*)ac_mixed_kernel,
         (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_MIXED>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_MIXED>,
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,

@@ -151,3 +151,26 @@ def test_ac_errors(ctx):
         ctx.ac_sweep(circ, abi.newton_config(), abi.ac_config(1.0, 10.0, 5, probes=(7,)), 1, 4)
     with pytest.raises(sg.SpicierError):
         ctx.ac_sweep(circ, abi.newton_config(), abi.ac_config(0.0, 10.0, 5), 1, 4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["opamp", "bjt"])
+def test_mixed_precision_against_fp64_oracle(ctx, name):
+    """FP32 complex LU with FP64 residual refinement: within 1e-9 of the FP64 oracle."""
+    if name == "opamp":
+        circ = configs.miller_opamp()
+        probes = [circ.node("out"), circ.node("n2"), circ.n - 1]
+    else:
+        circ = configs.bjt_diode_bias()
+        circ.Cap("CB", "b", "0", 1e-9)
+        circ.L("LC", "c", "c2", 1e-6)
+        circ.R("RC2", "c2", "0", 1e5)
+        probes = [circ.node("c"), circ.node("c2"), circ.n - 1]
+    cfg = abi.ac_config(1e1, 1e10, 10, abi.SP_AC_DEC, probes, precision=abi.SP_PREC_MIXED)
+    dc = abi.newton_config(precision=abi.SP_PREC_FP64)
+    h, st = ctx.ac_sweep(circ, dc, cfg, 3, 1024)
+    ho, so = oracle.ac_sweep(circ, dc, 3, 1024, Context.ac_frequencies(cfg), probes)
+    ok = (so & 0x0F) == 0
+    assert np.array_equal(st, so) and ok.mean() > 0.95
+    scale = np.abs(ho[ok]).max(axis=1, keepdims=True)
+    assert (np.abs(h[ok] - ho[ok]) <= 1e-9 * scale + 1e-18).all()
