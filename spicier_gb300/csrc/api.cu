@@ -132,6 +132,8 @@ int sp_ctx_destroy(sp_ctx* ctx) {
         cudaEventDestroy(r.b);
     }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    for (auto& kv : ctx->host_topos) sp_topology_destroy(kv.second);
+    ctx->host_topos.clear();
     spec_release_all(ctx);
     delete ctx;
     return SP_OK;
@@ -655,6 +657,41 @@ int sp_newton_dc_learned_device(sp_ctx* ctx, const sp_topology* topo, sp_mlp* ml
                             d_iters, d_status, d_resid, nullptr, d_moments, (cudaStream_t)stream, mlp);
 }
 
+// The topology of `c` for a host-buffer call: created on first use and kept
+// by the context (at most 16 circuits; the 17th clears the cache).
+static int host_topology(sp_ctx* ctx, const sp_circuit* c, sp_topology** out) {
+    std::string key;
+    auto put = [&](const void* p, size_t n) { key.append((const char*)p, n); };
+    put(&c->num_nodes, sizeof(int));
+    put(&c->num_branches, sizeof(int));
+    put(&c->num_elements, sizeof(int));
+    put(&c->num_params, sizeof(int));
+    put(&c->num_pulses, sizeof(int));
+    if (c->num_elements > 0 && c->elements) put(c->elements, sizeof(sp_element) * c->num_elements);
+    if (c->num_params > 0 && c->params) put(c->params, sizeof(sp_param) * c->num_params);
+    if (c->num_pulses > 0 && c->pulses) put(c->pulses, sizeof(sp_pulse) * c->num_pulses);
+    const char has_ns = c->nodeset ? 1 : 0;
+    put(&has_ns, 1);
+    if (c->nodeset && c->num_nodes + c->num_branches > 0)
+        put(c->nodeset, sizeof(double) * (size_t)(c->num_nodes + c->num_branches));
+    std::lock_guard<std::mutex> g(ctx->topo_mu);
+    auto it = ctx->host_topos.find(key);
+    if (it != ctx->host_topos.end()) {
+        *out = it->second;
+        return SP_OK;
+    }
+    if (ctx->host_topos.size() >= 16) {
+        for (auto& kv : ctx->host_topos) sp_topology_destroy(kv.second);
+        ctx->host_topos.clear();
+    }
+    sp_topology* t = nullptr;
+    int rc = sp_topology_create(ctx, c, &t);
+    if (rc) return rc;
+    ctx->host_topos[key] = t;
+    *out = t;
+    return SP_OK;
+}
+
 static int newton_dc_host(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* cfg, uint64_t seed,
                           uint64_t first_index, uint64_t count, const double* table, uint32_t table_cols,
                           const double* x0, double* x, int32_t* iters, uint8_t* status, double* resid,
@@ -663,12 +700,8 @@ static int newton_dc_host(sp_ctx* ctx, const sp_circuit* circuit, const sp_newto
     if (count == 0) return SP_OK;
     if (!x) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null output x");
     sp_topology* t = nullptr;
-    int rc = sp_topology_create(ctx, circuit, &t);
+    int rc = host_topology(ctx, circuit, &t);
     if (rc) return rc;
-    struct Guard {
-        sp_topology* t;
-        ~Guard() { sp_topology_destroy(t); }
-    } guard{t};
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaSetDevice(ctx->device);
     const int n = t->n;
@@ -1186,7 +1219,7 @@ int sp_transient(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
     if (tc->probe >= 0 && !probe) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "probe requested without a buffer");
     if (count == 0) return SP_OK;
     sp_topology* t = nullptr;
-    rc = sp_topology_create(ctx, circuit, &t);
+    rc = host_topology(ctx, circuit, &t);
     if (rc) return rc;
     int nv = 0;
     for (int e = 0; e < circuit->num_elements; ++e) nv += circuit->elements[e].kind == SP_EL_V;
@@ -1214,7 +1247,6 @@ int sp_transient(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config*
     }
     for (void* p : {(void*)dx, (void*)dp, (void*)dt, (void*)ds})
         if (p) cudaFree(p);
-    sp_topology_destroy(t);
     if (rc) return rc;
     return e == cudaSuccess ? SP_OK : cuda_fail(ctx, e, "transient copies");
 }
@@ -1340,7 +1372,7 @@ int sp_ac_sweep(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* 
     if (rc) return rc;
     if (count == 0) return SP_OK;
     sp_topology* t = nullptr;
-    rc = sp_topology_create(ctx, circuit, &t);
+    rc = host_topology(ctx, circuit, &t);
     if (rc) return rc;
     const size_t nf = ac_grid(ac).size();
     const size_t pbytes = 16 * nf * (size_t)ac->num_probe * count;
@@ -1363,7 +1395,6 @@ int sp_ac_sweep(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* 
     }
     for (void* p : {(void*)dp, (void*)dt, (void*)ds})
         if (p) cudaFree(p);
-    sp_topology_destroy(t);
     if (rc) return rc;
     return e == cudaSuccess ? SP_OK : cuda_fail(ctx, e, "AC copies");
 }

@@ -120,6 +120,10 @@ struct sp_ctx {
         int blocks_per_sm = 1;  // resident 128-thread blocks (the persistent grid)
     };
     std::map<std::string, Spec> spec_cache;
+    // topologies of the host-buffer entry points, keyed by the circuit's bytes,
+    // so repeated calls on one circuit upload and specialise it once
+    std::mutex topo_mu;
+    std::map<std::string, sp_topology*> host_topos;
     // second grow-only buffer for entry points that run the Newton path (which
     // owns `scratch`) and keep their own data across it
     void* aux = nullptr;
