@@ -23,6 +23,7 @@
 #pragma once
 #include "internal.h"
 #include "rng.cuh"
+#include "fpconv.cuh"
 
 namespace sp {
 
@@ -75,6 +76,11 @@ namespace SP_KERNEL_NS {
 // (an affine recurrence over the blocks), and every lane then recovers its
 // rows.  On exit D[i] = x_i.  L, R: scratch rows; fl: 2 x 32 scratch values.
 template <class T>
+__device__ __forceinline__ T from_f64(double v) { return v; }
+template <>
+__device__ __forceinline__ float from_f64<float>(double v) { return f64_to_f32_int(v); }
+
+template <class T>
 __device__ inline void warp_partition_solve(int N, int lane, const double* g, T* B, T* D, T* L, T* R, T* fl) {
     const int P = N / 2 < 32 ? N / 2 : 32;
     int lo = 0, hi = 0;
@@ -82,18 +88,18 @@ __device__ inline void warp_partition_solve(int N, int lane, const double* g, T*
         lo = 1 + (int)(((long long)lane * N) / P);
         hi = 1 + (int)(((long long)(lane + 1) * N) / P);
         // downward: move the sub-diagonal into the left spike L
-        L[lo] = lo > 1 ? -(T)g[lo] : (T)0;
+        L[lo] = lo > 1 ? -from_f64<T>(g[lo]) : (T)0;
         for (int i = lo + 1; i < hi; ++i) {
-            const T a = -(T)g[i], cprev = -(T)g[i];  // c_{i-1} = -g_i = a_i
+            const T a = -from_f64<T>(g[i]), cprev = -from_f64<T>(g[i]);  // c_{i-1} = -g_i = a_i
             const T f = a / B[i - 1];
             L[i] = -f * L[i - 1];
             B[i] = B[i] - f * cprev;
             D[i] = D[i] - f * D[i - 1];
         }
         // upward: move the super-diagonal into the right spike R
-        R[hi - 1] = hi - 1 < N ? -(T)g[hi] : (T)0;
+        R[hi - 1] = hi - 1 < N ? -from_f64<T>(g[hi]) : (T)0;
         for (int i = hi - 2; i >= lo; --i) {
-            const T cc = -(T)g[i + 1];
+            const T cc = -from_f64<T>(g[i + 1]);
             const T f = cc / B[i + 1];
             L[i] = L[i] - f * L[i + 1];
             R[i] = -f * R[i + 1];
@@ -224,29 +230,39 @@ struct LadderWarp {
             float* jr = reinterpret_cast<float*>(srhs);
             float* jc = reinterpret_cast<float*>(scp);
             float* jp = reinterpret_cast<float*>(sdp);
+            // exp(a) = expf(ah) (1 + al), a = ah + al split at FP32 (relative error
+            // ~1e-7, far inside the stage tolerances), conductance and Jacobian in
+            // FP32, conversions on the integer pipe: the FP64 pipe keeps only the
+            // residual (what the refinement needs) and the update
+            const float inv_nvt_f = f64_to_f32_int(inv_nvt), is_f = f64_to_f32_int(c.diode_is);
             for (int k = 1 + lane; k <= N; k += 32) {
                 const double xk = xs[k];
                 const double vl1 = limit(xk);
                 const double vl2 = limit(vl1);
-                const double e = dexp(vl2);
+                const double a = vl2 * inv_nvt;
+                const float ah = f64_to_f32_int(a);
+                const float ef = expf(ah);
+                const double e = f32_to_f64_int(ef) * (1.0 + (a - f32_to_f64_int(ah)));
                 const double id = c.diode_is * (e - 1.0);
-                const double gd = fmax(c.diode_is * e * inv_nvt, 1e-12);
+                const float gdf = fmaxf(is_f * ef * inv_nvt_f, 1e-12f);
                 const double xl = k == 1 ? V : xs[k - 1];
                 const double xr = k < N ? xs[k + 1] : 0.0;
                 const double gk1 = k < N ? g[k + 1] : 0.0;
                 // KCL: currents leaving node k (R left, R right, C companion, diode linearised at vl1)
-                const double F = g[k] * (xk - xl) + gk1 * (xk - xr) + (geq[k] * xk - ieq[k]) + (id + gd * (xk - vl1));
-                jd[k] = (float)(((g[k] + gk1) + geq[k]) + gd);
-                jr[k] = (float)(-F);
+                const double F = g[k] * (xk - xl) + gk1 * (xk - xr) + (geq[k] * xk - ieq[k]) + (id + f32_to_f64_int(gdf) * (xk - vl1));
+                jd[k] = f64_to_f32_int((g[k] + gk1) + geq[k]) + gdf;
+                jr[k] = __uint_as_float(__float_as_uint(f64_to_f32_int(F)) ^ 0x80000000u);
             }
             __syncwarp();
             warp_partition_solve<float>(N, lane, g, jd, jr, jc, jp, reinterpret_cast<float*>(sfl));
+            const float vrel = f64_to_f32_int(c.v_reltol), vabs = f64_to_f32_int(c.v_abstol);
             for (int k = 1 + lane; k <= N; k += 32) {
                 const double old = xs[k];
-                const double nw = old + (double)jr[k];
-                const double tol = c.v_reltol * fmax(fabs(nw), fabs(old)) + c.v_abstol;
-                ok = ok && fabs(nw - old) <= tol;
-                fin = fin && isfinite(nw);
+                const float dy = jr[k];
+                const double nw = old + f32_to_f64_int(dy);
+                const float nwf = f64_to_f32_int(nw), oldf = f64_to_f32_int(old);
+                ok = ok && !(fabsf(dy) > vrel * fmaxf(fabsf(nwf), fabsf(oldf)) + vabs);
+                fin = fin && isfinite(nwf);
                 xs[k] = nw;
             }
         }
