@@ -144,10 +144,15 @@ int sp_solve_batch_device(sp_ctx* ctx, const double* d_matrices, const double* d
  *                                                          mosfet/level1.rs:23-71
  *   NPN/PNP: f[0] IS, f[1] BF, f[2] BR, f[3] NF, f[4] NR, f[5] VAF (<=0: inf)
  *                                                          bjt.rs:23-76
+ *   BSIM3N/BSIM3P: f[0] = first of SP_B3_CARD consecutive slots holding the
+ *         model card and instance sizes in sp_bsim3_card order
+ *                                                          mosfet/bsim3/params.rs
  * node[] holds MNA node indices (0-based, ground = -1):
  *   two-terminal: node[0] = pos/anode, node[1] = neg/cathode
  *   MOSFET: node[0] = drain, node[1] = gate, node[2] = source
  *   BJT:    node[0] = collector, node[1] = base, node[2] = emitter
+ *   BSIM3:  node[0] = drain, node[1] = gate, node[2] = source, node[3] = bulk
+ *   node[3] is -1 for every other kind.
  * branch: index of the element's current variable (V and L only), else -1;
  *   its MNA row is num_nodes + branch.
  * wave: index into sp_circuit.pulses for a time-varying V/I, else -1. */
@@ -161,14 +166,32 @@ enum sp_element_kind {
     SP_EL_NMOS = 7,
     SP_EL_PMOS = 8,
     SP_EL_NPN = 9,
-    SP_EL_PNP = 10
+    SP_EL_PNP = 10,
+    SP_EL_BSIM3N = 11, /* BSIM3v3.3 DC model (LEVEL=49 / 8), mosfet/bsim3/evaluate.rs */
+    SP_EL_BSIM3P = 12
+};
+
+/* Parameter slots of a BSIM3 element, relative to its field[0]: the model
+ * parameters the DC evaluation reads (Bsim3Params, mosfet/bsim3/params.rs:13-143)
+ * with the instance sizes W, L, NF.  TNOM in kelvin.  Defaults:
+ * Bsim3Params::nmos_default / pmos_default (params.rs:160-310). */
+enum sp_bsim3_card {
+    SP_B3_TOX = 0, SP_B3_LINT, SP_B3_WINT,
+    SP_B3_VTH0, SP_B3_K1, SP_B3_K2, SP_B3_DVT0, SP_B3_DVT1, SP_B3_DVT2, SP_B3_NFACTOR,
+    SP_B3_K3, SP_B3_K3B, SP_B3_W0, SP_B3_DVT0W, SP_B3_DVT1W, SP_B3_DVT2W,
+    SP_B3_U0, SP_B3_UA, SP_B3_UB, SP_B3_UC, SP_B3_VSAT,
+    SP_B3_PCLM, SP_B3_PDIBLC1, SP_B3_PDIBLC2, SP_B3_DROUT,
+    SP_B3_ETA0, SP_B3_ETAB, SP_B3_DSUB, SP_B3_PDIBLCB, SP_B3_PVAG,
+    SP_B3_NCH, SP_B3_TNOM, SP_B3_KT2,
+    SP_B3_W, SP_B3_L, SP_B3_NF,
+    SP_B3_CARD /* number of slots */
 };
 
 #define SP_MAX_FIELDS 6
 
 typedef struct sp_element {
     int32_t kind;
-    int32_t node[3];
+    int32_t node[4];
     int32_t branch;
     int32_t wave;
     int32_t field[SP_MAX_FIELDS];
@@ -217,6 +240,16 @@ typedef struct sp_circuit {
      * default (newton.rs:80-83). */
     const double* nodeset;
 } sp_circuit;
+
+/* Batched BSIM3 DC evaluation (Bsim3Mosfet::evaluate, mosfet/bsim3/evaluate.rs:171-265,
+ * with Bsim3Derived::from_params at TNOM, derived.rs:81-196): device i has the
+ * card d_card[i][SP_B3_CARD] (sp_bsim3_card order) and the bias
+ * d_bias[i][3] = (vgs, vds, vbs); d_out[i][6] receives (ids, gds, gm, gmbs, vth,
+ * vdsat) and d_region[i] (optional) 0 subthreshold, 1 linear, 2 saturation.
+ * pmos != 0 selects the P-channel sign convention.  The same device function
+ * stamps BSIM3 elements in the Newton kernels. */
+int sp_bsim3_eval_device(sp_ctx* ctx, int pmos, const double* d_card, const double* d_bias, uint64_t count,
+                         double* d_out, uint8_t* d_region, void* stream);
 
 /* Histogram of column `col` of values[rows][ld] (Histogram::new,
  * statistics.rs:243-268): num_bins bins of width (max - min) / num_bins,

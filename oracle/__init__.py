@@ -71,6 +71,8 @@ def _bind(L):
         "or_rng_fill": (None, [i32, u64, u64, u32, u64, P(d)]),
         "or_mos_evaluate": (i32, [i32, P(d), d, d, P(d)]),
         "or_diode_evaluate": (None, [d, d, d, P(d)]),
+        "or_bsim3_evaluate": (None, [i32, P(d), P(d), u64, P(d), P(C.c_uint8)]),
+        "or_bsim3_default_card": (None, [i32, P(d)]),
         "or_limit_voltage": (d, [d, d]),
         "or_thermal_voltage": (d, [d]),
         "or_bjt_evaluate": (None, [i32, P(d), d, d, P(d)]),
@@ -264,6 +266,27 @@ def transient(circuit, cfg, seed, count, method, h, tstop, probe_idx=-1, first=0
     lib().or_transient(C.byref(cc), C.byref(cfg), seed, first, count, _dp(table), cols, method, h, tstop, probe_idx,
                        _dp(x), _dp(pr), st.ctypes.data_as(C.POINTER(C.c_uint8)), threads)
     return x, pr, st
+
+
+def bsim3_default_card(pmos=False):
+    """Bsim3Params::{nmos,pmos}_default as an sp_bsim3_card vector."""
+    from spicier_gb300 import _abi as abi
+    out = np.zeros(abi.SP_B3_CARD)
+    lib().or_bsim3_default_card(int(pmos), _dp(out))
+    return out
+
+
+def bsim3_evaluate(card, bias, pmos=False):
+    """Oracle BSIM3 evaluation: card[count][SP_B3_CARD], bias[count][3] ->
+    (out[count][6] = ids, gds, gm, gmbs, vth, vdsat; region[count])."""
+    card = np.ascontiguousarray(card, dtype=np.float64)
+    bias = np.ascontiguousarray(bias, dtype=np.float64)
+    n = bias.shape[0]
+    out = np.zeros((n, 6))
+    reg = np.zeros(n, dtype=np.uint8)
+    lib().or_bsim3_evaluate(int(pmos), _dp(card), _dp(bias), n, _dp(out),
+                            reg.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return out, reg
 
 
 def ac_frequencies(fstart, fstop, num_points, sweep):

@@ -124,6 +124,22 @@ int or_mos_evaluate(int pmos, const double* p6, double vgs, double vds, double* 
     return mos_evaluate(pmos != 0, mp, vgs, vds, &out3[0], &out3[1], &out3[2]);
 }
 
+// Bsim3Mosfet::evaluate for `count` devices: card[i][SP_B3_CARD], bias[i][3] =
+// (vgs, vds, vbs); out[i][6] = (ids, gds, gm, gmbs, vth, vdsat), region[i].
+void or_bsim3_evaluate(int pmos, const double* card, const double* bias, uint64_t count, double* out,
+                       uint8_t* region) {
+    const bool cr = math_mode() == 1;
+    for (uint64_t i = 0; i < count; ++i) {
+        const double* c = card + i * SP_B3_CARD;
+        const Bsim3Eval r = bsim3_evaluate(pmos != 0, c, bsim3_derive(c, cr), bias[3 * i], bias[3 * i + 1],
+                                           bias[3 * i + 2], cr);
+        double* o = out + 6 * i;
+        o[0] = r.ids, o[1] = r.gds, o[2] = r.gm, o[3] = r.gmbs, o[4] = r.vth, o[5] = r.vdsat;
+        if (region) region[i] = (uint8_t)r.region;
+    }
+}
+void or_bsim3_default_card(int pmos, double* card) { bsim3_default_card(pmos != 0, card); }
+
 void or_diode_evaluate(double is, double n, double vd, double* out2) {
     diode_evaluate(is, n, vd, &out2[0], &out2[1]);
 }

@@ -17,6 +17,7 @@
 
 #include "../include/spicier_gb300.h"
 #include "../spicier_gb300/csrc/cr_math.cuh"
+#include "bsim3.hpp"
 
 namespace oracle {
 
@@ -366,6 +367,36 @@ inline void stamp_dc(const sp_circuit& c, const double* P, const double* x, Mna&
                 m.current_source(cn, en, ic_eq);
                 double ib_eq = ib - gpi * vbe_ieq;
                 m.current_source(bn, en, ib_eq);
+                break;
+            }
+            case SP_EL_BSIM3N:
+            case SP_EL_BSIM3P: {  // bsim3/mod.rs:176-227, 275-294: no limiting
+                int d = nd[0], g = nd[1], s = nd[2], b = nd[3];
+                const double* card = P + el.field[0];
+                const bool cr = math_mode() == 1;
+                const Bsim3Derived dv = bsim3_derive(card, cr);
+                double vg = node_v(x, g), vd = node_v(x, d), vs = node_v(x, s), vb = node_v(x, b);
+                double vgs = vg - vs, vds = vd - vs, vbs = vb - vs;
+                const Bsim3Eval r = bsim3_evaluate(el.kind == SP_EL_BSIM3P, card, dv, vgs, vds, vbs, cr);
+                m.conductance(d, s, r.gds);
+                if (d >= 0) {
+                    if (g >= 0) m.add(d, g, r.gm);
+                    if (s >= 0) m.add(d, s, -r.gm);
+                }
+                if (s >= 0) {
+                    if (g >= 0) m.add(s, g, -r.gm);
+                    m.add(s, s, r.gm);
+                }
+                if (d >= 0) {
+                    if (b >= 0) m.add(d, b, r.gmbs);
+                    if (s >= 0) m.add(d, s, -r.gmbs);
+                }
+                if (s >= 0) {
+                    if (b >= 0) m.add(s, b, -r.gmbs);
+                    m.add(s, s, r.gmbs);
+                }
+                double ieq = r.ids - r.gds * vds - r.gm * vgs - r.gmbs * vbs;
+                m.current_source(d, s, ieq);
                 break;
             }
             default:

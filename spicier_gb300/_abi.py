@@ -45,6 +45,13 @@ SP_PREC_FP64_EXACT = 2
 # sp_element_kind
 SP_EL_R, SP_EL_C, SP_EL_L, SP_EL_V, SP_EL_I = 1, 2, 3, 4, 5
 SP_EL_D, SP_EL_NMOS, SP_EL_PMOS, SP_EL_NPN, SP_EL_PNP = 6, 7, 8, 9, 10
+SP_EL_BSIM3N, SP_EL_BSIM3P = 11, 12
+# sp_bsim3_card: the slots of a BSIM3 element from its field[0], in order
+BSIM3_CARD = ("tox", "lint", "wint", "vth0", "k1", "k2", "dvt0", "dvt1", "dvt2", "nfactor",
+              "k3", "k3b", "w0", "dvt0w", "dvt1w", "dvt2w", "u0", "ua", "ub", "uc", "vsat",
+              "pclm", "pdiblc1", "pdiblc2", "drout", "eta0", "etab", "dsub", "pdiblcb", "pvag",
+              "nch", "tnom", "kt2", "w", "l", "nf")
+SP_B3_CARD = len(BSIM3_CARD)
 SP_MAX_FIELDS = 6
 
 # sp_draw_kind
@@ -79,7 +86,7 @@ class SpBatchConfig(C.Structure):
 class SpElement(C.Structure):
     _fields_ = [
         ("kind", C.c_int32),
-        ("node", C.c_int32 * 3),
+        ("node", C.c_int32 * 4),
         ("branch", C.c_int32),
         ("wave", C.c_int32),
         ("field", C.c_int32 * SP_MAX_FIELDS),

@@ -120,6 +120,7 @@ def _bind(L):
         "sp_grid_solve_device": (i32, [vp, P(abi.SpGridConfig), u64, u64, u64, vp, vp, vp, vp, vp, vp]),
         "sp_grid_solve": (i32, [vp, P(abi.SpGridConfig), u64, u64, u64, vp, vp, vp, vp, vp]),
         "sp_histogram_device": (i32, [vp, vp, u64, u32, u32, vp, d, d, u32, vp, vp]),
+        "sp_bsim3_eval_device": (i32, [vp, i32, vp, vp, u64, vp, vp, vp]),
         "sp_yield_device": (i32, [vp, vp, u64, u32, vp, vp, u32, vp, vp]),
         "sp_profile_enable": (i32, [vp, i32]),
         "sp_profile_read": (i32, [vp, P(SpKernelTime), i32, P(i32)]),

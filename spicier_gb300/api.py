@@ -333,6 +333,19 @@ class Context:
                                                      _vp(newton), _vp(krylov), _vp(status), _vp(resid), stream))
 
     # -- statistics ------------------------------------------------------------
+    def bsim3_eval_device(self, pmos: bool, card, bias, out, region=None, stream: int = 0):
+        """Batched BSIM3 DC evaluation (Bsim3Mosfet::evaluate) on CUDA float64 tensors: card[count][SP_B3_CARD],
+        bias[count][3] = (vgs, vds, vbs) -> out[count][6] = (ids, gds, gm, gmbs, vth, vdsat), region[count] uint8."""
+        count = int(bias.shape[0])
+        if tuple(card.shape) != (count, abi.SP_B3_CARD) or tuple(bias.shape) != (count, 3) or tuple(out.shape) != (count, 6):
+            raise ValueError("card [count][SP_B3_CARD], bias [count][3] and out [count][6] expected")
+        for t in (card, bias, out):
+            if not (t.is_cuda and t.is_contiguous()) or t.element_size() != 8:
+                raise ValueError("contiguous CUDA float64 tensors expected")
+        check(self._ptr, load().sp_bsim3_eval_device(self._ptr, int(pmos), _vp(card), _vp(bias), count, _vp(out),
+                                                     _vp(region), stream))
+        return out
+
     def histogram_device(self, values, col: int, num_bins: int, min: float = None, max: float = None, status=None,
                          stream: int = 0):
         """Histogram of column `col` of a [rows][ld] CUDA tensor (Histogram::new; with min/max None, the

@@ -71,6 +71,22 @@ class Pulse:
     per: float
 
 
+def _bsim3_defaults(pmos: bool) -> Dict[str, float]:
+    """Bsim3Params::nmos_default / pmos_default (mosfet/bsim3/params.rs:160-310),
+    the entries the DC model reads."""
+    d = dict(tox=9e-9, lint=0.0, wint=0.0, vth0=-0.4 if pmos else 0.4, k1=0.5, k2=0.0, dvt0=2.2,
+             dvt1=0.53, dvt2=-0.032, nfactor=1.0, k3=0.0, k3b=0.0, w0=0.0, dvt0w=0.0, dvt1w=0.0,
+             dvt2w=0.0, u0=250.0 if pmos else 670.0, ua=2.25e-9, ub=5.87e-19, uc=-4.65e-11,
+             vsat=1.0e5 if pmos else 1.5e5, pclm=1.3, pdiblc1=0.39, pdiblc2=0.0086, drout=0.56,
+             eta0=0.08, etab=-0.07, dsub=0.56, pdiblcb=0.0, pvag=1.0, nch=1.7e17, tnom=300.15,
+             kt2=0.022, w=1e-6, l=100e-9, nf=1.0)
+    assert tuple(d) == abi.BSIM3_CARD
+    return d
+
+
+BSIM3_DEFAULTS = {False: _bsim3_defaults(False), True: _bsim3_defaults(True)}
+
+
 class Circuit:
     def __init__(self, title: str = ""):
         self.title = title
@@ -117,7 +133,7 @@ class Circuit:
 
     def _add(self, kind: int, name: str, nodes: Sequence[str], fields: Sequence[ParamSpec],
              field_names: Sequence[str], branch: bool = False, pulse: Optional[Pulse] = None) -> int:
-        idx = [self.node(nm) for nm in nodes] + [-1] * (3 - len(nodes))
+        idx = [self.node(nm) for nm in nodes] + [-1] * (4 - len(nodes))
         slots = [self.param(f, f"{name}.{fn}") for f, fn in zip(fields, field_names)]
         br = -1
         if branch:
@@ -168,6 +184,22 @@ class Circuit:
         return self._add(kind, name, (c, b, e), (is_, bf, br, nf, nr, vaf),
                          ("is", "bf", "br", "nf", "nr", "vaf"))
 
+    def B3(self, name, d, g, s, b, pmos: bool = False, **card: ParamSpec):
+        """BSIM3v3.3 MOSFET (LEVEL=49 / 8): drain, gate, source, bulk.  `card`
+        sets any sp_bsim3_card entry by its lower-case name (tox, vth0, u0, ...,
+        w, l, nf; tnom in kelvin), each a value or a distribution; the rest are
+        Bsim3Params::{nmos,pmos}_default (mosfet/bsim3/params.rs:160-310).  The
+        entries take consecutive parameter slots, the first in field[0]."""
+        vals = dict(BSIM3_DEFAULTS[bool(pmos)])
+        for k, v in card.items():
+            if k.lower() not in vals:
+                raise ValueError(f"{name}: {k} is not a BSIM3 card entry")
+            vals[k.lower()] = v
+        kind = abi.SP_EL_BSIM3P if pmos else abi.SP_EL_BSIM3N
+        i = self._add(kind, name, (d, g, s, b), [vals[k] for k in abi.BSIM3_CARD], abi.BSIM3_CARD)
+        self.elements[i]["field"] = self.elements[i]["field"][:1]
+        return i
+
     # -- export ------------------------------------------------------------------
     def to_c(self) -> abi.SpCircuit:
         """The sp_circuit view (arrays kept alive on this object)."""
@@ -177,7 +209,7 @@ class Circuit:
         els = (abi.SpElement * max(ne, 1))()
         for i, e in enumerate(self.elements):
             els[i].kind = e["kind"]
-            for k in range(3):
+            for k in range(4):
                 els[i].node[k] = e["node"][k]
             els[i].branch = e["branch"]
             els[i].wave = e["wave"]

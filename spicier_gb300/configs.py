@@ -105,3 +105,21 @@ def miller_opamp(vto_sigma: float = 0.020, kp_rel_sigma: float = 0.05, rbias: fl
         c.R("RL", "out", "vss", rload)
     c.Cap("CC", "nz", "out", 2e-12)
     return c
+
+
+def bsim3_cmos_chain() -> Circuit:
+    """BSIM3 (LEVEL=49, default 100 nm cards) CMOS inverter driving a common-source
+    stage with a 10 kOhm load, VDD 1.8 V.  Gaussian draws (rng index): VIN 0.8 V
+    sigma 50 mV (0), PMOS VTH0 -0.4 V sigma 20 mV (1), PMOS U0 250 sigma 10 (2),
+    inverter NMOS VTH0 0.4 V sigma 20 mV (3) and L 100 nm sigma 5 nm (4), stage
+    NMOS VTH0 0.4 V sigma 20 mV (5) and U0 670 sigma 20 (6).  Nodeset 0.9 V on the
+    inverter output and the stage output."""
+    c = Circuit("bsim3_cmos_chain")
+    c.V("VDD", "vdd", "0", 1.8)
+    c.V("VIN", "in", "0", Gauss(0.8, 0.05, 0))
+    c.B3("MP", "mid", "in", "vdd", "vdd", pmos=True, vth0=Gauss(-0.4, 0.02, 1), u0=Gauss(250.0, 10.0, 2), w=2e-6)
+    c.B3("MN", "mid", "in", "0", "0", vth0=Gauss(0.4, 0.02, 3), l=Gauss(100e-9, 5e-9, 4))
+    c.R("RL", "vdd", "out", 10e3)
+    c.B3("M2", "out", "mid", "0", "0", vth0=Gauss(0.4, 0.02, 5), u0=Gauss(670.0, 20.0, 6))
+    c.nodeset = {"mid": 0.9, "out": 0.9}
+    return c

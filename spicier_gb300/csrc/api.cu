@@ -354,17 +354,14 @@ static int validate_circuit(sp_ctx* ctx, const sp_circuit* c) {
     const int nn = c->num_nodes;
     for (int e = 0; e < c->num_elements; ++e) {
         const sp_element& el = c->elements[e];
-        if (el.kind < SP_EL_R || el.kind > SP_EL_PNP)
+        if (el.kind < SP_EL_R || el.kind > SP_EL_BSIM3P)
             return fail(ctx, SP_ERR_INVALID_ARGUMENT, "element %d: bad kind %d", e, el.kind);
-        int terms = (el.kind >= SP_EL_NMOS) ? 3 : 2;
+        const int terms = terminal_count(el.kind);
         for (int t = 0; t < terms; ++t)
             if (el.node[t] < -1 || el.node[t] >= nn)
                 return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: node %d out of range", e, el.node[t]);
-        int nf = (el.kind == SP_EL_D) ? 2 : (el.kind >= SP_EL_NMOS ? 6 : 1);
-        for (int f = 0; f < nf; ++f)
-            if (el.field[f] < 0 || el.field[f] >= c->num_params)
-                return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: field slot %d out of range", e,
-                            el.field[f]);
+        if (!element_slots_ok(el, c->num_params))
+            return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: parameter slot out of range", e);
         bool needs_branch = el.kind == SP_EL_V || el.kind == SP_EL_L;
         if (needs_branch && (el.branch < 0 || el.branch >= c->num_branches))
             return fail(ctx, SP_ERR_INVALID_DIMENSION, "element %d: branch %d out of range", e, el.branch);
@@ -1087,6 +1084,18 @@ int sp_grid_solve(sp_ctx* ctx, const sp_grid_config* cfg, uint64_t seed, uint64_
 // ---------------------------------------------------------------------------
 // Histogram and yield (statistics.rs)
 // ---------------------------------------------------------------------------
+int sp_bsim3_eval_device(sp_ctx* ctx, int pmos, const double* d_card, const double* d_bias, uint64_t count,
+                         double* d_out, uint8_t* d_region, void* stream) {
+    if (!ctx || (count && (!d_card || !d_bias || !d_out))) return SP_ERR_INVALID_ARGUMENT;
+    if (count > ((uint64_t)1 << 40)) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "at most 2^40 devices per call");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ProfScope prof(ctx, "bsim3_eval", (cudaStream_t)stream);
+    SP_CUDA(ctx, launch_bsim3_eval(pmos, d_card, d_bias, count, d_out, d_region, (cudaStream_t)stream),
+            "bsim3 evaluation launch");
+    return SP_OK;
+}
+
 int sp_histogram_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld, uint32_t col,
                         const uint8_t* d_status, double min, double max, uint32_t num_bins, uint64_t* d_bins,
                         void* stream) {
@@ -1273,6 +1282,16 @@ static std::vector<double> ac_grid(const sp_ac_config* c) {
     return f;
 }
 
+// The BSIM3 small-signal model needs its Meyer and junction capacitances
+// (evaluate_capacitances, mosfet/bsim3/evaluate.rs:82-168), which this
+// library does not evaluate: such circuits are refused, not approximated.
+static int ac_no_bsim3(sp_ctx* ctx, const sp_element* el, int num_elements) {
+    for (int e = 0; e < num_elements; ++e)
+        if (el[e].kind == SP_EL_BSIM3N || el[e].kind == SP_EL_BSIM3P)
+            return fail(ctx, SP_ERR_INVALID_ARGUMENT, "element %d: AC sweeps do not model BSIM3 elements", e);
+    return SP_OK;
+}
+
 static int ac_validate(sp_ctx* ctx, const sp_ac_config* c, int n, int num_elements) {
     if (!c) return SP_ERR_INVALID_ARGUMENT;
     if (c->sweep < SP_AC_LIN || c->sweep > SP_AC_OCT) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "unknown sweep type");
@@ -1355,6 +1374,7 @@ int sp_ac_sweep_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_con
     if (!ctx || !topo || !dc_cfg || !d_probe || !d_status) return SP_ERR_INVALID_ARGUMENT;
     if (topo->ctx != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "topology belongs to another context");
     int rc = ac_validate(ctx, ac, topo->n, topo->num_elements);
+    if (rc == SP_OK) rc = ac_no_bsim3(ctx, topo->h_elements.data(), topo->num_elements);
     if (rc) return rc;
     if (count == 0) return SP_OK;
     std::lock_guard<std::mutex> g(ctx->mu);
@@ -1369,6 +1389,7 @@ int sp_ac_sweep(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* 
                 double* probe, uint8_t* status) {
     if (!ctx || !circuit || !dc_cfg || !probe || !status) return SP_ERR_INVALID_ARGUMENT;
     int rc = ac_validate(ctx, ac, circuit->num_nodes + circuit->num_branches, circuit->num_elements);
+    if (rc == SP_OK && circuit->elements) rc = ac_no_bsim3(ctx, circuit->elements, circuit->num_elements);
     if (rc) return rc;
     if (count == 0) return SP_OK;
     sp_topology* t = nullptr;

@@ -14,6 +14,7 @@
 
 #include "../../include/spicier_gb300.h"
 #include "newton_dense.cuh"
+#include "pdl.cuh"
 
 namespace sp {
 
@@ -30,6 +31,8 @@ struct DrawLaunch {
     unsigned int* hard;   // count of draws whose rounding was undecided (or nullptr)
 };
 
+cudaError_t launch_bsim3_eval(int pmos, const double* card, const double* bias, uint64_t count, double* out,
+                              uint8_t* region, cudaStream_t st);
 cudaError_t launch_histogram(const double* v, uint64_t rows, uint32_t ld, uint32_t col, const uint8_t* status,
                              double mn, double mx, uint32_t nb, uint64_t* bins, int num_sms, cudaStream_t st);
 cudaError_t launch_yield(const double* v, uint64_t rows, uint32_t ld, const uint8_t* status,

@@ -34,6 +34,8 @@ __device__ inline double draw_one(const sp_param& p, uint64_t seed, uint32_t swe
 constexpr int kDrawSamples = 32, kDrawLanes = 8;
 
 __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 3) draw_kernel(DrawLaunch L) {
+    pdl_wait();
+    pdl_trigger();
     const uint64_t s = (uint64_t)blockIdx.x * kDrawSamples + threadIdx.x;
     const bool live = s < L.count;
     const DevCircuit& c = L.c;
@@ -62,7 +64,35 @@ __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 3) draw_kernel(Draw
 cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st) {
     if (L.count == 0) return cudaSuccess;
     const uint64_t grid = (L.count + kDrawSamples - 1) / kDrawSamples;
-    draw_kernel<<<(unsigned)grid, dim3(kDrawSamples, kDrawLanes), 0, st>>>(L);
+    return launch_chained(draw_kernel, dim3((unsigned)grid), dim3(kDrawSamples, kDrawLanes), 0, st, L);
+}
+
+// Batched Bsim3Mosfet::evaluate (one thread per device): the per-sample
+// constants from the device's card, then the evaluation at its bias.
+__global__ void bsim3_eval_kernel(int pmos, const double* __restrict__ card, const double* __restrict__ bias,
+                                  uint64_t count, double* __restrict__ out, uint8_t* __restrict__ region) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const double* c = card + i * SP_B3_CARD;
+    double k[B3C_COUNT];
+    bsim3_constants([&](int j) { return c[j]; }, [&](int j, double v) { k[j] = v; });
+    const Bsim3Out r = bsim3_eval(pmos != 0, [&](int j) { return k[j]; }, bias[3 * i], bias[3 * i + 1], bias[3 * i + 2]);
+    double* o = out + 6 * i;
+    o[0] = r.ids;
+    o[1] = r.gds;
+    o[2] = r.gm;
+    o[3] = r.gmbs;
+    o[4] = r.vth;
+    o[5] = r.vdsat;
+    if (region) region[i] = (uint8_t)r.region;
+}
+
+cudaError_t launch_bsim3_eval(int pmos, const double* card, const double* bias, uint64_t count, double* out,
+                              uint8_t* region, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    const int block = 128;
+    bsim3_eval_kernel<<<(unsigned)((count + block - 1) / block), block, 0, st>>>(pmos, card, bias, count, out,
+                                                                                region);
     return cudaGetLastError();
 }
 
@@ -91,11 +121,8 @@ cudaError_t launch_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t pa
 
 cudaError_t launch_newton_exact(const NewtonLaunch& L, bool fallback, int grid, int block, size_t smem,
                                 cudaStream_t st) {
-    if (fallback)
-        SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
-    else
-        SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
-    return cudaGetLastError();
+    if (fallback) return launch_chained(SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>, dim3(grid), dim3(block), smem, st, L);
+    return launch_chained(SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>, dim3(grid), dim3(block), smem, st, L);
 }
 
 // BatchedLuSolver::solve_batch in FP64 with the reference's LU

@@ -18,18 +18,13 @@ namespace sp {
 
 cudaError_t launch_newton_fast(int prec, const NewtonLaunch& L, bool fallback, int grid, int block,
                                size_t smem, cudaStream_t st) {
-    if (prec == SP_PREC_MIXED) {
-        if (fallback)
-            SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_MIXED><<<grid, block, smem, st>>>(L);
-        else
-            SP_KERNEL_NS::newton_primary_kernel<SP_PREC_MIXED><<<grid, block, smem, st>>>(L);
-    } else {
-        if (fallback)
-            SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
-        else
-            SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64><<<grid, block, smem, st>>>(L);
-    }
-    return cudaGetLastError();
+    using namespace SP_KERNEL_NS;
+    const dim3 g(grid), b(block);
+    if (prec == SP_PREC_MIXED)
+        return fallback ? launch_chained(newton_fallback_kernel<SP_PREC_MIXED>, g, b, smem, st, L)
+                        : launch_chained(newton_primary_kernel<SP_PREC_MIXED>, g, b, smem, st, L);
+    return fallback ? launch_chained(newton_fallback_kernel<SP_PREC_FP64>, g, b, smem, st, L)
+                    : launch_chained(newton_primary_kernel<SP_PREC_FP64>, g, b, smem, st, L);
 }
 
 // Mixed-precision BatchedLuSolver::solve_batch: FP32 partial-pivot LU in
@@ -262,6 +257,8 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
                                                            const uint8_t* __restrict__ status,
                                                            sp_moments* __restrict__ partial) {
     __shared__ sp_moments sh[256];
+    pdl_wait();
+    pdl_trigger();
     const uint32_t c = threadIdx.x % cp, g = threadIdx.x / cp, groups = 256 / cp;
     const uint64_t lo = (uint64_t)blockIdx.x * chunk, hi = min(rows, lo + chunk);
     sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
@@ -307,6 +304,8 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
 __global__ void __launch_bounds__(256) moments_tree_kernel(const sp_moments* __restrict__ partial, uint32_t nblocks,
                                                            sp_moments* __restrict__ out) {
     __shared__ sp_moments sh[256];
+    pdl_wait();
+    pdl_trigger();
     const uint32_t col = blockIdx.x;
     sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
     for (uint32_t b0 = threadIdx.x; b0 < nblocks; b0 += 4 * 256) {  // four partials in flight, merged in order
@@ -357,11 +356,10 @@ cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uin
         uint32_t cp = 1;
         while (cp < cols) cp <<= 1;
         const uint32_t nb = (uint32_t)((rows + chunk - 1) / chunk);
-        moments_rows_kernel<<<nb, 256, 0, st>>>(values, rows, ld, cols, cp, chunk, status, partial);
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = launch_chained(moments_rows_kernel, dim3(nb), dim3(256), 0, st, values, rows, ld, cols, cp,
+                                       chunk, status, partial);
         if (e != cudaSuccess) return e;
-        moments_tree_kernel<<<cols, 256, 0, st>>>(partial, nb, out);
-        return cudaGetLastError();
+        return launch_chained(moments_tree_kernel, dim3(cols), dim3(256), 0, st, partial, nb, out);
     }
     nblocks = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(nblocks, 256), std::max<uint64_t>(1, rows / 1024));
     dim3 grid(nblocks, cols);

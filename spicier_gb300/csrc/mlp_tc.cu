@@ -36,6 +36,7 @@
 
 #include "mlp_act.cuh"
 #include "mlp_tc.h"
+#include "pdl.cuh"
 
 namespace sp {
 namespace mlptc {
@@ -227,6 +228,8 @@ __host__ __device__ inline int teams_for(const Args& a) {
 
 __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int teams) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
+    pdl_wait();  // the drawn parameters (and the packed weights) are complete and visible
+    pdl_trigger();
     // 1024-byte alignment of the swizzled operands (the dynamic window may start lower)
     unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
     const Carve cv = carve(a, teams);
@@ -447,8 +450,7 @@ cudaError_t launch(const Args& a, int num_sms, cudaStream_t st) {
     int grid = (ntiles + teams - 1) / teams;
     if (grid > num_sms) grid = num_sms;
     if (grid < 1) return cudaSuccess;
-    infer_kernel<<<grid, teams * kTeam, smem, st>>>(a, teams);
-    return cudaGetLastError();
+    return launch_chained(infer_kernel, dim3(grid), dim3(teams * kTeam), smem, st, a, teams);
 }
 
 }  // namespace mlptc

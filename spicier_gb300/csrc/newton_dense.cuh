@@ -26,6 +26,7 @@
 //                   root of F, independent of the FP32 factorisation error.
 #pragma once
 #include "circuit_dev.cuh"
+#include "pdl.cuh"
 
 namespace sp {
 
@@ -315,6 +316,8 @@ namespace SP_KERNEL_NS {
 template <int PREC>
 __global__ void newton_primary_kernel(NewtonLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
+    pdl_wait();
+    pdl_trigger();
     const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.count) return;
     Work w = make_work<PREC>(smem, L.c.n, blockDim.x, threadIdx.x);
@@ -412,6 +415,8 @@ namespace SP_KERNEL_NS {
 template <int PREC>
 __global__ void newton_fallback_kernel(NewtonLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
+    pdl_wait();
+    pdl_trigger();
     Work w = make_work<PREC>(smem, L.c.n, blockDim.x, threadIdx.x);
     const int n = L.c.n;
     const bool warm = L.x0 != nullptr;

@@ -99,22 +99,20 @@ bool check_circuit(const sp_circuit* c, char* err, size_t err_len, int* code) {
     }
     for (int e = 0; e < c->num_elements; ++e) {
         const sp_element& el = c->elements[e];
-        if (el.kind < SP_EL_R || el.kind > SP_EL_PNP) {
+        if (el.kind < SP_EL_R || el.kind > SP_EL_BSIM3P) {
             *code = report(err, err_len, SP_ERR_INVALID_ARGUMENT, "element %d: bad kind %d", e, el.kind);
             return false;
         }
-        int terms = el.kind >= SP_EL_NMOS ? 3 : 2;
+        const int terms = terminal_count(el.kind);
         for (int t = 0; t < terms; ++t)
             if (el.node[t] < -1 || el.node[t] >= c->num_nodes) {
                 *code = report(err, err_len, SP_ERR_INVALID_DIMENSION, "element %d: node out of range", e);
                 return false;
             }
-        int nf = el.kind == SP_EL_D ? 2 : (el.kind >= SP_EL_NMOS ? 6 : 1);
-        for (int f = 0; f < nf; ++f)
-            if (el.field[f] < 0 || el.field[f] >= c->num_params) {
-                *code = report(err, err_len, SP_ERR_INVALID_DIMENSION, "element %d: field slot out of range", e);
-                return false;
-            }
+        if (!element_slots_ok(el, c->num_params)) {
+            *code = report(err, err_len, SP_ERR_INVALID_DIMENSION, "element %d: field slot out of range", e);
+            return false;
+        }
         if ((el.kind == SP_EL_V || el.kind == SP_EL_L) && (el.branch < 0 || el.branch >= c->num_branches)) {
             *code = report(err, err_len, SP_ERR_INVALID_DIMENSION, "element %d: branch out of range", e);
             return false;

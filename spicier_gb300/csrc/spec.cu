@@ -456,6 +456,8 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
         for (size_t j = 0; j < fcs.size(); ++j) o << "#define cf" << fcs[j] << " (spx_cf[" << j << " * 128])\n";
     }
     o << "extern \"C\" __global__ void __launch_bounds__(128, " << (sm ? (fp32_jac ? 4 : 2) : 1) << ") spec_newton(SpecArgs a) {\n"
+      << "  asm volatile(\"griddepcontrol.wait;\" ::: \"memory\");  // chained launch: predecessor complete\n"
+      << "  asm volatile(\"griddepcontrol.launch_dependents;\" ::: \"memory\");\n"
       << "  const u64 nthreads = (u64)gridDim.x * blockDim.x;\n"
       << "  u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
       << "  if (s >= a.count) return;\n"
@@ -593,6 +595,11 @@ int spec_prepare(sp_topology* t, int prec, std::string& err) {
         return t->spec_kernel[slot] ? SP_OK : SP_ERR_BACKEND;
     }
     t->spec_tried[slot] = true;
+    for (const sp_element& el : t->h_elements)
+        if (el.kind == SP_EL_BSIM3N || el.kind == SP_EL_BSIM3P) {
+            t->spec_log[slot] = err = "BSIM3 elements run in the generic kernels";
+            return SP_ERR_BACKEND;
+        }
     // cache key: precision, sizes, element list, parameter specs, nodeset
     std::string key;
     key.push_back((char)slot);
@@ -683,8 +690,8 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     void* args[] = {&a};
     const uint64_t resident = (uint64_t)t->ctx->num_sms * (uint64_t)t->spec_bpsm[slot];
     const unsigned grid = (unsigned)std::min<uint64_t>((L.count + 127) / 128, resident);
-    return cudaLaunchKernel((const void*)t->spec_kernel[slot], dim3(grid), dim3(128), args,
-                            spec_smem_bytes(t, prec == SP_PREC_MIXED), st);
+    ChainedLaunch cl(dim3(grid), dim3(128), spec_smem_bytes(t, prec == SP_PREC_MIXED), st);
+    return cudaLaunchKernelExC(&cl.cfg, (const void*)t->spec_kernel[slot], args);
 }
 
 void spec_release_all(sp_ctx* ctx) {
@@ -702,13 +709,11 @@ extern "C" int sp_specialize_source(const sp_circuit* c, int precision, int comp
     if (precision != SP_PREC_MIXED && precision != SP_PREC_FP64) return SP_ERR_INVALID_ARGUMENT;
     for (int e = 0; e < c->num_elements; ++e) {
         const sp_element& el = c->elements[e];
-        if (el.kind < SP_EL_R || el.kind > SP_EL_PNP) return SP_ERR_INVALID_ARGUMENT;
-        const int terms = el.kind >= SP_EL_NMOS ? 3 : 2;
+        if (el.kind < SP_EL_R || el.kind > SP_EL_PNP) return SP_ERR_INVALID_ARGUMENT;  // no BSIM3 here
+        const int terms = terminal_count(el.kind);
         for (int k = 0; k < terms; ++k)
             if (el.node[k] < -1 || el.node[k] >= c->num_nodes) return SP_ERR_INVALID_DIMENSION;
-        const int nf = el.kind == SP_EL_D ? 2 : (el.kind >= SP_EL_NMOS ? 6 : 1);
-        for (int f = 0; f < nf; ++f)
-            if (el.field[f] < 0 || el.field[f] >= c->num_params) return SP_ERR_INVALID_DIMENSION;
+        if (!element_slots_ok(el, c->num_params)) return SP_ERR_INVALID_DIMENSION;
         if ((el.kind == SP_EL_V || el.kind == SP_EL_L) && (el.branch < 0 || el.branch >= c->num_branches))
             return SP_ERR_INVALID_DIMENSION;
     }

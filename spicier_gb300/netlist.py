@@ -13,10 +13,14 @@ parser/commands.rs:600-735, crates/spicier-core/src/units.rs:15-50):
   [PULSE(v1 v2 [td tr tf pw per])] (a PULSE source's DC value is v1,
   Waveform::dc_value); I: name n+ n- [DC] value; D: name a k [model];
   M: name d g s b [model] [W= L= NF=] (the bulk becomes a node, as
-  expect_node makes it, but no model uses it);
+  expect_node makes it; only a BSIM3 model connects it);
   Q: name c b e [model];
-* .MODEL name D (IS N), NMOS / PMOS level 1 (VTO KP LAMBDA W L), NPN / PNP
-  (IS BF BR NF NR VAF); .PARAM name=value; .NODESET V(node)=value; .END.
+* .MODEL name D (IS N), NMOS / PMOS level 1 (VTO KP LAMBDA W L), NMOS / PMOS
+  LEVEL=49 or 8 (BSIM3: the card entries of Circuit.B3 by their SPICE names,
+  with the aliases DL, DW, VTHO, UO and TNOM in Celsius, parse_bsim3_params,
+  parser/commands.rs:1463-1575; entries the DC model does not read are
+  accepted and ignored), NPN / PNP (IS BF BR NF NR VAF); .PARAM name=value;
+  .NODESET V(node)=value; .END.
   Other dot commands (.OP .DC .TRAN .AC .PRINT .OPTIONS ...) are recorded in
   Netlist.commands and otherwise ignored.
 
@@ -32,7 +36,23 @@ import re
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Tuple
 
-from .circuit import Circuit, ParamSpec, Pulse
+from .circuit import BSIM3_DEFAULTS, Circuit, ParamSpec, Pulse
+
+_BSIM3_ALIAS = {"DL": "lint", "DW": "wint", "VTHO": "vth0", "UO": "u0"}
+
+
+def _bsim3_card(mp: Dict[str, float]) -> Dict[str, float]:
+    """Card entries a BSIM3 .MODEL sets (parse_bsim3_params, parser/commands.rs:1463-1575):
+    the defaults stay for the rest; TNOM is given in Celsius."""
+    from . import _abi as abi
+    card: Dict[str, float] = {}
+    for key, v in mp.items():
+        name = _BSIM3_ALIAS.get(key, key.lower())
+        if name == "tnom":
+            v = v + 273.15
+        if name in abi.BSIM3_CARD:
+            card[name] = v
+    return card
 
 _SUFFIX = {"T": 1e12, "G": 1e9, "MEG": 1e6, "K": 1e3, "": 1.0, "M": 1e-3, "MIL": 25.4e-6, "U": 1e-6, "N": 1e-9,
            "P": 1e-12, "F": 1e-15}
@@ -158,8 +178,8 @@ def parse_netlist(text: str, variations: Optional[Dict[str, ParamSpec]] = None) 
             if kind not in ("D", "NMOS", "PMOS", "NPN", "PNP"):
                 raise NetlistError(no, f"model type {kind} is outside the supported subset")
             mp = _kv(tk, 3, no, params)
-            if kind in ("NMOS", "PMOS") and int(mp.get("LEVEL", 1)) != 1:
-                raise NetlistError(no, "only level-1 MOSFET models are supported")
+            if kind in ("NMOS", "PMOS") and int(mp.get("LEVEL", 1)) not in (1, 8, 49):
+                raise NetlistError(no, "only level-1 and BSIM3 (LEVEL=49 / 8) MOSFET models are supported")
             models[tk[1].upper()] = _Model(kind, mp)
         elif cmd == "NODESET":
             i = 1
@@ -258,6 +278,14 @@ def parse_netlist(text: str, variations: Optional[Dict[str, ParamSpec]] = None) 
                     mp = dict(m.params)
                 k += 1
             inst = _kv(tk, k, no, params)
+            if int(mp.get("LEVEL", 1)) in (8, 49):
+                card = dict(BSIM3_DEFAULTS[pmos])
+                card.update(_bsim3_card(mp))
+                for key in ("W", "L", "NF"):  # instance overrides (parser/elements.rs:455-476)
+                    if key in inst:
+                        card[key.lower()] = inst[key]
+                c.B3(name, d, g, s_, bulk, pmos=pmos, **{k: spec(name, k, v) for k, v in card.items()})
+                continue
             vto = mp.get("VTO", -0.7 if pmos else 0.7)
             kp = mp.get("KP", 1e-5 if pmos else 2e-5)
             lam = mp.get("LAMBDA", 0.0)

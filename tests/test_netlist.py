@@ -105,6 +105,6 @@ def test_errors():
     with pytest.raises(NetlistError):
         parse_netlist("t\nR1 a 0 1k\n", {"R2.r": Gauss(1e3, 10.0, 0)})
     with pytest.raises(NetlistError):
-        parse_netlist("t\n.MODEL X NMOS LEVEL=49\n")
+        parse_netlist("t\n.MODEL X NMOS LEVEL=54\n")
     with pytest.raises(NetlistError):
         parse_netlist("t\nV1 a 0 SIN(0 1 1k)\n")
