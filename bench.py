@@ -524,9 +524,8 @@ def main():
                                     "roofline": {"bound": "hbm", "achieved": gbs_b3, "peak": hbm_peak, "unit": "GB/s",
                                                  "frac": gbs_b3 / hbm_peak,
                                                  "bytes_per_device": bytes_b3 // nb,
-                                                 "note": "not HBM-bound: each device's constants take one correctly "
-                                                         "rounded ln and three exp in integer fixed point (integer "
-                                                         "ALU), as the exact evaluation requires"}}}
+                                                 "note": "FP64-pipe bound, not HBM: ~20 divides and 5 square "
+                                                         "roots per device for its constants and evaluation"}}}
         bc = _cfgs.bsim3_cmos_chain()
         btopo = ctx.topology(bc)
         bx = torch.empty((N, bc.n), dtype=torch.float64, device=dev)

@@ -173,7 +173,8 @@ enum sp_element_kind {
 
 /* Parameter slots of a BSIM3 element, relative to its field[0]: the model
  * parameters the DC evaluation reads (Bsim3Params, mosfet/bsim3/params.rs:13-143)
- * with the instance sizes W, L, NF.  TNOM in kelvin.  Defaults:
+ * with the instance sizes W, L, NF, then those of the small-signal capacitances
+ * (AS, AD, PS, PD: 0 = estimated from Weff).  TNOM in kelvin.  Defaults:
  * Bsim3Params::nmos_default / pmos_default (params.rs:160-310). */
 enum sp_bsim3_card {
     SP_B3_TOX = 0, SP_B3_LINT, SP_B3_WINT,
@@ -184,6 +185,10 @@ enum sp_bsim3_card {
     SP_B3_ETA0, SP_B3_ETAB, SP_B3_DSUB, SP_B3_PDIBLCB, SP_B3_PVAG,
     SP_B3_NCH, SP_B3_TNOM, SP_B3_KT2,
     SP_B3_W, SP_B3_L, SP_B3_NF,
+    /* capacitances of the small-signal model (evaluate_capacitances, evaluate.rs:82-158) */
+    SP_B3_CGSO, SP_B3_CGDO, SP_B3_CGBO, SP_B3_CJ, SP_B3_CJSW, SP_B3_CJSWG,
+    SP_B3_MJ, SP_B3_MJSW, SP_B3_MJSWG, SP_B3_PB, SP_B3_PBSW, SP_B3_PBSWG,
+    SP_B3_AS, SP_B3_AD, SP_B3_PS, SP_B3_PD,
     SP_B3_CARD /* number of slots */
 };
 

@@ -13,7 +13,9 @@
 //   that source the only stimulus); I: no AC stimulus (ac_mag 0);
 //   D: gd at the operating point; MOSFET: gds and the gm VCCS; BJT: gpi, go
 //   and the gm VCCS (evaluate at the operating point, no limiting beyond
-//   what evaluate does).
+//   what evaluate does); BSIM3 (mosfet/bsim3/mod.rs:296-342, stamper
+//   stampers.rs:423-470): gds, the gm and gmbs VCCSs, and j w C for each of
+//   Cgs (g, s), Cgd (g, d), Cgb (g, b), Cbs (b, s), Cbd (b, d) that is > 0.
 #pragma once
 #include <cmath>
 #include <complex>
@@ -107,6 +109,7 @@ struct AcLinear {
     int n = 0;
     std::vector<double> G;  // column-major, real
     std::vector<double> rhs;
+    std::vector<double> caps;  // BSIM3 elements: cgs, cgd, cgb, cbs, cbd at element index * 5
 };
 
 inline AcLinear ac_linearise(const sp_circuit& c, const double* P, const double* x, int source) {
@@ -115,6 +118,7 @@ inline AcLinear ac_linearise(const sp_circuit& c, const double* P, const double*
     L.n = nn + c.num_branches;
     L.G.assign((size_t)L.n * L.n, 0.0);
     L.rhs.assign(L.n, 0.0);
+    L.caps.assign((size_t)c.num_elements * 5, 0.0);
     auto add = [&](int r, int col, double v) {
         if (r >= 0 && col >= 0) L.G[(size_t)col * L.n + r] += v;
     };
@@ -168,6 +172,22 @@ inline AcLinear ac_linearise(const sp_circuit& c, const double* P, const double*
                 vccs(cn, en, bn, en, o[3]);
                 break;
             }
+            case SP_EL_BSIM3N:
+            case SP_EL_BSIM3P: {
+                const int d = nd[0], g = nd[1], s = nd[2], b = nd[3];
+                const bool pm = el.kind == SP_EL_BSIM3P;
+                const double* card = P + el.field[0];
+                const bool cr = math_mode() == 1;
+                const Bsim3Derived dv = bsim3_derive(card, cr);
+                const double vgs = node_v(x, g) - node_v(x, s), vds = node_v(x, d) - node_v(x, s);
+                const double vbs = node_v(x, b) - node_v(x, s);
+                const Bsim3Eval r = bsim3_evaluate(pm, card, dv, vgs, vds, vbs, cr);
+                cond(d, s, r.gds);
+                vccs(d, s, g, s, r.gm);
+                vccs(d, s, b, s, r.gmbs);
+                bsim3_capacitances(pm, card, dv, vds, vbs, r.region, &L.caps[(size_t)e * 5]);
+                break;
+            }
             default:
                 break;
         }
@@ -192,6 +212,16 @@ inline void ac_matrix(const sp_circuit& c, const double* P, const AcLinear& L, d
         } else if (el.kind == SP_EL_L) {
             const int br = nn + el.branch;
             A[(size_t)br * n + br].im -= w * P[el.field[0]];
+        } else if (el.kind == SP_EL_BSIM3N || el.kind == SP_EL_BSIM3P) {
+            const int d = el.node[0], g = el.node[1], s = el.node[2], b = el.node[3];
+            const int pr[5][2] = {{g, s}, {g, d}, {g, b}, {b, s}, {b, d}};
+            for (int k = 0; k < 5; ++k) {
+                const double cap = L.caps[(size_t)e * 5 + k];
+                if (!(cap > 0.0)) continue;
+                const double y = w * cap;
+                const int i = pr[k][0], j = pr[k][1];
+                addc(i, i, y), addc(j, j, y), addc(i, j, -y), addc(j, i, -y);
+            }
         }
     }
 }

@@ -57,6 +57,11 @@ inline void bsim3_default_card(bool pmos, double* card) {
     c[SP_B3_PDIBLCB] = 0.0, c[SP_B3_PVAG] = 1.0;
     c[SP_B3_NCH] = 1.7e17, c[SP_B3_TNOM] = 300.15, c[SP_B3_KT2] = 0.022;
     c[SP_B3_W] = 1e-6, c[SP_B3_L] = 100e-9, c[SP_B3_NF] = 1.0;
+    c[SP_B3_CGSO] = 0.0, c[SP_B3_CGDO] = 0.0, c[SP_B3_CGBO] = 0.0;
+    c[SP_B3_CJ] = 5e-4, c[SP_B3_CJSW] = 5e-10, c[SP_B3_CJSWG] = 0.0;
+    c[SP_B3_MJ] = 0.5, c[SP_B3_MJSW] = 0.33, c[SP_B3_MJSWG] = 0.33;
+    c[SP_B3_PB] = 1.0, c[SP_B3_PBSW] = 1.0, c[SP_B3_PBSWG] = 1.0;
+    c[SP_B3_AS] = 0.0, c[SP_B3_AD] = 0.0, c[SP_B3_PS] = 0.0, c[SP_B3_PD] = 0.0;
 }
 
 // Bsim3Derived (the fields evaluate reads), derived.rs:81-196.
@@ -217,6 +222,53 @@ inline Bsim3Eval bsim3_evaluate(bool pmos, const double* p, const Bsim3Derived& 
     r.vth = sign * vth;
     r.vdsat = vdsat;
     return r;
+}
+
+// Bsim3Derived::junction_cap, derived.rs:323-345
+inline double bsim3_junction_cap(double cj0, double v, double pb, double mj) {
+    const double FC = 0.5;
+    if (cj0 <= 0.0) return 0.0;
+    v = std::fmin(v, pb * 0.95);
+    if (v < FC * pb) {
+        const double ratio = 1.0 - v / pb;
+        return cj0 / std::pow(ratio, mj);
+    }
+    const double f1 = std::pow(1.0 - FC, 1.0 + mj);
+    const double f2 = 1.0 + mj;
+    const double f3 = 1.0 - FC * (1.0 + mj);
+    return cj0 / f1 * (f3 + mj * v / pb / f2);
+}
+
+// evaluate_capacitances, evaluate.rs:82-158 (with derived.rs:122-163 for the
+// overlap capacitances and diffusion estimates): c = cgs, cgd, cgb, cbs, cbd.
+inline void bsim3_capacitances(bool pmos, const double* p, const Bsim3Derived& d, double vds, double vbs,
+                               int region, double* c) {
+    if (pmos) vds = -vds, vbs = -vbs;
+    const double cox_total = d.cox * d.weff * d.leff;
+    double cgs_int = 0.0, cgd_int = 0.0, cgb_int = 0.0;
+    if (region == 0) {
+        cgb_int = cox_total;
+    } else if (region == 1) {
+        const double c_half = cox_total / 2.0;
+        cgs_int = c_half, cgd_int = c_half;
+    } else {
+        cgs_int = cox_total * 2.0 / 3.0;
+    }
+    c[0] = cgs_int + p[SP_B3_CGSO] * d.weff;
+    c[1] = cgd_int + p[SP_B3_CGDO] * d.weff;
+    c[2] = cgb_int + p[SP_B3_CGBO] * d.leff;
+    const double vbd = vbs - vds;
+    const double diff_length = 0.5e-6;
+    const double as_eff = p[SP_B3_AS] > 0.0 ? p[SP_B3_AS] : d.weff * diff_length;
+    const double ad_eff = p[SP_B3_AD] > 0.0 ? p[SP_B3_AD] : d.weff * diff_length;
+    const double ps_eff = p[SP_B3_PS] > 0.0 ? p[SP_B3_PS] : 2.0 * (d.weff + diff_length);
+    const double pd_eff = p[SP_B3_PD] > 0.0 ? p[SP_B3_PD] : 2.0 * (d.weff + diff_length);
+    c[3] = bsim3_junction_cap(p[SP_B3_CJ] * as_eff, vbs, p[SP_B3_PB], p[SP_B3_MJ]) +
+           bsim3_junction_cap(p[SP_B3_CJSW] * ps_eff, vbs, p[SP_B3_PBSW], p[SP_B3_MJSW]) +
+           bsim3_junction_cap(p[SP_B3_CJSWG] * d.weff, vbs, p[SP_B3_PBSWG], p[SP_B3_MJSWG]);
+    c[4] = bsim3_junction_cap(p[SP_B3_CJ] * ad_eff, vbd, p[SP_B3_PB], p[SP_B3_MJ]) +
+           bsim3_junction_cap(p[SP_B3_CJSW] * pd_eff, vbd, p[SP_B3_PBSW], p[SP_B3_MJSW]) +
+           bsim3_junction_cap(p[SP_B3_CJSWG] * d.weff, vbd, p[SP_B3_PBSWG], p[SP_B3_MJSWG]);
 }
 
 }  // namespace oracle

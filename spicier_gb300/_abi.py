@@ -50,7 +50,9 @@ SP_EL_BSIM3N, SP_EL_BSIM3P = 11, 12
 BSIM3_CARD = ("tox", "lint", "wint", "vth0", "k1", "k2", "dvt0", "dvt1", "dvt2", "nfactor",
               "k3", "k3b", "w0", "dvt0w", "dvt1w", "dvt2w", "u0", "ua", "ub", "uc", "vsat",
               "pclm", "pdiblc1", "pdiblc2", "drout", "eta0", "etab", "dsub", "pdiblcb", "pvag",
-              "nch", "tnom", "kt2", "w", "l", "nf")
+              "nch", "tnom", "kt2", "w", "l", "nf",
+              "cgso", "cgdo", "cgbo", "cj", "cjsw", "cjswg", "mj", "mjsw", "mjswg", "pb", "pbsw", "pbswg",
+              "as_", "ad", "ps", "pd")
 SP_B3_CARD = len(BSIM3_CARD)
 SP_MAX_FIELDS = 6
 

@@ -79,7 +79,9 @@ def _bsim3_defaults(pmos: bool) -> Dict[str, float]:
              dvt2w=0.0, u0=250.0 if pmos else 670.0, ua=2.25e-9, ub=5.87e-19, uc=-4.65e-11,
              vsat=1.0e5 if pmos else 1.5e5, pclm=1.3, pdiblc1=0.39, pdiblc2=0.0086, drout=0.56,
              eta0=0.08, etab=-0.07, dsub=0.56, pdiblcb=0.0, pvag=1.0, nch=1.7e17, tnom=300.15,
-             kt2=0.022, w=1e-6, l=100e-9, nf=1.0)
+             kt2=0.022, w=1e-6, l=100e-9, nf=1.0,
+             cgso=0.0, cgdo=0.0, cgbo=0.0, cj=5e-4, cjsw=5e-10, cjswg=0.0, mj=0.5, mjsw=0.33, mjswg=0.33,
+             pb=1.0, pbsw=1.0, pbswg=1.0, as_=0.0, ad=0.0, ps=0.0, pd=0.0)
     assert tuple(d) == abi.BSIM3_CARD
     return d
 
@@ -187,7 +189,8 @@ class Circuit:
     def B3(self, name, d, g, s, b, pmos: bool = False, **card: ParamSpec):
         """BSIM3v3.3 MOSFET (LEVEL=49 / 8): drain, gate, source, bulk.  `card`
         sets any sp_bsim3_card entry by its lower-case name (tox, vth0, u0, ...,
-        w, l, nf; tnom in kelvin), each a value or a distribution; the rest are
+        w, l, nf, cgso, ..., as_, ad, ps, pd; tnom in kelvin), each a value or a
+        distribution; the rest are
         Bsim3Params::{nmos,pmos}_default (mosfet/bsim3/params.rs:160-310).  The
         entries take consecutive parameter slots, the first in field[0]."""
         vals = dict(BSIM3_DEFAULTS[bool(pmos)])

@@ -38,7 +38,24 @@ struct AcLaunch {
     unsigned int* singular; // [count] set when a frequency's matrix was singular
     double* work;           // global interleaved work area, or nullptr (shared memory)
     int refine;             // mixed kernel: FP64 residual refinement steps
+    SoA dv;                 // the DC pass's per-sample derived constants (BSIM3 elements)
 };
+
+// BSIM3 small-signal values at the operating point x (ac_info_at,
+// mosfet/bsim3/mod.rs:296-342): g = gds, gm, gmbs, then cgs, cgd, cgb, cbs, cbd.
+__device__ inline void bsim3_ac_values(const AcLaunch& L, uint64_t s, int e, const sp_element& el, const double* P,
+                                       const double* x, double* g) {
+    auto V = [&](int i) { return i >= 0 ? x[i] : 0.0; };
+    const int off = L.c.doff[e];
+    const auto K = [&](int i) { return L.dv(off + i, s); };
+    const auto C = [&](int k) { return P[el.field[0] + k]; };
+    const bool pm = el.kind == SP_EL_BSIM3P;
+    const double vs = V(el.node[2]);
+    const double vgs = V(el.node[1]) - vs, vds = V(el.node[0]) - vs, vbs = V(el.node[3]) - vs;
+    const Bsim3Out r = bsim3_eval(pm, K, vgs, vds, vbs);
+    g[0] = r.gds, g[1] = r.gm, g[2] = r.gmbs;
+    bsim3_caps(pm, K, C, vds, vbs, r.region, g + 3);
+}
 
 // Per-thread work bytes: exact kernel (FP64 complex matrix + rhs), mixed
 // kernel (FP32 complex matrix + rhs, FP64 x and residual).
@@ -243,6 +260,15 @@ __device__ inline void ac_unit(const AcLaunch& L, uint64_t u, CxArr A) {
                 vccs(a0, a2, a1, a2, o[3]);
                 break;
             }
+            case SP_EL_BSIM3N:
+            case SP_EL_BSIM3P: {  // stampers.rs:423-470: gds, gm and gmbs VCCSs (capacitances below)
+                double g[8];
+                bsim3_ac_values(L, s, e, el, P, x, g);
+                cond(a0, a2, g[0]);
+                vccs(a0, a2, a1, a2, g[1]);
+                vccs(a0, a2, el.node[3], a2, g[2]);
+                break;
+            }
             default:
                 break;
         }
@@ -257,6 +283,17 @@ __device__ inline void ac_unit(const AcLaunch& L, uint64_t u, CxArr A) {
         } else if (el.kind == SP_EL_L) {
             const int br = nn + el.branch;
             A[br * n + br].im() -= wv * P[el.field[0]];
+        } else if (el.kind == SP_EL_BSIM3N || el.kind == SP_EL_BSIM3P) {
+            double g[8];
+            bsim3_ac_values(L, s, e, el, P, x, g);
+            const int d = el.node[0], gt = el.node[1], so = el.node[2], b = el.node[3];
+            const int pr[5][2] = {{gt, so}, {gt, d}, {gt, b}, {b, so}, {b, d}};
+            for (int k = 0; k < 5; ++k) {
+                if (!(g[3 + k] > 0.0)) continue;
+                const double y = wv * g[3 + k];
+                const int i = pr[k][0], j = pr[k][1];
+                ac_add_im(A, n, i, i, y), ac_add_im(A, n, j, j, y), ac_add_im(A, n, i, j, -y), ac_add_im(A, n, j, i, -y);
+            }
         }
     }
     int8_t swap_with[64];
@@ -323,7 +360,10 @@ __device__ inline void ac_elements(const AcLaunch& L, uint64_t s, F visit) {
     for (int e = 0; e < c.num_elements; ++e) {
         const sp_element el = c.el[e];
         const int a0 = el.node[0], a1 = el.node[1], a2 = el.node[2];
-        double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+        double g[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        double& g0 = g[0];
+        double& g1 = g[1];
+        double& g2 = g[2];
         switch (el.kind) {
             case SP_EL_R: g0 = 1.0 / P[el.field[0]]; break;
             case SP_EL_C:
@@ -350,10 +390,12 @@ __device__ inline void ac_elements(const AcLaunch& L, uint64_t s, F visit) {
                 g0 = o[4], g1 = o[5], g2 = o[3];  // gpi, go, gm
                 break;
             }
+            case SP_EL_BSIM3N:
+            case SP_EL_BSIM3P: bsim3_ac_values(L, s, e, el, P, x, g); break;  // gds gm gmbs cgs cgd cgb cbs cbd
             default:
                 break;
         }
-        visit(el, e, g0, g1, g2);
+        visit(el, e, (const double*)g);
     }
 }
 
@@ -378,7 +420,8 @@ __device__ inline void ac_mixed_unit(const AcLaunch& L, uint64_t u, float* fbase
     auto aim = [&](int i, int j, float v) {
         if (i >= 0 && j >= 0) A.im(j * n + i) += v;
     };
-    ac_elements(L, s, [&](const sp_element& el, int, double g0, double g1, double g2) {
+    ac_elements(L, s, [&](const sp_element& el, int, const double* g) {
+        const double g0 = g[0], g1 = g[1], g2 = g[2];
         const int a0 = el.node[0], a1 = el.node[1], a2 = el.node[2];
         switch (el.kind) {
             case SP_EL_R:
@@ -412,6 +455,22 @@ __device__ inline void ac_mixed_unit(const AcLaunch& L, uint64_t u, float* fbase
                 are(a1, a1, gp), are(a2, a2, gp), are(a1, a2, -gp), are(a2, a1, -gp);
                 are(a0, a0, go), are(a2, a2, go), are(a0, a2, -go), are(a2, a0, -go);
                 are(a0, a1, gm), are(a0, a2, -gm), are(a2, a1, -gm), are(a2, a2, gm);
+                break;
+            }
+            case SP_EL_BSIM3N:
+            case SP_EL_BSIM3P: {  // d = a0, g = a1, s = a2, b = node[3]
+                const int a3 = el.node[3];
+                const float gd = (float)g0, gm = (float)g1, gb = (float)g2;
+                are(a0, a0, gd), are(a2, a2, gd), are(a0, a2, -gd), are(a2, a0, -gd);
+                are(a0, a1, gm), are(a0, a2, -gm), are(a2, a1, -gm), are(a2, a2, gm);
+                are(a0, a3, gb), are(a0, a2, -gb), are(a2, a3, -gb), are(a2, a2, gb);
+                const int pr[5][2] = {{a1, a2}, {a1, a0}, {a1, a3}, {a3, a2}, {a3, a0}};
+                for (int k = 0; k < 5; ++k) {
+                    if (!(g[3 + k] > 0.0)) continue;
+                    const float y = (float)(wv * g[3 + k]);
+                    const int i = pr[k][0], j = pr[k][1];
+                    aim(i, i, y), aim(j, j, y), aim(i, j, -y), aim(j, i, -y);
+                }
                 break;
             }
             default:
@@ -516,7 +575,8 @@ __device__ inline void ac_mixed_unit(const AcLaunch& L, uint64_t u, float* fbase
             auto sub = [&](int i, double vr, double vi) {
                 if (i >= 0) r.re(i) -= vr, r.im(i) -= vi;
             };
-            ac_elements(L, s, [&](const sp_element& el, int, double g0, double g1, double g2) {
+            ac_elements(L, s, [&](const sp_element& el, int, const double* g) {
+        const double g0 = g[0], g1 = g[1], g2 = g[2];
                 const int a0 = el.node[0], a1 = el.node[1], a2 = el.node[2];
                 switch (el.kind) {
                     case SP_EL_R:
@@ -556,6 +616,22 @@ __device__ inline void ac_mixed_unit(const AcLaunch& L, uint64_t u, float* fbase
                         const double ici = g1 * (xi(a0) - xi(a2)) + g2 * (xi(a1) - xi(a2));
                         sub(a1, ibr, ibi), sub(a2, -ibr, -ibi);
                         sub(a0, icr, ici), sub(a2, -icr, -ici);
+                        break;
+                    }
+                    case SP_EL_BSIM3N:
+                    case SP_EL_BSIM3P: {  // channel current, then j w C (v_i - v_j) of each capacitance
+                        const int a3 = el.node[3];
+                        const double ir = g0 * (xr(a0) - xr(a2)) + g1 * (xr(a1) - xr(a2)) + g2 * (xr(a3) - xr(a2));
+                        const double ii = g0 * (xi(a0) - xi(a2)) + g1 * (xi(a1) - xi(a2)) + g2 * (xi(a3) - xi(a2));
+                        sub(a0, ir, ii), sub(a2, -ir, -ii);
+                        const int pr[5][2] = {{a1, a2}, {a1, a0}, {a1, a3}, {a3, a2}, {a3, a0}};
+                        for (int k = 0; k < 5; ++k) {
+                            if (!(g[3 + k] > 0.0)) continue;
+                            const double y = wv * g[3 + k];
+                            const int i = pr[k][0], j = pr[k][1];
+                            const double cr = -y * (xi(i) - xi(j)), ci = y * (xr(i) - xr(j));
+                            sub(i, cr, ci), sub(j, -cr, -ci);
+                        }
                         break;
                     }
                     default:

@@ -1282,16 +1282,6 @@ static std::vector<double> ac_grid(const sp_ac_config* c) {
     return f;
 }
 
-// The BSIM3 small-signal model needs its Meyer and junction capacitances
-// (evaluate_capacitances, mosfet/bsim3/evaluate.rs:82-168), which this
-// library does not evaluate: such circuits are refused, not approximated.
-static int ac_no_bsim3(sp_ctx* ctx, const sp_element* el, int num_elements) {
-    for (int e = 0; e < num_elements; ++e)
-        if (el[e].kind == SP_EL_BSIM3N || el[e].kind == SP_EL_BSIM3P)
-            return fail(ctx, SP_ERR_INVALID_ARGUMENT, "element %d: AC sweeps do not model BSIM3 elements", e);
-    return SP_OK;
-}
-
 static int ac_validate(sp_ctx* ctx, const sp_ac_config* c, int n, int num_elements) {
     if (!c) return SP_ERR_INVALID_ARGUMENT;
     if (c->sweep < SP_AC_LIN || c->sweep > SP_AC_OCT) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "unknown sweep type");
@@ -1362,6 +1352,12 @@ static int ac_locked(sp_ctx* ctx, sp_topology* t, const sp_newton_config* dc_cfg
     L.singular = singular;
     L.work = work;
     L.refine = ac->refine > 0 ? ac->refine : 3;
+    {
+        NewtonScratch ns;  // the DC pass's layout: its derived constants are still in place
+        rc = newton_scratch(ctx, t, count, ns);
+        if (rc) return rc;
+        L.dv = SoA{ns.derived, (size_t)count};
+    }
     ProfScope prof(ctx, mixed ? "ac_sweep_mixed" : "ac_sweep_fp64", st);
     if (mixed) SP_CUDA(ctx, launch_ac_mixed(L, grid, block, shared ? per * block : 0, st), "AC launch");
     else SP_CUDA(ctx, launch_ac(L, grid, block, shared ? per * block : 0, st), "AC launch");
@@ -1374,7 +1370,6 @@ int sp_ac_sweep_device(sp_ctx* ctx, const sp_topology* topo, const sp_newton_con
     if (!ctx || !topo || !dc_cfg || !d_probe || !d_status) return SP_ERR_INVALID_ARGUMENT;
     if (topo->ctx != ctx) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "topology belongs to another context");
     int rc = ac_validate(ctx, ac, topo->n, topo->num_elements);
-    if (rc == SP_OK) rc = ac_no_bsim3(ctx, topo->h_elements.data(), topo->num_elements);
     if (rc) return rc;
     if (count == 0) return SP_OK;
     std::lock_guard<std::mutex> g(ctx->mu);
@@ -1389,7 +1384,6 @@ int sp_ac_sweep(sp_ctx* ctx, const sp_circuit* circuit, const sp_newton_config* 
                 double* probe, uint8_t* status) {
     if (!ctx || !circuit || !dc_cfg || !probe || !status) return SP_ERR_INVALID_ARGUMENT;
     int rc = ac_validate(ctx, ac, circuit->num_nodes + circuit->num_branches, circuit->num_elements);
-    if (rc == SP_OK && circuit->elements) rc = ac_no_bsim3(ctx, circuit->elements, circuit->num_elements);
     if (rc) return rc;
     if (count == 0) return SP_OK;
     sp_topology* t = nullptr;

@@ -304,6 +304,52 @@ __host__ __device__ inline Bsim3Out bsim3_eval(bool pmos, KF K, double vgs, doub
     return r;
 }
 
+// Bsim3Derived::junction_cap (derived.rs:323-345), FC = 0.5.
+__host__ __device__ inline double bsim3_junction_cap(double cj0, double v, double pb, double mj) {
+    if (cj0 <= 0.0) return 0.0;
+    v = fmin(v, pb * 0.95);
+    if (v < 0.5 * pb) return cj0 / pow(1.0 - v / pb, mj);
+    const double f1 = pow(1.0 - 0.5, 1.0 + mj), f2 = 1.0 + mj, f3 = 1.0 - 0.5 * (1.0 + mj);
+    return cj0 / f1 * (f3 + mj * v / pb / f2);
+}
+
+// evaluate_capacitances (evaluate.rs:82-158) at the terminal voltages and the
+// region evaluate returned: out = (cgs, cgd, cgb, cbs, cbd).  K reads the
+// per-sample constants, C the card slots.
+template <class KF, class CF>
+__host__ __device__ inline void bsim3_caps(bool pmos, KF K, CF C, double vds, double vbs, int region,
+                                           double* out) {
+    if (pmos) {
+        vds = -vds;
+        vbs = -vbs;
+    }
+    const double weff = K(B3C_WEFF), leff = K(B3C_LEFF);
+    const double cox_total = K(B3C_COX) * weff * leff;
+    double cgs = 0.0, cgd = 0.0, cgb = 0.0;
+    if (region == 0) {
+        cgb = cox_total;
+    } else if (region == 1) {
+        cgs = cox_total / 2.0;
+        cgd = cgs;
+    } else {
+        cgs = cox_total * 2.0 / 3.0;
+    }
+    out[0] = cgs + C(SP_B3_CGSO) * weff;
+    out[1] = cgd + C(SP_B3_CGDO) * weff;
+    out[2] = cgb + C(SP_B3_CGBO) * leff;
+    const double vbd = vbs - vds, diff = 0.5e-6;
+    const double as_e = C(SP_B3_AS) > 0.0 ? C(SP_B3_AS) : weff * diff;
+    const double ad_e = C(SP_B3_AD) > 0.0 ? C(SP_B3_AD) : weff * diff;
+    const double ps_e = C(SP_B3_PS) > 0.0 ? C(SP_B3_PS) : 2.0 * (weff + diff);
+    const double pd_e = C(SP_B3_PD) > 0.0 ? C(SP_B3_PD) : 2.0 * (weff + diff);
+    out[3] = bsim3_junction_cap(C(SP_B3_CJ) * as_e, vbs, C(SP_B3_PB), C(SP_B3_MJ)) +
+             bsim3_junction_cap(C(SP_B3_CJSW) * ps_e, vbs, C(SP_B3_PBSW), C(SP_B3_MJSW)) +
+             bsim3_junction_cap(C(SP_B3_CJSWG) * weff, vbs, C(SP_B3_PBSWG), C(SP_B3_MJSWG));
+    out[4] = bsim3_junction_cap(C(SP_B3_CJ) * ad_e, vbd, C(SP_B3_PB), C(SP_B3_MJ)) +
+             bsim3_junction_cap(C(SP_B3_CJSW) * pd_e, vbd, C(SP_B3_PBSW), C(SP_B3_MJSW)) +
+             bsim3_junction_cap(C(SP_B3_CJSWG) * weff, vbd, C(SP_B3_PBSWG), C(SP_B3_MJSWG));
+}
+
 // Derived per-sample constants of one element from its parameters
 // (P(slot) -> value; out(k, value) stores derived constant k).  The same
 // operation order as the reference's per-call computations, done once.

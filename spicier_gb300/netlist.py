@@ -38,7 +38,7 @@ from typing import Dict, List, Optional, Tuple
 
 from .circuit import BSIM3_DEFAULTS, Circuit, ParamSpec, Pulse
 
-_BSIM3_ALIAS = {"DL": "lint", "DW": "wint", "VTHO": "vth0", "UO": "u0"}
+_BSIM3_ALIAS = {"DL": "lint", "DW": "wint", "VTHO": "vth0", "UO": "u0", "AS": "as_"}
 
 
 def _bsim3_card(mp: Dict[str, float]) -> Dict[str, float]:
@@ -281,9 +281,9 @@ def parse_netlist(text: str, variations: Optional[Dict[str, ParamSpec]] = None) 
             if int(mp.get("LEVEL", 1)) in (8, 49):
                 card = dict(BSIM3_DEFAULTS[pmos])
                 card.update(_bsim3_card(mp))
-                for key in ("W", "L", "NF"):  # instance overrides (parser/elements.rs:455-476)
+                for key in ("W", "L", "NF", "AS", "AD", "PS", "PD"):  # instance overrides (parser/elements.rs:455-476)
                     if key in inst:
-                        card[key.lower()] = inst[key]
+                        card[_BSIM3_ALIAS.get(key, key.lower())] = inst[key]
                 c.B3(name, d, g, s_, bulk, pmos=pmos, **{k: spec(name, k, v) for k, v in card.items()})
                 continue
             vto = mp.get("VTO", -0.7 if pmos else 0.7)

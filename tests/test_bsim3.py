@@ -188,6 +188,39 @@ def test_cmos_chain_oracle():
     assert (mid > 0.0).all() and (mid < 1.8).all() and (out > 0.0).all() and (out <= 1.8 + 1e-9).all()
 
 
+def cs_amp_with_caps():
+    """BSIM3 common-source stage with overlap and junction capacitances, a
+    source-follower BSIM3 load on the output and Monte Carlo thresholds."""
+    c = Circuit("bsim3_cs_ac")
+    c.V("VDD", "vdd", "0", 1.8)
+    c.V("VG", "g", "0", Gauss(0.75, 0.02, 0))
+    c.R("RD", "vdd", "d", Gauss(5e3, 100.0, 1))
+    c.B3("M1", "d", "g", "0", "0", vth0=Gauss(0.4, 0.02, 2), cgso=3e-10, cgdo=3e-10, cgbo=1e-10, cjswg=2e-10)
+    c.B3("M2", "vdd", "d", "out", "0", vth0=Gauss(0.4, 0.02, 3), w=2e-6, cgso=3e-10, cgdo=3e-10)
+    c.R("RS", "out", "0", 20e3)
+    c.nodeset = {"d": 0.9, "out": 0.3}
+    return c
+
+
+def test_ac_low_frequency_gain_matches_dc_model():
+    """At 1 kHz the stage gain is -gm / (gds + 1/RD + load) of the DC model at the
+    operating point; at 100 GHz the capacitances have rolled it off."""
+    circ = cs_amp_with_caps()
+    f = oracle.ac_frequencies(1e3, 1e11, 1, 1)
+    vg = [i for i, e in enumerate(circ.elements) if e["name"] == "VG"][0]
+    h, st = oracle.ac_sweep(circ, abi.newton_config(), 2, 8, f, [circ.node("d")], source=vg)
+    x, _, sx, P = oracle.newton_dc(circ, abi.newton_config(), seed=2, count=8)
+    assert ((st & abi.SP_ST_MASK) == 0).all()
+    base = circ.elements[[e["name"] for e in circ.elements].index("M1")]["field"][0]
+    for k in range(8):
+        cardk = P[k, base:base + abi.SP_B3_CARD]
+        r = ev(cardk, x[k, circ.node("g")], x[k, circ.node("d")], 0.0)
+        # the follower's gate loads nothing at DC: only gds, gm and RD shape the gain
+        gain = -r["gm"] / (r["gds"] + 1.0 / P[k, [i for i, l in enumerate(circ.param_labels) if l == "RD.r"][0]])
+        assert abs(h[k, 0, 0].real - gain) < 1e-6 * abs(gain) and abs(h[k, 0, 0].imag) < 1e-3 * abs(gain)
+        assert abs(h[k, -1, 0]) < 0.5 * abs(gain)
+
+
 # --------------------------------------------------------------------------- GPU
 def random_cards(rng, n, pmos):
     base = oracle.bsim3_default_card(pmos)
@@ -262,8 +295,20 @@ def test_newton_bsim3_against_oracle(ctx):
 
 
 @pytest.mark.gpu
-def test_bsim3_refused_by_ac(ctx):
-    import spicier_gb300 as sg
-    circ = configs.bsim3_cmos_chain()
-    with pytest.raises(sg.SpicierError):
-        ctx.ac_sweep(circ, abi.newton_config(), abi.ac_config(1e3, 1e6, 5), 1, 4)
+@pytest.mark.parametrize("prec", [abi.SP_PREC_FP64, abi.SP_PREC_MIXED])
+def test_ac_sweep_against_oracle(ctx, prec):
+    """BSIM3 small-signal sweeps (gds, gm, gmbs and the Meyer / junction
+    capacitances at each sample's operating point) within 1e-9 of the oracle."""
+    from spicier_gb300.api import Context
+    circ = cs_amp_with_caps()
+    probes = [circ.node("out"), circ.node("d")]
+    cfg = abi.ac_config(1e3, 1e11, 5, abi.SP_AC_DEC, probes, precision=prec)
+    dc = abi.newton_config(precision=abi.SP_PREC_FP64)
+    n = 512
+    h, st = ctx.ac_sweep(circ, dc, cfg, 2, n)
+    with oracle.math_mode("cr"):
+        ho, so = oracle.ac_sweep(circ, dc, 2, n, Context.ac_frequencies(cfg), probes)
+    ok = (so & abi.SP_ST_MASK) == 0
+    assert np.array_equal(st, so) and ok.mean() > 0.99
+    scale = np.abs(ho[ok]).max(axis=1, keepdims=True)
+    assert (np.abs(h[ok] - ho[ok]) <= 1e-9 * scale + 1e-18).all()
