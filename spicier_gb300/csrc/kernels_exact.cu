@@ -33,7 +33,7 @@ __device__ inline double draw_one(const sp_param& p, uint64_t seed, uint32_t swe
 // constants of elements y, y+8, ... from the slots the block just wrote.
 constexpr int kDrawSamples = 32, kDrawLanes = 8;
 
-__global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 3) draw_kernel(DrawLaunch L) {
+__global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_kernel(DrawLaunch L) {
     pdl_wait();
     pdl_trigger();
     const uint64_t s = (uint64_t)blockIdx.x * kDrawSamples + threadIdx.x;
