@@ -312,3 +312,23 @@ def test_ac_sweep_against_oracle(ctx, prec):
     assert np.array_equal(st, so) and ok.mean() > 0.99
     scale = np.abs(ho[ok]).max(axis=1, keepdims=True)
     assert (np.abs(h[ok] - ho[ok]) <= 1e-9 * scale + 1e-18).all()
+
+
+@pytest.mark.gpu
+def test_netlist_bsim3_sweep_on_gpu(ctx):
+    """A BSIM3 netlist with Monte Carlo variations by ELEMENT.field, solved on the
+    GPU and by the oracle from the same text."""
+    nl = parse_netlist("""BSIM3 NMOS Amplifier
+.MODEL NMOD NMOS LEVEL=49 VTH0=0.4 K1=0.5 U0=670 TOX=9e-9 VSAT=1.5e5
+VDD 1 0 DC 3.3
+VGS 2 0 DC 1.0
+RD 1 3 5k
+M1 3 2 0 0 NMOD W=1u L=100n
+.end""", {"M1.vth0": Gauss(0.4, 0.02, 0), "M1.l": Gauss(100e-9, 5e-9, 1), "RD.r": Gauss(5e3, 200.0, 2)})
+    circ = nl.circuit
+    n = 8192
+    r = ctx.newton_dc(circ, abi.newton_config(precision=abi.SP_PREC_FP64), seed=9, count=n)
+    with oracle.math_mode("cr"):
+        xo, io, so, _ = oracle.newton_dc(circ, abi.newton_config(), seed=9, count=n)
+    assert np.array_equal(r.status, so) and ((so & abi.SP_ST_MASK) == 0).all()
+    np.testing.assert_allclose(r.x, xo, rtol=1e-9, atol=1e-15)

@@ -36,16 +36,17 @@ def _bits_equal(a, b):
 
 
 @pytest.mark.parametrize("prec", [abi.SP_PREC_MIXED, abi.SP_PREC_FP64_EXACT])
-def test_static_entry_matches_allocating_entry(product_lib, prec):
+@pytest.mark.parametrize("make,N", [(configs.miller_opamp, 4096), (configs.bsim3_cmos_chain, 2048)])
+def test_static_entry_matches_allocating_entry(product_lib, prec, make, N):
     static = _bind(product_lib)
     ctx = sg.Context(0)
-    circ = configs.miller_opamp()
+    circ = make()
     topo = ctx.topology(circ)
     # the static entry runs the generic kernels (compiling a specialised one
     # would allocate); compare against the same kernels on the allocating side
     ctx.specialize(topo, abi.SP_PREC_MIXED, False)
     cfg = abi.newton_config(precision=prec)
-    N, n = 4096, circ.n
+    n = circ.n
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream().cuda_stream
     errbuf = C.create_string_buffer(256)
