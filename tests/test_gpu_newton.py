@@ -205,3 +205,25 @@ def test_errors_are_statuses(ctx):
     tab.R("R", "a", "0", 1.0)
     with pytest.raises(sg.SpicierError):
         ctx.newton_dc(tab, abi.newton_config(), seed=0, count=4, table=np.zeros((4, 2)))
+
+
+@pytest.mark.parametrize("prec", [MIXED, EXACT])
+def test_host_entry_mapped_output(ctx, prec):
+    """sp_newton_dc with page-locked output buffers (the bench's end-to-end
+    leg): results identical to those copied into pageable buffers."""
+    import ctypes as C
+
+    import torch
+    from spicier_gb300._lib import check, load
+    circ = configs.miller_opamp()
+    N, n = 4096, circ.n
+    cfg = abi.newton_config(precision=prec)
+    r = ctx.newton_dc(circ, cfg, seed=2, count=N, first=777)
+    x = torch.full((N, n), -1.0, dtype=torch.float64).pin_memory()
+    it = torch.zeros(N, dtype=torch.int32).pin_memory()
+    st = torch.zeros(N, dtype=torch.uint8).pin_memory()
+    cc = circ.to_c()
+    check(ctx._ptr, load().sp_newton_dc(ctx._ptr, C.byref(cc), C.byref(cfg), 2, 777, N, None, 0, None,
+                                        x.data_ptr(), it.data_ptr(), st.data_ptr(), None, None, None))
+    assert same_bits(x.numpy(), r.x)
+    assert np.array_equal(it.numpy(), r.iters) and np.array_equal(st.numpy(), r.status)
