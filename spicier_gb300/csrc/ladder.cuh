@@ -370,11 +370,16 @@ __global__ void __launch_bounds__(128, 2) ladder_kernel(LadderLaunch L) {
             if (t + h > c.tstop) h = c.tstop - t;
             const double V = ladder_pulse(c.pulse, t + h);
             const double hg = gamma * h;
+            // MIXED: one reciprocal per step instead of a divide per node (GB300's
+            // FP64 divide is a long FP64-pipe sequence); the other modes keep the
+            // reference's 2 C / (gamma h) per node
+            const bool mx = PREC == SP_PREC_MIXED;
+            const double r_hg = 2.0 / hg;
             for (int k = 1 + lane; k <= N; k += 32) {
                 svp[k] = vp[k];
                 sip[k] = ip[k];
                 svpp[k] = vpp[k];
-                geq[k] = 2.0 * C[k] / hg;
+                geq[k] = mx ? C[k] * r_hg : 2.0 * C[k] / hg;
                 ieq[k] = geq[k] * vp[k] + ip[k];
             }
             for (int k = lane; k <= N + 1; k += 32) xs[k] = x[k];
@@ -387,11 +392,12 @@ __global__ void __launch_bounds__(128, 2) ladder_kernel(LadderLaunch L) {
                 const double denom = 1.0 + 2.0 * rho;
                 const double a1 = (1.0 + rho) * (1.0 + rho) / denom, a2 = -rho * rho / denom,
                              b0 = (1.0 + rho) / denom;
+                const double r_b0h2 = 1.0 / (b0 * h2);
                 for (int k = 1 + lane; k <= N; k += 32) {
                     vpp[k] = vp[k];
-                    ip[k] = 2.0 * C[k] / hg * (xs[k] - vpp[k]) - ip[k];
+                    ip[k] = (mx ? C[k] * r_hg : 2.0 * C[k] / hg) * (xs[k] - vpp[k]) - ip[k];
                     vp[k] = xs[k];
-                    geq[k] = C[k] / (b0 * h2);
+                    geq[k] = mx ? C[k] * r_b0h2 : C[k] / (b0 * h2);
                     ieq[k] = geq[k] * (a1 * vp[k] + a2 * vpp[k]);
                 }
                 __syncwarp();
@@ -418,11 +424,12 @@ __global__ void __launch_bounds__(128, 2) ladder_kernel(LadderLaunch L) {
                 continue;
             }
             double lte = 0.0, ref = 0.0;
+            const double r_h = 1.0 / h, r_2h = 2.0 / h;
             for (int k = 1 + lane; k <= N; k += 32) {
                 const double v_new = xs[k];
-                const double i_trap = 2.0 * C[k] / h * (v_new - svp[k]) - sip[k];
-                const double i_be = C[k] / h * (v_new - svp[k]);
-                lte = fmax(lte, fabs(i_trap - i_be) / 3.0);
+                const double i_trap = (mx ? C[k] * r_2h : 2.0 * C[k] / h) * (v_new - svp[k]) - sip[k];
+                const double i_be = (mx ? C[k] * r_h : C[k] / h) * (v_new - svp[k]);
+                lte = fmax(lte, mx ? fabs(i_trap - i_be) * (1.0 / 3.0) : fabs(i_trap - i_be) / 3.0);
                 ref = fmax(ref, fabs(v_new));
             }
             const double max_lte = warp_max(lte), max_ref = warp_max(ref);
