@@ -332,3 +332,18 @@ M1 3 2 0 0 NMOD W=1u L=100n
         xo, io, so, _ = oracle.newton_dc(circ, abi.newton_config(), seed=9, count=n)
     assert np.array_equal(r.status, so) and ((so & abi.SP_ST_MASK) == 0).all()
     np.testing.assert_allclose(r.x, xo, rtol=1e-9, atol=1e-15)
+
+
+@pytest.mark.gpu
+def test_nonconverging_golden_inverter_matches_oracle(ctx):
+    """The golden inverter netlist (PMOS with source and drain exchanged) fails
+    in the reference's model; the GPU takes the same path through Newton, gmin
+    and source stepping: same status flags and iteration totals as the oracle."""
+    g = json.load(open(GOLDEN))
+    text = [c for c in g["circuits"] if c["name"] == "bsim3_cmos_inverter"][0]["netlist"]
+    circ = parse_netlist(text).circuit
+    r = ctx.newton_dc(circ, abi.newton_config(precision=abi.SP_PREC_FP64_EXACT), seed=1, count=4)
+    with oracle.math_mode("cr"):
+        xo, io, so, _ = oracle.newton_dc(circ, abi.newton_config(), seed=1, count=4)
+    assert (so & abi.SP_ST_MASK == abi.SP_ST_FAILED).all()
+    assert np.array_equal(r.status, so) and np.array_equal(r.iters, io)
