@@ -881,8 +881,12 @@ struct LadderPlan {
 static LadderPlan ladder_plan(const sp_ctx* ctx, const sp_ladder_config* c, uint64_t count) {
     LadderPlan p;
     p.stride = (c->max_sections + 2 + 31) & ~31;
-    p.smem = (size_t)4 * (4 * p.stride + 64) * 8;  // four warps x (diag, rhs, c', d', block unknowns)
-    const int bpsm = std::max(1, std::min(8, (int)((228 * 1024 - 1024) / (p.smem + 1024))));
+    // four warps x (diag, rhs, c', d', block unknowns): FP64 elements, or FP32 in
+    // the mixed mode, whose smaller footprint leaves the SM's L1 to the
+    // per-ladder arrays
+    p.smem = (size_t)4 * ladder_warp_doubles(p.stride, c->precision) * 8;
+    // resident blocks per SM: the kernel's launch bounds allow two (registers), shared memory may allow fewer
+    const int bpsm = std::max(1, std::min(2, (int)((228 * 1024 - 1024) / (p.smem + 1024))));
     p.blocks = std::min<uint64_t>((count + 3) / 4, (uint64_t)ctx->num_sms * bpsm);
     const int bins = c->max_sections - c->min_sections + 1;
     p.bh = align256(4 * (size_t)bins);

@@ -32,6 +32,12 @@ enum LadderArray {
     LA_G, LA_C, LA_VP, LA_IP, LA_VPP, LA_SVP, LA_SIP, LA_SVPP, LA_X, LA_XS, LA_GEQ, LA_IEQ, LA_COUNT
 };
 
+// Shared doubles of one warp's solver scratch: four stride-long arrays of the
+// element type (FP32 in the mixed mode) and 64 block unknowns.
+__host__ __device__ inline int ladder_warp_doubles(int stride, int prec) {
+    return prec == SP_PREC_MIXED ? 2 * stride + 64 : 4 * stride + 64;
+}
+
 struct LadderLaunch {
     sp_ladder_config cfg;
     uint64_t seed, first, count;
@@ -306,14 +312,16 @@ __global__ void __launch_bounds__(128, 2) ladder_kernel(LadderLaunch L) {
     const int slot = blockIdx.x * (blockDim.x >> 5) + wib;
     if (slot >= L.slots) return;
     const sp_ladder_config& c = L.cfg;
-    double* sm = reinterpret_cast<double*>(lsm) + (size_t)wib * (4 * L.stride + 64);
+    const int wd = ladder_warp_doubles(L.stride, PREC);
+    double* sm = reinterpret_cast<double*>(lsm) + (size_t)wib * wd;
     LadderWarp<PREC> W{L, c};
     for (int a = 0; a < LA_COUNT; ++a) W.A[a] = L.ws + ((size_t)slot * LA_COUNT + a) * L.stride;
+    const int ast = PREC == SP_PREC_MIXED ? L.stride / 2 : L.stride;  // doubles per scratch array
     W.sdiag = sm;
-    W.srhs = sm + L.stride;
-    W.scp = sm + 2 * L.stride;
-    W.sdp = sm + 3 * L.stride;
-    W.sfl = sm + 4 * L.stride;
+    W.srhs = sm + ast;
+    W.scp = sm + 2 * ast;
+    W.sdp = sm + 3 * ast;
+    W.sfl = sm + 4 * ast;
     W.lane = lane;
     W.hard = 0;
     W.nvt = c.diode_n * thermal_voltage_300();
