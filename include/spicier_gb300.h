@@ -319,6 +319,18 @@ int sp_ladder_transient_device(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_
                                uint64_t first_index, uint64_t count, double* d_x_final,
                                int32_t* d_n, int32_t* d_accepted, int32_t* d_rejected,
                                int32_t* d_iters, uint8_t* d_status, double* d_probe, void* stream);
+/* sp_ladder_transient_device that also records the size of every accepted
+ * step: d_steps[count][max_steps_recorded] receives instance i's first
+ * max_steps_recorded accepted step sizes in order (d_accepted[i] says how
+ * many were taken); their prefix sums are the accepted time points, the
+ * `time` of each TimePoint in the reference's TransientResult
+ * (crates/spicier-solver/src/transient/result.rs:7-16).  Replaying them through
+ * the same step arithmetic reproduces the run along its own step sequence. */
+int sp_ladder_transient_steps_device(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed,
+                                     uint64_t first_index, uint64_t count, double* d_x_final,
+                                     int32_t* d_n, int32_t* d_accepted, int32_t* d_rejected,
+                                     int32_t* d_iters, uint8_t* d_status, double* d_probe,
+                                     double* d_steps, int32_t max_steps_recorded, void* stream);
 /* Same on host buffers (copies out; synchronises). */
 int sp_ladder_transient(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed, uint64_t first_index,
                         uint64_t count, double* x_final, int32_t* n, int32_t* accepted,
@@ -500,8 +512,12 @@ int sp_newton_dc(sp_ctx* ctx, const sp_circuit* circuit,
  * are rejected with SP_ERR_BATCH_TOO_LARGE.  Runs on the current device.  The
  * first call on a device does a one-time set-up (it looks up the array's
  * address with cudaGetSymbolAddress): make it before any stream capture.
- * All calls on a device share the array, so calls that overlap on the GPU
- * race; order them.  Outputs as for sp_newton_dc_device (no moments); err
+ * Every call copies the circuit from pageable host memory, so a call whose
+ * stream is capturing returns SP_ERR_INVALID_ARGUMENT and enqueues nothing.
+ * The set-up is kept per device ordinal: cudaDeviceReset after the first
+ * call is not supported.  All calls on a device share the array, so calls
+ * that overlap on the GPU race; order them.  Outputs as for
+ * sp_newton_dc_device (no moments); err
  * (optional, err_len bytes) receives a message on failure. */
 int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_config* cfg,
                         uint64_t seed, uint64_t first_index, uint64_t num_samples,
@@ -606,9 +622,11 @@ int sp_mlp_set_io(sp_mlp* mlp, const int32_t* in_slots, const float* in_mean,
  * The network then only has to learn what is not linear in the inputs. */
 int sp_mlp_set_linear(sp_mlp* mlp, const double* lin);
 /* Inference kernel of the warm start.  AUTO picks the tcgen05 kernel (TMEM
- * accumulators, weights resident in shared memory) when the shape allows it
- * (n_in <= 32, n_out <= 32, hidden 64 or 128, 1..4 hidden layers), else the
- * fused mma.sync kernel (hidden <= 256), else the layer-by-layer GEMMs. */
+ * accumulators; weights resident in shared memory for hidden 64 or 128,
+ * streamed from L2 through shared-memory slots for hidden 256) when the
+ * shape allows it (n_in <= 32, n_out <= 32, hidden 64, 128 or 256, 1..4
+ * hidden layers), else the fused mma.sync kernel (hidden <= 256), else the
+ * layer-by-layer GEMMs. */
 enum sp_mlp_kernel {
     SP_MLP_KERNEL_AUTO = 0,
     SP_MLP_KERNEL_TCGEN05 = 1,
@@ -658,6 +676,19 @@ int sp_draw_params_device(sp_ctx* ctx, const sp_topology* topo, uint64_t seed,
                           const double* d_table, uint32_t table_cols,
                           double* d_params, void* stream);
 
+/* The same draws on the host, with the C library's ln, cos and exp, in the
+ * reference's operation order (generate_gaussian_parameters and
+ * gaussian_scaled, rng.rs:120-150 and 208-227): out[num_samples][num_params]
+ * for sweep indices first_index ..  The reference's Gaussian draws are its
+ * host libm's bits, which are not correctly rounded; the device draws are
+ * correctly rounded and agree with glibc in about 99.8 % of draws.  A sweep
+ * given this table (each slot read as a table column) runs on the
+ * reference's own draws on this host.  threads <= 0: all host threads.
+ * Table parameters copy table[i][col] (NaN without a table).  Needs no GPU. */
+int sp_draw_params_host(const sp_circuit* circuit, uint64_t seed, uint64_t first_index,
+                        uint64_t num_samples, const double* table, uint32_t table_cols,
+                        double* out, int threads);
+
 /* Raw hash RNG on device (rng.rs:39-150): out[i] for sweep index
  * first_index + i and parameter param_index.  kind: 0 uniform, 1 gaussian,
  * 2 uniform_f32 (as double), 3 gaussian_f32 (as double). */
@@ -686,6 +717,16 @@ int sp_profile_read(sp_ctx* ctx, sp_kernel_time* out, int cap, int* count);
 int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32_t ld,
                       uint32_t cols, const uint8_t* d_status, sp_moments* d_out,
                       void* stream);
+
+/* StatisticsAccumulator::merge (statistics.rs:148-155) for n unknowns:
+ * acc[i] absorbs other[i] (counts and sums added, min/max combined), as
+ * StreamingStatistics::merge (statistics.rs:548-559) does per node.  This is
+ * how the moments of chunked sweeps, or of the sample ranges of several
+ * processes, combine into the moments of the whole sweep.  The device form
+ * runs on `stream`; the host form needs no GPU. */
+int sp_moments_merge_device(sp_ctx* ctx, sp_moments* d_acc, const sp_moments* d_other,
+                            uint32_t n, void* stream);
+int sp_moments_merge(sp_moments* acc, const sp_moments* other, uint32_t n);
 
 #ifdef __cplusplus
 }

@@ -95,6 +95,8 @@ def _bind(L):
         "or_yield": (None, [P(d), u64, u32, vp_, vp_, u32, P(u64)]),
         "or_ladder_transient": (None, [vp_, u64, u64, u64, P(d), P(i32), P(i32), P(i32), P(i32), P(C.c_uint8),
                                        P(d), i32]),
+        "or_ladder_steps": (None, [vp_, u64, u64, u64, P(d), i32, P(i32), i32]),
+        "or_ladder_replay": (None, [vp_, u64, u64, u64, P(d), i32, P(i32), P(d), P(i32), P(C.c_uint8), P(d), i32]),
         "or_get_math_mode": (i32, []),
         "or_cr_log": (d, [d, P(C.c_uint)]),
         "or_cr_cos": (d, [d, P(C.c_uint)]),
@@ -205,6 +207,34 @@ def ladder_transient(cfg, seed, count, first=0, threads=0):
                           rej.ctypes.data_as(i32p), it.ctypes.data_as(i32p),
                           st.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(pr), threads)
     return dict(x=x, n=n, accepted=acc, rejected=rej, iterations=it, status=st, probe=pr[:, :cfg.num_probe])
+
+
+def ladder_steps(cfg, seed, count, first=0, max_rec=4096, threads=0):
+    """Accepted step sizes of the oracle's adaptive ladder runs: (steps[count][max_rec], nsteps[count])."""
+    steps = np.zeros((count, max_rec))
+    ns = np.zeros(count, np.int32)
+    lib().or_ladder_steps(C.byref(cfg), seed, first, count, _dp(steps), max_rec,
+                          ns.ctypes.data_as(C.POINTER(C.c_int32)), threads)
+    return steps, ns
+
+
+def ladder_replay(cfg, seed, steps, nsteps, first=0, threads=0):
+    """Oracle ladders replayed along recorded accepted step sizes
+    steps[count][max_rec] (nsteps[i] of row i used): dict of x, iterations,
+    status, probe."""
+    L = lib()
+    steps = np.ascontiguousarray(steps, dtype=np.float64)
+    nsteps = np.ascontiguousarray(nsteps, dtype=np.int32)
+    count, max_rec = steps.shape
+    ld = cfg.max_sections + 2
+    x = np.zeros((count, ld))
+    it = np.zeros(count, np.int32)
+    st = np.zeros(count, np.uint8)
+    pr = np.zeros((count, max(cfg.num_probe, 1)))
+    i32p = C.POINTER(C.c_int32)
+    L.or_ladder_replay(C.byref(cfg), seed, first, count, _dp(steps), max_rec, nsteps.ctypes.data_as(i32p), _dp(x),
+                       it.ctypes.data_as(i32p), st.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(pr), threads)
+    return dict(x=x, iterations=it, status=st, probe=pr[:, :cfg.num_probe])
 
 
 def ladder_draw(cfg, seed, inst):

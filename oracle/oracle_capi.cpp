@@ -426,4 +426,41 @@ void or_ladder_transient(const sp_ladder_config* c, uint64_t seed, uint64_t firs
     });
 }
 
+// The accepted step sizes of the adaptive runs of ladders first .. first +
+// count - 1: steps[i][0..min(nsteps[i], max_rec)-1].
+void or_ladder_steps(const sp_ladder_config* c, uint64_t seed, uint64_t first, uint64_t count, double* steps,
+                     int max_rec, int32_t* nsteps, int threads) {
+    const int ld = c->max_sections + 2;
+    parallel_for(count, threads, [&](int, uint64_t lo, uint64_t hi) {
+        std::vector<double> pr(std::max(c->num_probe, 1)), x(ld);
+        for (uint64_t i = lo; i < hi; ++i) {
+            Ladder L = ladder_draw(*c, seed, (uint32_t)(first + i));
+            LadderOutcome o = ladder_transient(*c, L, x.data(), pr.data());
+            nsteps[i] = (int32_t)o.steps.size();
+            for (int k = 0; k < max_rec; ++k) steps[i * (uint64_t)max_rec + k] = k < nsteps[i] ? o.steps[k] : 0.0;
+        }
+    });
+}
+
+// The ladders first .. first + count - 1 replayed along recorded step
+// sequences: steps[i][0..nsteps[i]-1] (row stride max_rec) are instance i's
+// accepted step sizes; outputs as or_ladder_transient (rejected stays 0).
+void or_ladder_replay(const sp_ladder_config* c, uint64_t seed, uint64_t first, uint64_t count, const double* steps,
+                      int max_rec, const int32_t* nsteps, double* x_final, int32_t* iters, uint8_t* status,
+                      double* probe, int threads) {
+    const int ld = c->max_sections + 2;
+    parallel_for(count, threads, [&](int, uint64_t lo, uint64_t hi) {
+        std::vector<double> pr(std::max(c->num_probe, 1));
+        for (uint64_t i = lo; i < hi; ++i) {
+            Ladder L = ladder_draw(*c, seed, (uint32_t)(first + i));
+            const int ns = std::min(std::max(nsteps[i], 0), max_rec);
+            LadderOutcome o = ladder_transient(*c, L, x_final + i * ld, pr.data(), steps + i * (uint64_t)max_rec, ns);
+            for (int k = L.N + 2; k < ld; ++k) x_final[i * ld + k] = 0.0;
+            if (probe) std::copy(pr.begin(), pr.begin() + c->num_probe, probe + i * c->num_probe);
+            iters[i] = o.iterations;
+            status[i] = o.status;
+        }
+    });
+}
+
 }  // extern "C"

@@ -88,6 +88,7 @@ inline Ladder ladder_draw(const sp_ladder_config& c, uint64_t seed, uint32_t ins
 struct LadderOutcome {
     uint8_t status = SP_ST_CONVERGED;
     int32_t accepted = 0, rejected = 0, iterations = 0;
+    std::vector<double> steps;  // accepted step sizes, in order
 };
 
 struct LadderSolver {
@@ -180,7 +181,14 @@ struct LadderSolver {
 };
 
 // One instance: x_final[N+2], probe[num_probe] of v_N.
-inline LadderOutcome ladder_transient(const sp_ladder_config& c, const Ladder& L, double* x_final, double* probe) {
+// Replay (forced != nullptr): the step sizes are forced[0..nforced-1], taken in
+// order with no clamping and no LTE test, every step accepted; everything else
+// is the adaptive run's arithmetic, so a GPU run's recorded accepted steps
+// replayed here give the oracle's result along the GPU's own step sequence.
+// A stage that fails in a replay ends the instance FAILED (a replay cannot
+// retry with a smaller step).
+inline LadderOutcome ladder_transient(const sp_ladder_config& c, const Ladder& L, double* x_final, double* probe,
+                                      const double* forced = nullptr, int nforced = 0) {
     LadderSolver S(c, L);
     const int N = L.N, n = N + 2;
     LadderOutcome out;
@@ -200,13 +208,17 @@ inline LadderOutcome ladder_transient(const sp_ladder_config& c, const Ladder& L
     };
     record(0.0, x.data(), 0.0, x.data());
     int steps = 0;
-    while (t < c.tstop) {
+    while (forced ? out.accepted < nforced : t < c.tstop) {
         if (++steps > c.max_steps) {
             out.status = SP_ST_FAILED;
             break;
         }
-        h = std::min(std::max(h, c.h_min), c.h_max);  // h.clamp(h_min, h_max)
-        if (t + h > c.tstop) h = c.tstop - t;
+        if (forced) {
+            h = forced[out.accepted];
+        } else {
+            h = std::min(std::max(h, c.h_min), c.h_max);  // h.clamp(h_min, h_max)
+            if (t + h > c.tstop) h = c.tstop - t;
+        }
         const double V = eval_pulse(c.pulse, t + h);
         svp = vp;
         sip = ip;
@@ -244,6 +256,10 @@ inline LadderOutcome ladder_transient(const sp_ladder_config& c, const Ladder& L
             out.status = SP_ST_NONFINITE;
             break;
         }
+        if ((it1 < 0 || it2 < 0) && forced) {
+            out.status = SP_ST_FAILED;
+            break;
+        }
         if (it1 < 0 || it2 < 0) {  // a stage's Newton solve failed
             vp = svp;
             ip = sip;
@@ -267,7 +283,7 @@ inline LadderOutcome ladder_transient(const sp_ladder_config& c, const Ladder& L
             max_ref = std::fmax(max_ref, std::fabs(v_new));
         }
         const double tol = std::fmax(c.lte_abstol, c.lte_reltol * max_ref);
-        if (max_lte > tol && h > c.h_min) {
+        if (!forced && max_lte > tol && h > c.h_min) {
             vp = svp;
             ip = sip;
             vpp = svpp;
@@ -286,6 +302,7 @@ inline LadderOutcome ladder_transient(const sp_ladder_config& c, const Ladder& L
             vp[k] = v_new;
         }
         record(t, x.data(), t + h, x2.data());
+        out.steps.push_back(h);
         x = x2;
         t += h;
         ++out.accepted;

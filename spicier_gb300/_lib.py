@@ -112,9 +112,12 @@ def _bind(L):
                                       u32, vp, vp, vp, vp]),
         "sp_transient": (i32, [vp, P(abi.SpCircuit), P(abi.SpNewtonConfig), P(abi.SpTransientConfig), u64, u64, u64, vp, u32, vp,
                                vp, vp]),
+        "sp_draw_params_host": (i32, [P(abi.SpCircuit), u64, u64, u64, vp, u32, vp, i32]),
         "sp_ladder_config_default": (None, [P(abi.SpLadderConfig)]),
         "sp_ladder_transient_device": (i32, [vp, P(abi.SpLadderConfig), u64, u64, u64, vp, vp, vp, vp, vp, vp, vp,
                                              vp]),
+        "sp_ladder_transient_steps_device": (i32, [vp, P(abi.SpLadderConfig), u64, u64, u64, vp, vp, vp, vp, vp,
+                                                   vp, vp, vp, i32, vp]),
         "sp_ladder_transient": (i32, [vp, P(abi.SpLadderConfig), u64, u64, u64, vp, vp, vp, vp, vp, vp, vp]),
         "sp_grid_config_default": (None, [P(abi.SpGridConfig)]),
         "sp_grid_solve_device": (i32, [vp, P(abi.SpGridConfig), u64, u64, u64, vp, vp, vp, vp, vp, vp]),
@@ -122,6 +125,8 @@ def _bind(L):
         "sp_histogram_device": (i32, [vp, vp, u64, u32, u32, vp, d, d, u32, vp, vp]),
         "sp_bsim3_eval_device": (i32, [vp, i32, vp, vp, u64, vp, vp, vp]),
         "sp_yield_device": (i32, [vp, vp, u64, u32, vp, vp, u32, vp, vp]),
+        "sp_moments_merge_device": (i32, [vp, vp, vp, u32, vp]),
+        "sp_moments_merge": (i32, [vp, vp, u32]),
         "sp_profile_enable": (i32, [vp, i32]),
         "sp_profile_read": (i32, [vp, P(SpKernelTime), i32, P(i32)]),
     }

@@ -256,6 +256,32 @@ class Context:
                                                            _vp(accepted), _vp(rejected), _vp(iterations),
                                                            _vp(status), _vp(probe), stream))
 
+    def ladder_transient_steps(self, cfg, seed: int, count: int, first: int = 0, max_steps: int = 4096) -> dict:
+        """ladder_transient plus every instance's accepted step sizes
+        (sp_ladder_transient_steps_device): adds steps [count][max_steps]
+        (row i valid up to accepted[i]).  Runs on the device through torch
+        buffers and copies the results back."""
+        import torch
+        dev = torch.device("cuda", self.device)
+        ld = cfg.max_sections + 2
+        t = dict(x=torch.zeros((count, ld), dtype=torch.float64, device=dev),
+                 n=torch.zeros(count, dtype=torch.int32, device=dev),
+                 accepted=torch.zeros(count, dtype=torch.int32, device=dev),
+                 rejected=torch.zeros(count, dtype=torch.int32, device=dev),
+                 iterations=torch.zeros(count, dtype=torch.int32, device=dev),
+                 status=torch.zeros(count, dtype=torch.uint8, device=dev),
+                 probe=torch.zeros((count, max(cfg.num_probe, 1)), dtype=torch.float64, device=dev),
+                 steps=torch.zeros((count, max_steps), dtype=torch.float64, device=dev))
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        check(self._ptr, load().sp_ladder_transient_steps_device(
+            self._ptr, C.byref(cfg), seed, first, count, _vp(t["x"]), _vp(t["n"]), _vp(t["accepted"]),
+            _vp(t["rejected"]), _vp(t["iterations"]), _vp(t["status"]), _vp(t["probe"]) if cfg.num_probe else None,
+            _vp(t["steps"]), max_steps, stream))
+        torch.cuda.synchronize(dev)
+        out = {k: v.cpu().numpy() for k, v in t.items()}
+        out["probe"] = out["probe"][:, :cfg.num_probe]
+        return out
+
     # -- AC small-signal sweeps ------------------------------------------------
     @staticmethod
     def ac_frequencies(cfg: abi.SpAcConfig) -> np.ndarray:
@@ -470,6 +496,40 @@ class Mlp:
             o += r
             out.append((W, b))
         return out
+
+
+def draw_params_host(circuit: Circuit, seed: int, count: int, first: int = 0, table=None,
+                     threads: int = 0) -> np.ndarray:
+    """Per-sample parameters [count][num_params] drawn on the host with the C
+    library's ln/cos/exp (sp_draw_params_host): the reference's own draw bits
+    on this host (crates/spicier-batched-sweep/src/rng.rs:120-150)."""
+    npar = len(circuit.params)
+    out = np.zeros((count, max(npar, 1)))
+    cols = 0
+    if table is not None:
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        cols = table.shape[1]
+    cc = circuit.to_c()
+    rc = load().sp_draw_params_host(C.byref(cc), seed, first, count, _vp(table), cols, _vp(out), threads)
+    if rc != 0:
+        raise SpicierError(rc, "sp_draw_params_host")
+    return out[:, :npar]
+
+
+def table_circuit(circuit: Circuit) -> Circuit:
+    """A copy of `circuit` whose parameter slot k reads column k of the sweep's
+    table: run it with the table from draw_params_host to sweep on the host
+    libm's draws (same elements, same slots, same nodeset)."""
+    import copy
+    c = copy.copy(circuit)
+    c._c_keepalive = None  # the copy builds its own sp_circuit view
+    c.node_index = dict(circuit.node_index)
+    c.elements = copy.deepcopy(circuit.elements)
+    c.param_labels = list(circuit.param_labels)
+    c.pulses = list(circuit.pulses)
+    c.nodeset = dict(circuit.nodeset)
+    c.params = [(abi.SP_DRAW_TABLE, k, 0.0, 0.0) for k in range(len(circuit.params))]
+    return c
 
 
 def specialized_source(circuit: Circuit, precision: int = abi.SP_PREC_MIXED, compile: bool = False):

@@ -25,6 +25,7 @@ UNITS = {
     "mlp.cu": [],
     "mlp_tc.cu": [],
     "spec.cu": [],
+    "host_draw.cu": [],
 }
 EXTRA_UNITS: dict = {}
 

@@ -108,6 +108,8 @@ int sp_ctx_create(int device, sp_ctx** out) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, 256);
+    if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, 256);
     if (e == cudaSuccess) e = prepare_exact_kernels(ctx->max_smem);
     if (e == cudaSuccess) e = prepare_fast_kernels(ctx->max_smem);
     if (e != cudaSuccess) {
@@ -125,6 +127,7 @@ int sp_ctx_destroy(sp_ctx* ctx) {
     cudaDeviceSynchronize();
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->aux) cudaFree(ctx->aux);
+    if (ctx->counters) cudaFree(ctx->counters);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
     for (auto& r : ctx->recs) {
@@ -521,7 +524,9 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (count > ctx->cfg.max_batch_per_launch)
         return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %llu exceeds maximum %llu",
                     (unsigned long long)count, (unsigned long long)ctx->cfg.max_batch_per_launch);
-    if (count > 0xffffffffull) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "more than 2^32 samples per call");
+    if (count > 0xffffffffull)
+        return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %llu exceeds maximum %llu", (unsigned long long)count,
+                    0xffffffffull);
     if (first_index + count > 0x100000000ull)
         return fail(ctx, SP_ERR_INVALID_ARGUMENT, "sweep index beyond u32 (rng.rs keys sweeps by u32)");
     if (t->has_table && !d_table) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "circuit needs a parameter table");
@@ -546,8 +551,8 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
             return fail(ctx, SP_ERR_INVALID_DIMENSION, "network input slot %d beyond the circuit's %d parameters",
                         mlp_max_slot(warm), t->num_params);
         if (count > mlp_max_rows())
-            return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "learned sweeps take at most %llu samples per call",
-                        (unsigned long long)mlp_max_rows());
+            return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %llu exceeds maximum %llu",
+                        (unsigned long long)count, (unsigned long long)mlp_max_rows());
     }
     NewtonScratch s;
     int rc = newton_scratch(ctx, t, count, s, warm != nullptr);
@@ -622,7 +627,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (d_moments) {
         ProfScope prof(ctx, "moments", st);
         e = launch_moments(d_x, count, (uint32_t)t->n, (uint32_t)t->n, d_status, s.partial, s.moment_blocks,
-                           d_moments, st);
+                           d_moments, st, ctx->counters);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "moments launch");
     }
     return SP_OK;
@@ -807,8 +812,29 @@ int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32
     if (rc) return rc;
     ScratchOrder order(ctx, (cudaStream_t)stream);
     SP_CUDA(ctx, launch_moments(d_values, rows, ld, cols, d_status, (sp_moments*)ctx->scratch, mb, d_out,
-                                (cudaStream_t)stream),
+                                (cudaStream_t)stream, ctx->counters),
             "moments launch");
+    return SP_OK;
+}
+
+int sp_moments_merge_device(sp_ctx* ctx, sp_moments* d_acc, const sp_moments* d_other, uint32_t n, void* stream) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    if (n && (!d_acc || !d_other)) return fail(ctx, SP_ERR_INVALID_ARGUMENT, "null buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    SP_CUDA(ctx, launch_moments_merge(d_acc, d_other, n, (cudaStream_t)stream), "moments merge launch");
+    return SP_OK;
+}
+
+int sp_moments_merge(sp_moments* acc, const sp_moments* other, uint32_t n) {
+    if (n && (!acc || !other)) return SP_ERR_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; ++i) {
+        acc[i].count += other[i].count;
+        acc[i].sum += other[i].sum;
+        acc[i].sum_sq += other[i].sum_sq;
+        acc[i].min = std::fmin(acc[i].min, other[i].min);  // f64::min: a NaN operand gives the other
+        acc[i].max = std::fmax(acc[i].max, other[i].max);
+    }
     return SP_OK;
 }
 
@@ -866,7 +892,9 @@ static int ladder_validate(sp_ctx* ctx, const sp_ladder_config* c, uint64_t coun
         return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad iteration, step or probe counts");
     if (c->precision < SP_PREC_FP64 || c->precision > SP_PREC_FP64_EXACT)
         return fail(ctx, SP_ERR_INVALID_ARGUMENT, "unknown precision");
-    if (count > 0xffffffffull) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "more than 2^32 instances");
+    if (count > 0xffffffffull)
+        return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %llu exceeds maximum %llu", (unsigned long long)count,
+                    0xffffffffull);
     return SP_OK;
 }
 
@@ -898,7 +926,8 @@ static LadderPlan ladder_plan(const sp_ctx* ctx, const sp_ladder_config* c, uint
 
 static int ladder_locked(sp_ctx* ctx, const sp_ladder_config* c, uint64_t seed, uint64_t first, uint64_t count,
                          double* d_x, int32_t* d_n, int32_t* d_acc, int32_t* d_rej, int32_t* d_it, uint8_t* d_st,
-                         double* d_probe, size_t extra, cudaStream_t st) {
+                         double* d_probe, size_t extra, cudaStream_t st, double* d_steps = nullptr,
+                         int max_rec = 0) {
     const LadderPlan p = ladder_plan(ctx, c, count);
     if (p.smem > (size_t)ctx->max_smem) return fail(ctx, SP_ERR_INVALID_DIMENSION, "ladder too long for shared memory");
     const int stride = p.stride;
@@ -925,6 +954,8 @@ static int ladder_locked(sp_ctx* ctx, const sp_ladder_config* c, uint64_t seed, 
     L.iters = d_it;
     L.status = d_st;
     L.probe = d_probe;
+    L.steps = max_rec > 0 ? d_steps : nullptr;
+    L.max_rec = max_rec;
     SP_CUDA(ctx, launch_ladder_prelude(*c, seed, first, count, hist, (uint32_t*)L.order, L.next, st), "ladder order");
     static const char* names[3] = {"ladder_transient_fp64", "ladder_transient_mixed", "ladder_transient_fp64_exact"};
     ProfScope prof(ctx, names[c->precision], st);
@@ -950,6 +981,26 @@ int sp_ladder_transient_device(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_
     ScratchOrder order(ctx, (cudaStream_t)stream);
     return ladder_locked(ctx, cfg, seed, first_index, count, d_x_final, d_n, d_accepted, d_rejected, d_iters,
                          d_status, cfg->num_probe ? d_probe : nullptr, 0, (cudaStream_t)stream);
+}
+
+int sp_ladder_transient_steps_device(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed, uint64_t first_index,
+                                     uint64_t count, double* d_x_final, int32_t* d_n, int32_t* d_accepted,
+                                     int32_t* d_rejected, int32_t* d_iters, uint8_t* d_status, double* d_probe,
+                                     double* d_steps, int32_t max_steps_recorded, void* stream) {
+    if (!ctx) return SP_ERR_INVALID_ARGUMENT;
+    int rc = ladder_validate(ctx, cfg, count);
+    if (rc) return rc;
+    if (max_steps_recorded < 0 || (max_steps_recorded > 0 && !d_steps))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad step record buffer");
+    if (count == 0) return SP_OK;
+    if (!d_x_final || !d_n || !d_accepted || !d_rejected || !d_iters || !d_status || (cfg->num_probe && !d_probe))
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT, "missing output buffer");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ScratchOrder order(ctx, (cudaStream_t)stream);
+    return ladder_locked(ctx, cfg, seed, first_index, count, d_x_final, d_n, d_accepted, d_rejected, d_iters,
+                         d_status, cfg->num_probe ? d_probe : nullptr, 0, (cudaStream_t)stream, d_steps,
+                         max_steps_recorded);
 }
 
 int sp_ladder_transient(sp_ctx* ctx, const sp_ladder_config* cfg, uint64_t seed, uint64_t first_index,
@@ -1009,7 +1060,9 @@ static int grid_validate(sp_ctx* ctx, const sp_grid_config* c, uint64_t count) {
         return fail(ctx, SP_ERR_INVALID_ARGUMENT, "precision must be SP_PREC_FP64 or SP_PREC_MIXED");
     if (!(c->r_lo > 0) || !(c->r_hi >= c->r_lo) || !(c->krylov_tol > 0))
         return fail(ctx, SP_ERR_INVALID_ARGUMENT, "bad resistance range or tolerance");
-    if (count > 0x7fffffffull) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "too many instances");
+    if (count > 0x7fffffffull)
+        return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %llu exceeds maximum %llu", (unsigned long long)count,
+                    0x7fffffffull);
     const size_t smem = grid_smem_bytes(*c, c->precision == SP_PREC_MIXED ? 4 : 8);
     if (smem > (size_t)ctx->max_smem) return fail(ctx, SP_ERR_INVALID_DIMENSION, "grid too large for shared memory");
     return SP_OK;
@@ -1091,7 +1144,9 @@ int sp_grid_solve(sp_ctx* ctx, const sp_grid_config* cfg, uint64_t seed, uint64_
 int sp_bsim3_eval_device(sp_ctx* ctx, int pmos, const double* d_card, const double* d_bias, uint64_t count,
                          double* d_out, uint8_t* d_region, void* stream) {
     if (!ctx || (count && (!d_card || !d_bias || !d_out))) return SP_ERR_INVALID_ARGUMENT;
-    if (count > ((uint64_t)1 << 40)) return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "at most 2^40 devices per call");
+    if (count > ((uint64_t)1 << 40))
+        return fail(ctx, SP_ERR_BATCH_TOO_LARGE, "Batch size %llu exceeds maximum %llu", (unsigned long long)count,
+                    1ull << 40);
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaSetDevice(ctx->device);
     ProfScope prof(ctx, "bsim3_eval", (cudaStream_t)stream);

@@ -73,9 +73,12 @@ cudaError_t launch_newton_fast(int prec, const NewtonLaunch& L, bool fallback, i
                                size_t smem, cudaStream_t st);
 cudaError_t launch_lu_batch_mixed(const double* mats, const double* rhs, int n, uint64_t batch,
                                   double* sol, uint8_t* sing, int refine_steps, cudaStream_t st);
+// counter: a zero-initialised word of the context (the single-pass kernel's
+// arrival counter, reset by the kernel), or nullptr for the two-kernel path.
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
-                           cudaStream_t st);
+                           cudaStream_t st, unsigned int* counter = nullptr);
+cudaError_t launch_moments_merge(sp_moments* acc, const sp_moments* other, uint32_t n, cudaStream_t st);
 cudaError_t prepare_fast_kernels(int max_smem);
 
 // Largest dense size of the thread-per-sample Newton kernels.
@@ -131,6 +134,9 @@ struct sp_ctx {
     // owns `scratch`) and keep their own data across it
     void* aux = nullptr;
     size_t aux_bytes = 0;
+    // zero-initialised device words: [0] the single-pass moments kernel's
+    // arrival counter (each launch leaves it at zero)
+    unsigned int* counters = nullptr;
 };
 
 // Brackets one kernel launch with events when the context is profiling.

@@ -53,6 +53,8 @@ struct LadderLaunch {
     int32_t* iters;
     uint8_t* status;
     double* probe;          // [count][num_probe] or nullptr
+    double* steps;          // [count][max_rec] accepted step sizes, or nullptr
+    int max_rec;            // steps recorded per instance (the first max_rec)
 };
 
 __host__ __device__ inline int ladder_sections(const sp_ladder_config& c, uint64_t seed, uint32_t inst) {
@@ -462,6 +464,7 @@ __global__ void __launch_bounds__(128, 2) ladder_kernel(LadderLaunch L) {
             for (int k = lane; k <= N + 1; k += 32) x[k] = xs[k];
             __syncwarp();
             record(t, xa, t + h, xb);
+            if (L.steps && lane == 0 && accepted < L.max_rec) L.steps[(size_t)i * L.max_rec + accepted] = h;
             t += h;
             ++accepted;
             if (max_lte < tol * 0.5 && h < c.h_max) h *= fmin(fmin(sqrt(tol / fmax(max_lte, 1e-20)), 2.0), 1.5);

@@ -13,6 +13,7 @@
 #include <cuda_bf16.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -897,7 +898,12 @@ int sp_mlp_set_io(sp_mlp* m, const int32_t* in_slots, const float* in_mean, cons
 int sp_mlp_forward_device(sp_mlp* m, const float* d_x, uint64_t rows, float* d_y, void* stream) {
     if (!m || !d_x || !d_y) return SP_ERR_INVALID_ARGUMENT;
     if (rows == 0) return SP_OK;
-    if (rows > kMaxRows) return mlp_fail(m->ctx, SP_ERR_BATCH_TOO_LARGE, "more than 2^22 rows");
+    if (rows > kMaxRows) {
+        char msg[96];
+        snprintf(msg, sizeof msg, "Batch size %llu exceeds maximum %llu", (unsigned long long)rows,
+                 (unsigned long long)kMaxRows);
+        return mlp_fail(m->ctx, SP_ERR_BATCH_TOO_LARGE, msg);
+    }
     std::lock_guard<std::mutex> g(m->ctx->mu);
     cudaSetDevice(m->ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
@@ -991,7 +997,7 @@ extern "C" int sp_mlp_set_inference_kernel(sp_mlp* m, int kind) {
     if (!m || kind < SP_MLP_KERNEL_AUTO || kind > SP_MLP_KERNEL_LAYERED) return SP_ERR_INVALID_ARGUMENT;
     if (kind == SP_MLP_KERNEL_TCGEN05 && !sp::tc_eligible(m))
         return mlp_fail(m->ctx, SP_ERR_INVALID_DIMENSION,
-                        "tcgen05 inference needs n_in <= 32, n_out <= 32, hidden 64 or 128, 1..4 hidden layers");
+                        "tcgen05 inference needs n_in <= 32, n_out <= 32, hidden 64, 128 or 256, 1..4 hidden layers");
     if (kind == SP_MLP_KERNEL_MMA_SYNC && !(m->H <= FH && m->L <= 9))
         return mlp_fail(m->ctx, SP_ERR_INVALID_DIMENSION, "the fused mma.sync kernel needs hidden <= 256");
     std::lock_guard<std::mutex> g(m->ctx->mu);

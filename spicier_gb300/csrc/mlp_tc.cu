@@ -29,10 +29,35 @@
 // restarts those samples cold), raises the error flag, and the CTA frees
 // its TMEM before it returns.
 //
-// Scope: n_in <= 32, n_out <= 32, hidden width 64 or 128, 1..4 hidden layers;
-// the mma.sync kernel in mlp.cu serves every other shape.
+// Hidden width 256 (stream_kernel): the weights (304 KB for 10 -> 3x256 ->
+// 12) no longer fit in shared memory, so they stream from L2 through a ring
+// of 16 KB slots, each one K-block (64 K) of 128 weight rows (or the whole
+// K-block of the 32-row output layer).  Roles per CTA (576 threads):
+//   producer warp  one thread walks the CTA's fixed unit sequence and copies
+//                  each unit into the next free slot with the TMA unit
+//                  (full[slot] completes on the bytes, empty[slot] on the
+//                  MMAs that read it);
+//   MMA warp       one thread issues, for each (tile, layer) job in the
+//                  same order, one tcgen05.mma (M = 128, N = unit rows,
+//                  K = 16) per 16 K of every unit, commits each unit to its
+//                  empty barrier and the job to the team's accumulator
+//                  barrier;
+//   two teams      of eight warps (warp w reads TMEM lanes 32 (w % 4) ..
+//                  and column half (w / 4) % 2) each own a 128-sample tile,
+//                  a 64 KB activation buffer and 256 TMEM columns, and run
+//                  the epilogue of one layer while the tensor cores run the
+//                  other team's layer: jobs alternate team 0 / team 1 layer
+//                  by layer, so the MMA chain of one tile overlaps the
+//                  bias + GELU + BF16 repack of the other.
+// The weights never depend on the activations, so the producer runs ahead of
+// the MMA warp by the ring's depth across layers and tiles.
+//
+// Scope: n_in <= 32, n_out <= 32, hidden width 64, 128 or 256, 1..4 hidden
+// layers; the mma.sync kernel in mlp.cu serves every other shape.
 #include <cuda_bf16.h>
 #include <stdint.h>
+
+#include <mutex>
 
 #include "mlp_act.cuh"
 #include "mlp_tc.h"
@@ -392,11 +417,320 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
                      : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Hidden width 256: weights streamed from L2 (see the file comment).
+constexpr int kSTeams = 2;                            // tiles in flight per CTA
+constexpr int kSTeamWarps = 8;                        // warps per team
+constexpr int kSTeamThreads = kSTeamWarps * 32;       // 256
+constexpr int kSProducerWarp = kSTeams * kSTeamWarps;  // warp 16
+constexpr int kSIssuerWarp = kSProducerWarp + 1;       // warp 17
+constexpr int kSThreads = (kSIssuerWarp + 1) * 32;     // 576
+constexpr uint32_t kSUnit = 16384;                    // one ring slot: 128 rows x 64 K of BF16
+constexpr uint32_t kSAbytes = 128u * 256u * 2u;       // one activation tile: 128 samples x 256 BF16
+constexpr int kSMaxSlots = 6;
+
+struct SCarve {
+    uint32_t abuf, ring, bias, lin, io, slots, mbar, flag, tslot, total;
+};
+
+__host__ __device__ inline SCarve scarve(const Args& a, int nslots) {
+    SCarve c;
+    c.abuf = 0;  // kSTeams x kSAbytes, 1024-aligned
+    c.ring = kSTeams * kSAbytes;
+    c.bias = c.ring + (uint32_t)nslots * kSUnit;
+    c.lin = c.bias + 4u * (uint32_t)a.bias_total;
+    c.io = c.lin + 4u * (uint32_t)(a.n_out * a.n_in);
+    c.slots = c.io + 4u * (uint32_t)(2 * (a.n_in + a.n_out));
+    c.mbar = (c.slots + 4u * (uint32_t)a.n_in + 7u) & ~7u;  // full[6], empty[6], ready[2], acc[2]
+    c.flag = c.mbar + 8u * (2 * kSMaxSlots + 2 * kSTeams);
+    c.tslot = c.flag + 16u;
+    c.total = c.tslot + 16u;
+    return c;
+}
+
+__host__ __device__ inline int stream_slots(const Args& a) {
+    for (int s = kSMaxSlots; s >= 2; --s)
+        if (1024u + scarve(a, s).total <= kSmemLimit) return s;
+    return 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
+// Bounded wait that also gives up when another role of the CTA has raised
+// the abort flag (and raises it itself on a timeout).
+__device__ __forceinline__ bool mbar_wait_ab(uint32_t mbar, uint32_t parity, volatile int* abort_flag) {
+    const long long t0 = clock64();
+    while (!mbar_try(mbar, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void team_sync_n(int id, int n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ bool team_all_n(int id, int n, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.b32 q, %1, 0;\n\t"
+        "bar.red.and.pred p, %2, %3, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
+
+// Units of layer ly: ceil(N / 128) row halves x Kp / 64 K-blocks, the row
+// half outer; unit u covers rows nh*128 .. of K-block kb.
+__device__ __forceinline__ int layer_units(const Layer& ly) { return ((ly.N + 127) / 128) * (ly.Kp / 64); }
+
+__global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    pdl_wait();  // the drawn parameters (and the packed weights) are complete and visible
+    pdl_trigger();
+    unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    const SCarve cv = scarve(a, nslots);
+    float* bias_s = reinterpret_cast<float*>(sm + cv.bias);
+    float* lin_s = reinterpret_cast<float*>(sm + cv.lin);
+    float* io_s = reinterpret_cast<float*>(sm + cv.io);
+    int* slots_s = reinterpret_cast<int*>(sm + cv.slots);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + cv.mbar);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + cv.flag);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + cv.tslot);
+    const uint32_t full0 = smem_u32(&mbar[0]), empty0 = smem_u32(&mbar[kSMaxSlots]);
+    const uint32_t ready0 = smem_u32(&mbar[2 * kSMaxSlots]), acc0 = smem_u32(&mbar[2 * kSMaxSlots + kSTeams]);
+    const uint32_t ring_s = smem_u32(sm + cv.ring);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int t = 0; t < 2 * kSMaxSlots + 2 * kSTeams; ++t)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[t])) : "memory");
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = tid; i < a.bias_total; i += kSThreads) bias_s[i] = a.bias[i];
+    for (int i = tid; i < a.n_out * a.n_in; i += kSThreads) lin_s[i] = a.lin ? a.lin[i] : 0.f;
+    for (int i = tid; i < 2 * (a.n_in + a.n_out); i += kSThreads)
+        io_s[i] = (i >= a.n_in && i < 2 * a.n_in) ? 1.0f / a.io[i] : a.io[i];
+    for (int i = tid; i < a.n_in; i += kSThreads) slots_s[i] = a.slots[i];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(512u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = *tmem_slot;
+    const int ntiles = (a.rows + kTile - 1) / kTile;
+    // this CTA's tiles: k-th = blockIdx.x + k gridDim.x; tile k belongs to team k % 2
+    const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+
+    if (warp == kSProducerWarp) {
+        if (lane == 0) {
+            uint32_t g = 0;
+            bool ok = true;
+            for (int k2 = 0; ok && k2 < my_tiles; k2 += kSTeams)
+                for (int l = 0; ok && l < a.L; ++l)
+                    for (int T = 0; ok && T < kSTeams; ++T) {
+                        if (k2 + T >= my_tiles) continue;
+                        const Layer& ly = a.layer[l];
+                        const int kbs = ly.Kp / 64, nu = layer_units(ly);
+                        for (int u = 0; u < nu; ++u, ++g) {
+                            const int nh = u / kbs, kb = u % kbs;
+                            const uint32_t slot = g % (uint32_t)nslots;
+                            if (!mbar_wait_ab(empty0 + 8 * slot, ((g / nslots) & 1u) ^ 1u, abort_flag)) {
+                                ok = false;
+                                break;
+                            }
+                            const int rows_u = min(128, ly.N - nh * 128);
+                            const uint32_t bytes = (uint32_t)rows_u * 128u;
+                            mbar_expect_tx(full0 + 8 * slot, bytes);
+                            bulk_g2s(ring_s + slot * kSUnit,
+                                     static_cast<const unsigned char*>(a.img) + ly.img_off + (size_t)kb * ly.N * 128 +
+                                         (size_t)nh * 128 * 128,
+                                     bytes, full0 + 8 * slot);
+                        }
+                    }
+            if (!ok) {
+                // copies still in flight land before the CTA releases its shared memory
+                const uint32_t n_in_flight = g < (uint32_t)nslots ? g : (uint32_t)nslots;
+                for (uint32_t j = g - n_in_flight; j < g; ++j) {
+                    const long long t0 = clock64();
+                    while (!mbar_try(full0 + 8 * (j % nslots), (j / nslots) & 1u))
+                        if (clock64() - t0 > kWaitCycles) break;
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == kSIssuerWarp) {
+        if (lane == 0) {
+            uint32_t g = 0, jobs[kSTeams] = {0u, 0u};
+            bool ok = true;
+            for (int k2 = 0; ok && k2 < my_tiles; k2 += kSTeams)
+                for (int l = 0; ok && l < a.L; ++l)
+                    for (int T = 0; ok && T < kSTeams; ++T) {
+                        if (k2 + T >= my_tiles) continue;
+                        // team T's activations for layer l are in its buffer (and its
+                        // previous accumulator has been read)
+                        if (!mbar_wait_ab(ready0 + 8 * T, jobs[T] & 1u, abort_flag)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_after();
+                        const Layer& ly = a.layer[l];
+                        const int kbs = ly.Kp / 64, nu = layer_units(ly);
+                        const uint32_t abuf_s = smem_u32(sm + cv.abuf) + (uint32_t)T * kSAbytes;
+                        for (int u = 0; u < nu; ++u, ++g) {
+                            const int nh = u / kbs, kb = u % kbs;
+                            const uint32_t slot = g % (uint32_t)nslots;
+                            if (!mbar_wait_ab(full0 + 8 * slot, (g / nslots) & 1u, abort_flag)) {
+                                ok = false;
+                                break;
+                            }
+                            tc_after();
+                            const int rows_u = min(128, ly.N - nh * 128);
+                            const uint32_t id = idesc_bf16(rows_u);
+                            const uint32_t d = tmem + (uint32_t)(T * 256 + nh * 128);
+                            const uint32_t ab = abuf_s + (uint32_t)kb * (kTile * 128), bb = ring_s + slot * kSUnit;
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                mma_bf16_ss(d, sdesc(ab + k * 32), sdesc(bb + k * 32), id, (kb | k) != 0);
+                            mma_commit(empty0 + 8 * slot);  // the slot is free once these MMAs complete
+                        }
+                        if (!ok) break;
+                        mma_commit(acc0 + 8 * T);  // the job's accumulator is complete
+                        ++jobs[T];
+                    }
+        }
+        __syncwarp();
+    } else {
+        // team T: warps 8T .. 8T+7; warp w reads TMEM lanes 32 (w % 4) .. and column half (w / 4) % 2
+        const int T = warp / kSTeamWarps, wt = warp % kSTeamWarps, quarter = wt & 3, ch = wt >> 2;
+        const int row = quarter * 32 + lane, bar_id = 1 + T;
+        unsigned char* abuf = sm + cv.abuf + (uint32_t)T * kSAbytes;
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16, acc_b = acc0 + 8 * T;
+        const float* in_mean = io_s;
+        const float* in_rscale = io_s + a.n_in;
+        const float* out_mean = io_s + 2 * a.n_in;
+        const float* out_scale = out_mean + a.n_out;
+        uint32_t jobs = 0;
+        bool ok = true;
+        int k = T;
+        for (; k < my_tiles; k += kSTeams) {
+            const int tile = (int)blockIdx.x + k * (int)gridDim.x;
+            const int s = tile * kTile + row;
+            const bool live = s < a.rows;
+            if (ch == 0) {
+                // inputs of row `row`: K-block 0, chunks 0..3 data, 4..7 zero
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    uint32_t w[4];
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) {
+                        const int j = c * 8 + 2 * h;
+                        const float x0v = (j < a.n_in && live)
+                                              ? (f64_to_f32(a.params_soa[(size_t)slots_s[j] * a.stride + s]) -
+                                                 in_mean[j]) * in_rscale[j]
+                                              : 0.f;
+                        const float x1v = (j + 1 < a.n_in && live)
+                                              ? (f64_to_f32(a.params_soa[(size_t)slots_s[j + 1] * a.stride + s]) -
+                                                 in_mean[j + 1]) * in_rscale[j + 1]
+                                              : 0.f;
+                        w[h] = pack2(x0v, x1v);
+                    }
+                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+                }
+#pragma unroll
+                for (int c = 4; c < 8; ++c)
+                    *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(0u, 0u, 0u, 0u);
+            }
+            for (int l = 0; l < a.L; ++l) {
+                // this layer's A operand is written (and the accumulator read): hand it to the MMA warp
+                fence_async_smem();
+                tc_before();
+                team_sync_n(bar_id, kSTeamThreads);
+                if (wt == 0 && lane == 0) mbar_arrive(ready0 + 8 * T);
+                ok = team_all_n(bar_id, kSTeamThreads, mbar_wait_ab(acc_b, jobs & 1u, abort_flag));
+                ++jobs;
+                if (!ok) break;
+                tc_after();
+                const Layer& ly = a.layer[l];
+                const float* bias = bias_s + ly.bias_off;
+                if (l + 1 < a.L) {
+                    const int half = ly.N / 2;  // columns per column half (128 for H = 256)
+                    for (int c0 = ch * half; c0 < (ch + 1) * half; c0 += 32) {
+                        float v[32];
+                        tmem_ld32(tmem + lane_base + (uint32_t)(T * 256 + c0), v);
+                        uint32_t w[16];
+#pragma unroll
+                        for (int i = 0; i < 16; ++i)
+                            w[i] = pack2(act::gelu(v[2 * i] + bias[c0 + 2 * i]),
+                                         act::gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8 + q)) =
+                                make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+                    }
+                } else if (ch == 0) {
+                    float v[32];
+                    tmem_ld32(tmem + lane_base + (uint32_t)(T * 256), v);  // the output layer is 32 wide
+                    if (live) {
+                        // x[o] = out_mean + out_scale (y + b), then the linear term input by
+                        // input (the centred inputs are re-read: they were not kept live)
+#pragma unroll
+                        for (int o = 0; o < 32; ++o)
+                            v[o] = o < a.n_out ? out_mean[o] + out_scale[o] * (v[o] + bias[o]) : 0.f;
+                        for (int j = 0; j < a.n_in; ++j) {
+                            const float pj = f64_to_f32(a.params_soa[(size_t)slots_s[j] * a.stride + s]) - in_mean[j];
+#pragma unroll
+                            for (int o = 0; o < 32; ++o)
+                                if (o < a.n_out) v[o] = fmaf(lin_s[o * a.n_in + j], pj, v[o]);
+                        }
+#pragma unroll
+                        for (int o = 0; o < 32; ++o)
+                            if (o < a.n_out) a.x0[(size_t)s * a.n_out + o] = f32_to_f64(v[o]);
+                    }
+                }
+            }
+            if (!ok) break;
+        }
+        if (!ok) {
+            // timeout: this team's remaining samples start cold (NaN warm start)
+            if (wt == 0 && lane == 0) atomicExch(a.err, 1);
+            if (ch == 0)
+                for (; k < my_tiles; k += kSTeams) {
+                    const int s = ((int)blockIdx.x + k * (int)gridDim.x) * kTile + row;
+                    if (s < a.rows)
+                        for (int o = 0; o < a.n_out; ++o)
+                            a.x0[(size_t)s * a.n_out + o] = __longlong_as_double(0x7ff8000000000000LL);
+                }
+        }
+    }
+    // every MMA has completed (its team waited on the commit, or everything
+    // gave up after a bounded wait) and no copy is in flight
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+}
+
 }  // namespace
 
 bool supported(int n_in, int n_out, int hidden, int gemm_layers) {
-    return n_in >= 1 && n_in <= kMaxIn && n_out >= 1 && n_out <= 32 && (hidden == 64 || hidden == 128) &&
-           gemm_layers >= 2 && gemm_layers <= kMaxLayers;
+    return n_in >= 1 && n_in <= kMaxIn && n_out >= 1 && n_out <= 32 &&
+           (hidden == 64 || hidden == 128 || hidden == 256) && gemm_layers >= 2 && gemm_layers <= kMaxLayers;
 }
 
 int plan(int n_in, int n_out, int hidden, int gemm_layers, Args* a) {
@@ -419,7 +753,13 @@ int plan(int n_in, int n_out, int hidden, int gemm_layers, Args* a) {
     return off;
 }
 
+static bool streams(const Args& a) { return a.layer[0].N == 256; }
+
 size_t smem_bytes(const Args& a) {
+    if (streams(a)) {
+        const int s = stream_slots(a);
+        return s ? 1024 + (size_t)scarve(a, s).total : 0;
+    }
     const int t = teams_for(a);
     return t ? 1024 + (size_t)carve(a, t).total : 0;
 }
@@ -434,19 +774,38 @@ cudaError_t pack(const __nv_bfloat16* wt, const size_t* woff, const Args& a, voi
     return cudaGetLastError();
 }
 
-cudaError_t launch(const Args& a, int num_sms, cudaStream_t st) {
+// Raises the kernels' dynamic shared-memory limit once per device.
+static cudaError_t configure_device() {
+    static std::mutex mu;
     static bool configured[64] = {};
     int dev = 0;
-    cudaGetDevice(&dev);
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    if (dev >= 0 && dev < 64 && configured[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(stream_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = true;
+    return e;
+}
+
+cudaError_t launch(const Args& a, int num_sms, cudaStream_t st) {
+    cudaError_t e = configure_device();
+    if (e != cudaSuccess) return e;
+    const int ntiles = (a.rows + kTile - 1) / kTile;
+    if (streams(a)) {
+        const int nslots = stream_slots(a);
+        if (nslots == 0) return cudaErrorInvalidValue;
+        const size_t smem = 1024 + (size_t)scarve(a, nslots).total;
+        // one CTA per SM; a CTA takes tiles blockIdx.x + k gridDim.x
+        int grid = ntiles < num_sms ? ntiles : num_sms;
+        if (grid < 1) return cudaSuccess;
+        return launch_chained(stream_kernel, dim3(grid), dim3(kSThreads), smem, st, a, nslots);
+    }
     const int teams = teams_for(a);
     if (teams == 0) return cudaErrorInvalidValue;
     const size_t smem = 1024 + (size_t)carve(a, teams).total;
-    if (dev < 64 && !configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
-        if (e != cudaSuccess) return e;
-        configured[dev] = true;
-    }
-    const int ntiles = (a.rows + kTile - 1) / kTile;
     int grid = (ntiles + teams - 1) / teams;
     if (grid > num_sms) grid = num_sms;
     if (grid < 1) return cudaSuccess;

@@ -35,8 +35,9 @@ struct Args {
     Layer layer[kMaxLayers];
 };
 
-// Shapes this kernel runs: n_in <= 32, n_out <= 32, hidden 64 or 128,
-// 2..5 GEMM layers.
+// Shapes these kernels run: n_in <= 32, n_out <= 32, 2..5 GEMM layers, and
+// hidden width 64 or 128 (every weight resident in shared memory) or 256
+// (weights streamed from L2 through a ring of shared-memory slots).
 bool supported(int n_in, int n_out, int hidden, int gemm_layers);
 // Fills the layer table of `a` (and n_in, n_out); returns the image size.
 int plan(int n_in, int n_out, int hidden, int gemm_layers, Args* a);

@@ -19,6 +19,12 @@
 //  * All calls on a device share the one array, which keeps the contents of
 //    the last call.  Calls whose work overlaps on the GPU (different streams,
 //    or different host threads without ordering) race on it; order them.
+//  * Every call copies the circuit from pageable host memory, so a call
+//    whose stream is capturing returns SP_ERR_INVALID_ARGUMENT and enqueues
+//    nothing.
+//  * The set-up is kept per device ordinal for the life of the process;
+//    cudaDeviceReset after the first call is not supported (the cached
+//    symbol address and kernel attributes belong to the destroyed context).
 //  * The caller passes inputs and outputs (device pointers) as for
 //    sp_newton_dc_device; sweeps that need more scratch than the array holds
 //    are rejected with SP_ERR_BATCH_TOO_LARGE and a message giving the limit.
@@ -180,10 +186,23 @@ extern "C" int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_co
                       "Batch size %llu exceeds maximum %llu for this circuit: the static scratch holds %zu bytes",
                       (unsigned long long)num_samples, (unsigned long long)max_samples, kStaticScratchBytes);
 
+    cudaStream_t st = (cudaStream_t)stream;
+    // Every call copies the circuit from pageable host memory (partly from
+    // this stack frame); a graph recorded from such copies would replay them
+    // from memory that no longer holds the circuit, so a capturing stream is
+    // refused before anything is enqueued.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing(st, &cap);
+    if (ce != cudaSuccess)
+        return report(err, err_len, SP_ERR_BACKEND, "cudaStreamIsCapturing: %s", cudaGetErrorString(ce));
+    if (cap != cudaStreamCaptureStatusNone)
+        return report(err, err_len, SP_ERR_INVALID_ARGUMENT,
+                      "the stream is capturing: sp_newton_dc_static copies the circuit from host memory on every "
+                      "call and cannot be recorded into a CUDA graph");
+
     DeviceSetup* dev = nullptr;
     int rc = setup_current_device(&dev, err, err_len);
     if (rc) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
     unsigned char* base = dev->scratch;
     sp_element* del = (sp_element*)base;
     sp_param* dpar = (sp_param*)(base + be);

@@ -152,6 +152,7 @@ class WarmStart:
         torch.cuda.synchronize()
         self.mlp.set_io(self.inputs, in_mean, in_scale, out_mean, out_scale)
         self._io = (out_mean, out_scale)
+        self._in = (in_mean, in_scale)
         per_epoch = rows // batch
         self.report = TrainReport(samples, int(ok.sum().item()), list(self.inputs),
                                   [c.param_labels[s] for s in self.inputs],
@@ -181,6 +182,14 @@ class WarmStart:
         pred = io[0] + io[1] * y.double().cpu().numpy() + Pc @ self._lin.T
         err = pred - x.cpu().numpy()
         return np.sqrt((err ** 2).mean(0)) / self.tolerance
+
+    def use_network(self, on: bool = True):
+        """With on=False the warm start is the FP64-fitted linear term alone,
+        out_mean + lin (p - in_mean): the network's output is scaled by zero.
+        This isolates what the trained network adds over the linear fit."""
+        out_mean, out_scale = self._io
+        self.mlp.set_io(self.inputs, self._in[0], self._in[1], out_mean,
+                        out_scale if on else np.zeros_like(out_scale))
 
     WARM_MAX_ITERATIONS = 8  # a miss restarts cold after this many iterations
 

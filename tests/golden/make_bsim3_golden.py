@@ -1,9 +1,9 @@
 #!/usr/bin/env python3
 """Writes tests/golden/bsim3_dc.json from the reference's own BSIM3 golden
-data (run from the repository root, with the Spicier sources at $SPICIER_SRC,
-default /root/reference):
+data (run from the repository root; the argument is a checkout of the
+Spicier sources):
 
-    python tests/golden/make_bsim3_golden.py
+    python tests/golden/make_bsim3_golden.py <path to spicier>
 
 The source is crates/spicier-parser/tests/golden_data/dc_bsim3.json
 (ngspice-45 operating points of five BSIM3v3.3 netlists, with the tolerances
@@ -12,13 +12,15 @@ quantities and tolerances are copied unchanged; nothing is computed here.
 """
 import json
 import os
+import sys
 
-SRC = os.environ.get("SPICIER_SRC", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
-    path = os.path.join(SRC, "crates/spicier-parser/tests/golden_data/dc_bsim3.json")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_bsim3_golden.py <path to the Spicier sources>")
+    path = os.path.join(sys.argv[1], "crates/spicier-parser/tests/golden_data/dc_bsim3.json")
     with open(path) as f:
         data = json.load(f)
     out = {"source": "crates/spicier-parser/tests/golden_data/dc_bsim3.json",

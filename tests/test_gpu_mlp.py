@@ -107,7 +107,7 @@ def test_learned_warm_start_cuts_iterations(ctx):
     assert np.array_equal(h.iters, il) and np.array_equal(h.status, sl)
 
 
-@pytest.mark.parametrize("H,nl", [(128, 3), (64, 2), (128, 1)])
+@pytest.mark.parametrize("H,nl", [(128, 3), (64, 2), (128, 1), (256, 3), (256, 1)])
 def test_inference_kernels_match_oracle(ctx, H, nl):
     """The tcgen05 warm-start kernel, the fused mma.sync kernel and the
     layer-by-layer GEMMs against the numpy oracle (same BF16 rounding points),
@@ -145,7 +145,35 @@ def test_inference_kernels_match_oracle(ctx, H, nl):
 
 
 def test_tcgen05_rejects_unsupported_shape(ctx):
-    m = Mlp(ctx, 17, 12, 256, 3, seed=1)
-    with pytest.raises(sg.SpicierError):
-        m.set_inference_kernel(abi.SP_MLP_KERNEL_TCGEN05)
+    for H in (192, 512):
+        m = Mlp(ctx, 17, 12, H, 3, seed=1)
+        with pytest.raises(sg.SpicierError):
+            m.set_inference_kernel(abi.SP_MLP_KERNEL_TCGEN05)
+        m.close()
+
+
+@pytest.mark.parametrize("rows", [1, 127, 129, 300, 128 * 152 * 3 + 5, 262144])
+def test_tcgen05_hidden256_row_counts(ctx, rows):
+    """The streaming kernel (hidden 256) on the workload's 10 -> 3x256 -> 12
+    network over row counts that leave a CTA with no tile, one tile, an odd
+    number of tiles (team 1 idle in the last pair) and many tiles: equal to
+    the layer-by-layer GEMMs up to the BF16 rounding points."""
+    n_in, n_out = 10, 12
+    m = Mlp(ctx, n_in, n_out, 256, 3, seed=7)
+    rng = np.random.default_rng(rows)
+    slots = np.arange(n_in, dtype=np.int32)
+    m.set_io(slots, np.zeros(n_in, np.float32), np.ones(n_in, np.float32), np.zeros(n_out, np.float32),
+             np.ones(n_out, np.float32))
+    P = torch.tensor(rng.normal(0, 1, (n_in, rows)), device="cuda")
+    outs = {}
+    for kind in (abi.SP_MLP_KERNEL_TCGEN05, abi.SP_MLP_KERNEL_LAYERED):
+        m.set_inference_kernel(kind)
+        x0 = torch.full((rows, n_out), float("nan"), dtype=torch.float64, device="cuda")
+        m.warm_start_device(P, rows, rows, x0)
+        torch.cuda.synchronize()
+        outs[kind] = x0.cpu().numpy()
+    a, b = outs[abi.SP_MLP_KERNEL_TCGEN05], outs[abi.SP_MLP_KERNEL_LAYERED]
+    assert np.isfinite(a).all()
+    err = np.abs(a - b)
+    assert err.mean() < 2e-3 and err.max() < 0.1, (err.mean(), err.max())
     m.close()

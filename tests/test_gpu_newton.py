@@ -205,6 +205,17 @@ def test_errors_are_statuses(ctx):
     tab.R("R", "a", "0", 1.0)
     with pytest.raises(sg.SpicierError):
         ctx.newton_dc(tab, abi.newton_config(), seed=0, count=4, table=np.zeros((4, 2)))
+    # BatchTooLarge carries the reference variant's own text, "Batch size {size} exceeds
+    # maximum {max}" (error.rs:28-30), so a binding recovers both fields from it
+    cfg = ctx.config()
+    small = type(cfg)(cfg.min_batch_size, cfg.min_matrix_size, 100)
+    ctx.set_config(small)
+    try:
+        with pytest.raises(sg.SpicierError) as e:
+            ctx.newton_dc(configs.cs_nmos_amp(), abi.newton_config(), seed=0, count=101)
+        assert e.value.kind == "BatchTooLarge" and "Batch size 101 exceeds maximum 100" in str(e.value)
+    finally:
+        ctx.set_config(cfg)
 
 
 @pytest.mark.parametrize("prec", [MIXED, EXACT])

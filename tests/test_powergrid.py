@@ -75,6 +75,40 @@ def test_mixed_meets_residual_target(ctx):
     assert (np.abs(g["x"][:, :n] - o["x"][:, :n]) <= tol).all()
 
 
+@pytest.fixture(scope="module")
+def full_oracle():
+    """Corners 0..3 of the workload's 64 x 64 mesh (4,097 unknowns, 512 sinks):
+    one random layout under the four R x VTO corners."""
+    with oracle.math_mode("cr"):
+        return oracle.grid_solve(abi.grid_config(), 1, 4, threads=4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [abi.SP_PREC_FP64, abi.SP_PREC_MIXED])
+def test_full_size_mesh_against_oracle(ctx, full_oracle, prec):
+    """The workload mesh against the oracle.  Each Newton step's linear solve
+    stops at a relative residual of 1e-9, so two Krylov solvers (CGS2 here,
+    MGS in the oracle) agree to about 1e-8 of the node voltages, not to the
+    last bit: FP64 within 1e-7 V and the SPICE tolerance, MIXED within the
+    SPICE tolerance (reltol 1e-3, vntol 1e-6 V; abstol 1e-12 A plus reltol
+    for the supply current) and its 1e-9 A residual target."""
+    cfg = abi.grid_config(precision=prec)
+    g = ctx.grid_solve(cfg, 1, 4)
+    o = full_oracle
+    assert (g["status"] == 0).all() and (o["status"] == 0).all()
+    n = cfg.rows * cfg.cols
+    tol_v = 1e-3 * np.maximum(np.abs(g["x"][:, :n]), np.abs(o["x"][:, :n])) + 1e-6
+    assert (np.abs(g["x"][:, :n] - o["x"][:, :n]) <= tol_v).all()
+    tol_i = 1e-3 * np.abs(o["x"][:, n]) + 1e-12
+    assert (np.abs(g["x"][:, n] - o["x"][:, n]) <= tol_i).all()
+    if prec == abi.SP_PREC_FP64:
+        assert np.array_equal(g["newton"], o["newton"])
+        assert np.abs(g["x"][:, :n] - o["x"][:, :n]).max() < 1e-7
+        assert g["resid"].max() < 1e-7
+    else:
+        assert g["resid"].max() <= cfg.resid_target
+
+
 @pytest.mark.gpu
 def test_full_size_mesh(ctx):
     cfg = abi.grid_config(precision=abi.SP_PREC_MIXED)
