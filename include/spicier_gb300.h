@@ -718,6 +718,29 @@ int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32
                       uint32_t cols, const uint8_t* d_status, sp_moments* d_out,
                       void* stream);
 
+/* ---------------------------------------------------------------------- */
+/* Launch settings chosen by an autotuner (no counterpart in the reference, */
+/* whose dispatch thresholds are fixed, crates/spicier-solver/src/         */
+/* dispatch.rs:85-120).  A setting applies to the sizes of one bucket: key */
+/* "<setting>@<bucket>", bucket = sp_tune_bucket(size) (the smallest power */
+/* of two >= size, at least 4).  Settings and their size:                  */
+/*   lu.cta               1: CTA-per-system batched LU even where one      */
+/*                        thread per system fits (n <= 28); size n         */
+/*   newton.block.fp64 | .mixed | .exact  threads per block of the generic */
+/*                        thread-per-sample Newton kernels; size MNA n     */
+/*   spec.bpsm.fp64 | .mixed  resident blocks per SM of the topology-      */
+/*                        specialised kernel (at most the occupancy limit) */
+/*   ladder.bpsm          resident blocks per SM of the ladder transients  */
+/*                        (at most what fits); size max_sections           */
+/*   mlp.teams            128-sample tiles in flight per SM of the tcgen05 */
+/*                        warm start (resident weights); size hidden width */
+/* value <= 0 removes a setting.  Results do not depend on any setting.    */
+/* sp_tune_get returns 1 and the value when the key is set, else 0.        */
+/* ---------------------------------------------------------------------- */
+int sp_tune_set(sp_ctx* ctx, const char* key, int value);
+int sp_tune_get(sp_ctx* ctx, const char* key, int* value);
+int sp_tune_bucket(long long size);
+
 /* StatisticsAccumulator::merge (statistics.rs:148-155) for n unknowns:
  * acc[i] absorbs other[i] (counts and sums added, min/max combined), as
  * StreamingStatistics::merge (statistics.rs:548-559) does per node.  This is

@@ -125,6 +125,9 @@ def _bind(L):
         "sp_histogram_device": (i32, [vp, vp, u64, u32, u32, vp, d, d, u32, vp, vp]),
         "sp_bsim3_eval_device": (i32, [vp, i32, vp, vp, u64, vp, vp, vp]),
         "sp_yield_device": (i32, [vp, vp, u64, u32, vp, vp, u32, vp, vp]),
+        "sp_tune_set": (i32, [vp, C.c_char_p, i32]),
+        "sp_tune_get": (i32, [vp, C.c_char_p, P(i32)]),
+        "sp_tune_bucket": (i32, [C.c_longlong]),
         "sp_moments_merge_device": (i32, [vp, vp, vp, u32, vp]),
         "sp_moments_merge": (i32, [vp, vp, u32]),
         "sp_profile_enable": (i32, [vp, i32]),

@@ -89,6 +89,13 @@ struct ScratchOrder {
 
 }  // namespace
 
+int tune_get(sp_ctx* ctx, const char* name, long long n, int dflt) {
+    std::lock_guard<std::mutex> g(ctx->tune_mu);
+    if (ctx->tune.empty()) return dflt;
+    auto it = ctx->tune.find(std::string(name) + "@" + std::to_string(tune_bucket(n)));
+    return it == ctx->tune.end() ? dflt : it->second;
+}
+
 extern "C" {
 
 const char* sp_version(void) { return "spicier-gb300 0.1.0 sm_103a"; }
@@ -108,8 +115,6 @@ int sp_ctx_create(int device, sp_ctx** out) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, 256);
-    if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, 256);
     if (e == cudaSuccess) e = prepare_exact_kernels(ctx->max_smem);
     if (e == cudaSuccess) e = prepare_fast_kernels(ctx->max_smem);
     if (e != cudaSuccess) {
@@ -127,7 +132,6 @@ int sp_ctx_destroy(sp_ctx* ctx) {
     cudaDeviceSynchronize();
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->aux) cudaFree(ctx->aux);
-    if (ctx->counters) cudaFree(ctx->counters);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
     for (auto& r : ctx->recs) {
@@ -271,7 +275,10 @@ static int solve_batch_device_locked(sp_ctx* ctx, const double* d_m, const doubl
     if (n > (size_t)kMaxBatchLuN)
         return fail(ctx, SP_ERR_INVALID_DIMENSION, "n = %zu exceeds the batched dense LU limit %d", n,
                     kMaxBatchLuN);
-    if (n > (size_t)kMaxDenseN) {
+    // one thread per system up to kMaxDenseN unknowns unless the tuner chose
+    // the CTA-per-system kernel for this size (setting "lu.cta", 1 = CTA)
+    const bool cta = n > (size_t)kMaxDenseN || tune_get(ctx, "lu.cta", (long long)n, 0) == 1;
+    if (cta) {
         // one CTA per system, FP64 in the reference's order (both precisions)
         ProfScope prof(ctx, "lu_batch_cta", st);
         double* work = nullptr;
@@ -588,6 +595,12 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
                                         : work_bytes_per_thread<SP_PREC_FP64>(t->n);
     int block = pick_block(per, ctx->max_smem);
     if (!block) return fail(ctx, SP_ERR_INVALID_DIMENSION, "MNA size %d does not fit shared memory", t->n);
+    {
+        // tuned threads per block (setting "newton.block.<precision>"), within what shared memory allows
+        static const char* bname[3] = {"newton.block.fp64", "newton.block.mixed", "newton.block.exact"};
+        const int tb = tune_get(ctx, bname[prec], t->n, 0);
+        if (tb >= 32 && tb % 32 == 0 && tb <= 1024 && per * tb <= (size_t)ctx->max_smem) block = tb;
+    }
     size_t smem = per * block;
     int grid = (int)((count + block - 1) / block);
     static const char* kname[3] = {"newton_primary_fp64", "newton_primary_mixed", "newton_primary_fp64_exact"};
@@ -616,18 +629,23 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (e != cudaSuccess) return cuda_fail(ctx, e, "newton launch");
     const bool any_fallback = d_x0 || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE));
     if (any_fallback) {
-        // one wave of blocks: the miss list is usually empty or short, and a
-        // second wave of large-shared-memory blocks costs a few microseconds
-        int fgrid = std::min(grid, std::max(1, ctx->num_sms));
+        // one-warp blocks (a few KB of shared memory each) fit beside the
+        // primary kernel's blocks, so under programmatic dependent launch they
+        // are resident while it drains and an empty miss list costs almost
+        // nothing; four per SM keep as many threads on a long miss list as
+        // one 128-thread block per SM did
+        const int fblock = 32;
+        const int fgrid = std::max(1, std::min(ctx->num_sms * 4, (int)((count + fblock - 1) / fblock)));
+        const size_t fsmem = per * fblock;
         ProfScope prof(ctx, fname[prec], st);
-        e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, true, fgrid, block, smem, st)
-                                       : launch_newton_fast(kprec, L, true, fgrid, block, smem, st);
+        e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, true, fgrid, fblock, fsmem, st)
+                                       : launch_newton_fast(kprec, L, true, fgrid, fblock, fsmem, st);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback launch");
     }
     if (d_moments) {
         ProfScope prof(ctx, "moments", st);
         e = launch_moments(d_x, count, (uint32_t)t->n, (uint32_t)t->n, d_status, s.partial, s.moment_blocks,
-                           d_moments, st, ctx->counters);
+                           d_moments, st);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "moments launch");
     }
     return SP_OK;
@@ -812,10 +830,30 @@ int sp_moments_device(sp_ctx* ctx, const double* d_values, uint64_t rows, uint32
     if (rc) return rc;
     ScratchOrder order(ctx, (cudaStream_t)stream);
     SP_CUDA(ctx, launch_moments(d_values, rows, ld, cols, d_status, (sp_moments*)ctx->scratch, mb, d_out,
-                                (cudaStream_t)stream, ctx->counters),
+                                (cudaStream_t)stream),
             "moments launch");
     return SP_OK;
 }
+
+int sp_tune_set(sp_ctx* ctx, const char* key, int value) {
+    if (!ctx || !key || !*key) return SP_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(ctx->tune_mu);
+    if (value <= 0)
+        ctx->tune.erase(key);
+    else
+        ctx->tune[key] = value;
+    return SP_OK;
+}
+
+int sp_tune_get(sp_ctx* ctx, const char* key, int* value) {
+    if (!ctx || !key || !value) return SP_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(ctx->tune_mu);
+    auto it = ctx->tune.find(key);
+    *value = it == ctx->tune.end() ? 0 : it->second;
+    return it == ctx->tune.end() ? 0 : 1;
+}
+
+int sp_tune_bucket(long long n) { return tune_bucket(n); }
 
 int sp_moments_merge_device(sp_ctx* ctx, sp_moments* d_acc, const sp_moments* d_other, uint32_t n, void* stream) {
     if (!ctx) return SP_ERR_INVALID_ARGUMENT;
@@ -914,7 +952,10 @@ static LadderPlan ladder_plan(const sp_ctx* ctx, const sp_ladder_config* c, uint
     // per-ladder arrays
     p.smem = (size_t)4 * ladder_warp_doubles(p.stride, c->precision) * 8;
     // resident blocks per SM: the kernel's launch bounds allow two (registers), shared memory may allow fewer
-    const int bpsm = std::max(1, std::min(2, (int)((228 * 1024 - 1024) / (p.smem + 1024))));
+    int bpsm = std::max(1, std::min(2, (int)((228 * 1024 - 1024) / (p.smem + 1024))));
+    // tuned resident blocks per SM (setting "ladder.bpsm"), never above what fits
+    const int tb = tune_get(const_cast<sp_ctx*>(ctx), "ladder.bpsm", c->max_sections, 0);
+    if (tb >= 1 && tb < bpsm) bpsm = tb;
     p.blocks = std::min<uint64_t>((count + 3) / 4, (uint64_t)ctx->num_sms * bpsm);
     const int bins = c->max_sections - c->min_sections + 1;
     p.bh = align256(4 * (size_t)bins);

@@ -73,11 +73,9 @@ cudaError_t launch_newton_fast(int prec, const NewtonLaunch& L, bool fallback, i
                                size_t smem, cudaStream_t st);
 cudaError_t launch_lu_batch_mixed(const double* mats, const double* rhs, int n, uint64_t batch,
                                   double* sol, uint8_t* sing, int refine_steps, cudaStream_t st);
-// counter: a zero-initialised word of the context (the single-pass kernel's
-// arrival counter, reset by the kernel), or nullptr for the two-kernel path.
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
-                           cudaStream_t st, unsigned int* counter = nullptr);
+                           cudaStream_t st);
 cudaError_t launch_moments_merge(sp_moments* acc, const sp_moments* other, uint32_t n, cudaStream_t st);
 cudaError_t prepare_fast_kernels(int max_smem);
 
@@ -134,10 +132,20 @@ struct sp_ctx {
     // owns `scratch`) and keep their own data across it
     void* aux = nullptr;
     size_t aux_bytes = 0;
-    // zero-initialised device words: [0] the single-pass moments kernel's
-    // arrival counter (each launch leaves it at zero)
-    unsigned int* counters = nullptr;
+    // launch settings chosen by the autotuner (sp_tune_set), keyed
+    // "<setting>@<size bucket>"; absent keys keep the built-in heuristics
+    std::mutex tune_mu;
+    std::map<std::string, int> tune;
 };
+
+// Size bucket of a tuning key: the smallest power of two >= n (at least 4).
+inline int tune_bucket(long long n) {
+    int b = 4;
+    while (b < n && b < (1 << 30)) b <<= 1;
+    return b;
+}
+// The tuned value of setting `name` at size n, or dflt when none was set.
+int tune_get(sp_ctx* ctx, const char* name, long long n, int dflt);
 
 // Brackets one kernel launch with events when the context is profiling.
 struct ProfScope {

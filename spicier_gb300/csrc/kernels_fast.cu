@@ -234,7 +234,6 @@ __global__ void moments_final_kernel(const sp_moments* __restrict__ partial, uin
 // (about eight chunks per SM, one batch of loads per thread), so the result
 // depends only on rows and cols.
 constexpr int kMomChunkMin = 64;
-constexpr uint64_t kMomOnepassChunks = 256;  // chunks of the single-pass kernel (two blocks per SM)
 
 __host__ __device__ inline uint64_t moments_chunk(uint64_t rows, uint32_t max_blocks) {
     const uint64_t target = max_blocks < 1216 ? max_blocks : 1216;  // about eight blocks per SM
@@ -300,90 +299,6 @@ __global__ void __launch_bounds__(256) moments_rows_kernel(const double* __restr
     if (threadIdx.x < cols) partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
 }
 
-// Shuffle-merge of one sp_moments across a warp (lane + o into lane).
-__device__ __forceinline__ void mom_shfl_merge(sp_moments& m, int o) {
-    sp_moments b;
-    b.count = __shfl_down_sync(0xffffffffu, m.count, o);
-    b.sum = __shfl_down_sync(0xffffffffu, m.sum, o);
-    b.sum_sq = __shfl_down_sync(0xffffffffu, m.sum_sq, o);
-    b.min = __shfl_down_sync(0xffffffffu, m.min, o);
-    b.max = __shfl_down_sync(0xffffffffu, m.max, o);
-    mom_merge(m, b);
-}
-
-// Single-pass moments of a narrow table (cols <= 32): the chunk pass of
-// moments_rows_kernel, then the block that finishes last (a counter that it
-// resets for the next launch) merges every column's partials, one warp per
-// column: lane l merges partials l, l + 32, ... in order, then a fixed
-// shuffle tree.  The summation order depends only on rows and cols.
-__global__ void __launch_bounds__(256) moments_onepass_kernel(const double* __restrict__ v, uint64_t rows,
-                                                              uint32_t ld, uint32_t cols, uint32_t cp,
-                                                              uint64_t chunk, const uint8_t* __restrict__ status,
-                                                              sp_moments* __restrict__ partial,
-                                                              unsigned int* __restrict__ counter,
-                                                              sp_moments* __restrict__ out) {
-    __shared__ sp_moments sh[256];
-    __shared__ bool last;
-    pdl_wait();
-    pdl_trigger();
-    const uint32_t c = threadIdx.x % cp, g = threadIdx.x / cp, groups = 256 / cp;
-    const uint64_t lo = (uint64_t)blockIdx.x * chunk, hi = min(rows, lo + chunk);
-    sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
-    long long kmin = order_key(CUDART_INF), kmax = order_key(-CUDART_INF);
-    if (c < cols) {
-        for (uint64_t i0 = lo + g; i0 < hi; i0 += 4 * (uint64_t)groups) {
-            double xs[4];
-            bool ok[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint64_t i = i0 + (uint64_t)u * groups;
-                ok[u] = i < hi && (!status || (status[i] & SP_ST_MASK) == SP_ST_CONVERGED);
-                xs[u] = ok[u] ? v[i * ld + c] : 0.0;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (!ok[u]) continue;
-                const double x = xs[u];
-                m.count += 1;
-                m.sum += x;
-                m.sum_sq += x * x;
-                const long long k = order_key(x);
-                kmin = k < kmin ? k : kmin;
-                kmax = k > kmax ? k : kmax;
-            }
-        }
-    }
-    m.min = from_key(kmin);
-    m.max = from_key(kmax);
-    sh[threadIdx.x] = m;
-    __syncthreads();
-    for (uint32_t w = groups / 2; w >= 1; w >>= 1) {
-        if (g < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w * cp]);
-        __syncthreads();
-    }
-    if (threadIdx.x < cols) partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
-    __threadfence();  // this block's partials are visible before it is counted
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t col = warp; col < cols; col += 8) {
-        sp_moments a{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
-        for (uint32_t b = lane; b < gridDim.x; b += 32) {
-            const sp_moments* p = &partial[(size_t)col * gridDim.x + b];
-            // L2 reads: the partials were written by other blocks of this launch
-            const sp_moments q{(uint64_t)__ldcg(reinterpret_cast<const unsigned long long*>(&p->count)),
-                               __ldcg(&p->sum), __ldcg(&p->sum_sq), __ldcg(&p->min), __ldcg(&p->max)};
-            mom_merge(a, q);
-        }
-        for (int o = 16; o >= 1; o >>= 1) mom_shfl_merge(a, o);
-        if (lane == 0) out[col] = a;
-    }
-    if (threadIdx.x == 0) *counter = 0u;  // ready for the next launch
-}
-
 // One block per column: each thread merges partials t, t + 256, ... in order,
 // then a pairwise tree; deterministic for a given partial count.
 __global__ void __launch_bounds__(256) moments_tree_kernel(const sp_moments* __restrict__ partial, uint32_t nblocks,
@@ -446,23 +361,11 @@ cudaError_t launch_moments_merge(sp_moments* acc, const sp_moments* other, uint3
 
 cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uint32_t cols,
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
-                           cudaStream_t st, unsigned int* counter) {
+                           cudaStream_t st) {
     if (cols == 0) return cudaSuccess;
     if (rows == 0) {  // empty accumulators (count 0, min +inf, max -inf)
         moments_tree_kernel<<<cols, 256, 0, st>>>(partial, 0, out);
         return cudaGetLastError();
-    }
-    if (counter && cols <= 32) {
-        // single pass over at most kMomOnepassChunks chunks (a function of rows only)
-        uint64_t chunk = (rows + kMomOnepassChunks - 1) / kMomOnepassChunks;
-        chunk = (chunk + kMomChunkMin - 1) / kMomChunkMin * kMomChunkMin;
-        const uint32_t nb = (uint32_t)((rows + chunk - 1) / chunk);
-        if (nb <= nblocks) {
-            uint32_t cp = 1;
-            while (cp < cols) cp <<= 1;
-            return launch_chained(moments_onepass_kernel, dim3(nb), dim3(256), 0, st, values, rows, ld, cols, cp,
-                                  chunk, status, partial, counter, out);
-        }
     }
     const uint64_t chunk = moments_chunk(rows, nblocks);
     if (cols <= 32 && (rows + chunk - 1) / chunk <= nblocks) {

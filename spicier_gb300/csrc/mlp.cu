@@ -1053,6 +1053,7 @@ cudaError_t tc_warm_start(sp_mlp* m, const double* params_soa, size_t stride, in
     a.img = m->tc_img;
     a.x0 = x0;
     a.err = m->tc_err;
+    a.teams_pref = tune_get(m->ctx, "mlp.teams", m->H, 0);  // tiles in flight per CTA (tuned)
     return mlptc::launch(a, m->num_sms, st);
 }
 

@@ -803,8 +803,9 @@ cudaError_t launch(const Args& a, int num_sms, cudaStream_t st) {
         if (grid < 1) return cudaSuccess;
         return launch_chained(stream_kernel, dim3(grid), dim3(kSThreads), smem, st, a, nslots);
     }
-    const int teams = teams_for(a);
+    int teams = teams_for(a);
     if (teams == 0) return cudaErrorInvalidValue;
+    if (a.teams_pref > 0 && a.teams_pref < teams) teams = a.teams_pref;
     const size_t smem = 1024 + (size_t)carve(a, teams).total;
     int grid = (ntiles + teams - 1) / teams;
     if (grid > num_sms) grid = num_sms;

@@ -32,6 +32,7 @@ struct Args {
     double* x0;                // [rows][n_out]
     int* err;                  // set to 1 when a bounded wait timed out
     int n_in, n_out, L, img_bytes, bias_total;
+    int teams_pref;            // 0: the most tiles in flight that fit; else at most this many (tuned)
     Layer layer[kMaxLayers];
 };
 

@@ -688,7 +688,11 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     a.next = L.work_next;
     if (!a.next) return cudaErrorInvalidValue;
     void* args[] = {&a};
-    const uint64_t resident = (uint64_t)t->ctx->num_sms * (uint64_t)t->spec_bpsm[slot];
+    // tuned resident blocks per SM (setting "spec.bpsm.<precision>"), never above the occupancy limit
+    int bpsm = t->spec_bpsm[slot];
+    const int tb = tune_get(t->ctx, prec == SP_PREC_MIXED ? "spec.bpsm.mixed" : "spec.bpsm.fp64", t->n, 0);
+    if (tb >= 1 && tb < bpsm) bpsm = tb;
+    const uint64_t resident = (uint64_t)t->ctx->num_sms * (uint64_t)bpsm;
     const unsigned grid = (unsigned)std::min<uint64_t>((L.count + 127) / 128, resident);
     ChainedLaunch cl(dim3(grid), dim3(128), spec_smem_bytes(t, prec == SP_PREC_MIXED), st);
     return cudaLaunchKernelExC(&cl.cfg, (const void*)t->spec_kernel[slot], args);
