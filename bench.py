@@ -147,13 +147,14 @@ __global__ void fma_chain(T* out, int iters, T a, T b) {
     }
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
-// two integer ALU operations (xor, add) per chain step
+// one three-input logic operation per value and step, each mixing two
+// values so that no step folds away: the integer ALU pipe alone
 __global__ void alu_chain(unsigned* out, int iters, unsigned a, unsigned b) {
-    unsigned x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+    unsigned x0 = threadIdx.x ^ b, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
              x7 = x0 + 7;
     for (int i = 0; i < iters; ++i) {
-        x0 = (x0 ^ a) + b; x1 = (x1 ^ a) + b; x2 = (x2 ^ a) + b; x3 = (x3 ^ a) + b;
-        x4 = (x4 ^ a) + b; x5 = (x5 ^ a) + b; x6 = (x6 ^ a) + b; x7 = (x7 ^ a) + b;
+        x0 = (x0 ^ x1) | a; x1 = (x1 ^ x2) | a; x2 = (x2 ^ x3) | a; x3 = (x3 ^ x4) | a;
+        x4 = (x4 ^ x5) | a; x5 = (x5 ^ x6) | a; x6 = (x6 ^ x7) | a; x7 = (x7 ^ x0) | a;
     }
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 ^ x1 ^ x2 ^ x3 ^ x4 ^ x5 ^ x6 ^ x7;
 }
@@ -186,7 +187,7 @@ extern "C" int pipe_peaks(double* out) {
     ms = timed(fma_chain<float>, blocks, (float*)buf, i32, 0.999f, 0.001f);
     out[1] = 2.0 * 8 * (double)i32 * blocks * threads / (ms * 1e9);
     ms = timed(alu_chain, blocks, (unsigned*)buf, ialu, 0x9e3779b9u, 0x7f4a7c15u);
-    out[2] = 2.0 * 8 * (double)ialu * blocks * threads / (ms * 1e9);
+    out[2] = 8.0 * (double)ialu * blocks * threads / (ms * 1e9);
     cudaFree(buf);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
@@ -211,7 +212,7 @@ def measure_pipe_peaks():
         if f(out) == 0:
             best = [max(b, v) for b, v in zip(best, out)]
     return {"fp64_tflops": best[0], "fp32_tflops": best[1], "int_alu_tops": best[2],
-            "probe": "independent FMA / xor+add chains, 8 per thread, 8 blocks of 256 per SM (bench.py PIPE_PROBE)"}
+            "probe": "independent FMA / logic-op chains, 8 per thread, 8 blocks of 256 per SM (bench.py PIPE_PROBE)"}
 
 
 def structural_nnz(circuit):
@@ -662,7 +663,7 @@ def main():
         if inst and alu_peak:
             a = inst * 32 * N / (ms * 1e-3) / 1e12
             entry.update({"bound": "int_alu", "achieved": a, "peak": alu_peak, "unit": "T ALU ops/s",
-                          "frac": a / alu_peak, "peak_source": "xor+add chains measured live by this bench",
+                          "frac": a / alu_peak, "peak_source": "logic-op chains measured live by this bench",
                           "note": "integer ALU ops per sample from the committed ncu capture "
                                   "(sm__inst_executed_pipe_alu), times the live launch duration"})
         else:
@@ -938,9 +939,11 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r, dt, _, done = cpu_baseline(circ, N, min_seconds=10.0)
+        r1, dt1, _, done1 = cpu_baseline(circ, 4096, threads=1, min_seconds=2.0)
         cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"{done} op-amp Monte Carlo samples ({N}-sample chunks), plain FP64 Newton from the "
-                         f"nodeset, {dt:.1f} s on all host threads"}
+                         f"nodeset, {dt:.1f} s on all host threads",
+               "single_thread": {"value": r1, "sample": f"{done1} samples on one host thread, {dt1:.1f} s"}}
 
     if rank == 0:
         def arm(r):
@@ -974,6 +977,7 @@ def main():
             "lu_vs_cublas_speedup": None if not lu_cmp or "unavailable" in lu_cmp else
             {k: round(v["speedup"], 2) for k, v in lu_cmp.items()},
             "cpu_baseline_solves_per_s": None if cpu is None else cpu["value"],
+            "cpu_single_thread_solves_per_s": None if cpu is None else cpu["single_thread"]["value"],
         }
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

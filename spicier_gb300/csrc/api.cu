@@ -42,21 +42,8 @@ int cuda_fail(sp_ctx* ctx, cudaError_t e, const char* what) {
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Grow-only device scratch owned by the context.
 int ensure_scratch(sp_ctx* ctx, size_t bytes) {
-    if (bytes <= ctx->scratch_bytes) return SP_OK;
-    if (ctx->scratch) {
-        cudaError_t e = cudaDeviceSynchronize();
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronise before scratch growth");
-        cudaFree(ctx->scratch);
-        ctx->scratch = nullptr;
-        ctx->scratch_bytes = 0;
-    }
-    size_t want = align256(bytes + bytes / 4);
-    cudaError_t e = cudaMalloc(&ctx->scratch, want);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "scratch allocation");
-    ctx->scratch_bytes = want;
-    return SP_OK;
+    return ::grow_buffer(ctx, &ctx->scratch, &ctx->scratch_bytes, bytes, "scratch");
 }
 
 // Threads per block of the thread-per-sample kernels: the largest multiple of
@@ -69,25 +56,51 @@ int pick_block(size_t per_thread, int max_smem) {
     return block;
 }
 
-// Calls on different streams share the context's scratch: each call orders
-// itself after the previous user (skipped while the stream is being captured
-// into a CUDA graph, where the caller orders the work).
-struct ScratchOrder {
-    sp_ctx* ctx;
-    cudaStream_t st;
-    bool capturing = false;
-    ScratchOrder(sp_ctx* c, cudaStream_t s) : ctx(c), st(s) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(st, &cs);
-        capturing = cs != cudaStreamCaptureStatusNone;
-        if (!capturing) cudaStreamWaitEvent(st, ctx->scratch_done, 0);
-    }
-    ~ScratchOrder() {
-        if (!capturing) cudaEventRecord(ctx->scratch_done, st);
-    }
-};
 
 }  // namespace
+
+// Grow a context-owned device buffer (grow-only).  Inside a call's ordering
+// guard the old buffer is freed and the new one allocated in the calling
+// stream's order (cudaFreeAsync / cudaMallocAsync): the stream already waits
+// for every earlier user of the context's buffers, so nothing else on the
+// device is stalled.  A stream being captured into a CUDA graph cannot grow
+// them (the allocation would belong to the graph); outside a guard the growth
+// waits for the device.
+int grow_buffer(sp_ctx* ctx, void** buf, size_t* have, size_t bytes, const char* what) {
+    if (bytes <= *have) return SP_OK;
+    if (ctx->order_active && ctx->order_capturing)
+        return fail(ctx, SP_ERR_INVALID_ARGUMENT,
+                    "the context's %s must grow to %zu bytes while the stream is being captured: make the same "
+                    "call once before the capture",
+                    what, bytes);
+    const size_t want = align256(bytes + bytes / 4);
+    void* p = nullptr;
+    cudaError_t e;
+    if (ctx->order_active) {
+        if (*buf) {
+            e = cudaFreeAsync(*buf, ctx->order_stream);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+        }
+        *buf = nullptr;
+        *have = 0;
+        e = cudaMallocAsync(&p, want, ctx->order_stream);
+    } else {
+        if (*buf) {
+            e = cudaDeviceSynchronize();
+            if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+            cudaFreeAsync(*buf, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+        }
+        *buf = nullptr;
+        *have = 0;
+        e = cudaMallocAsync(&p, want, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+    *buf = p;
+    *have = want;
+    return SP_OK;
+}
 
 int tune_get(sp_ctx* ctx, const char* name, long long n, int dflt) {
     std::lock_guard<std::mutex> g(ctx->tune_mu);
@@ -130,8 +143,10 @@ int sp_ctx_destroy(sp_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaDeviceSynchronize();
-    if (ctx->scratch) cudaFree(ctx->scratch);
-    if (ctx->aux) cudaFree(ctx->aux);
+    // both buffers come from the stream-ordered allocator
+    if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->stream);
+    if (ctx->aux) cudaFreeAsync(ctx->aux, ctx->stream);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
     for (auto& r : ctx->recs) {
@@ -249,19 +264,7 @@ void sp_newton_config_default(sp_newton_config* c) {
 // solve_batch
 // ---------------------------------------------------------------------------
 static int ensure_aux(sp_ctx* ctx, size_t bytes) {
-    if (bytes <= ctx->aux_bytes) return SP_OK;
-    if (ctx->aux) {
-        cudaError_t e = cudaDeviceSynchronize();
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronise before buffer growth");
-        cudaFree(ctx->aux);
-        ctx->aux = nullptr;
-        ctx->aux_bytes = 0;
-    }
-    const size_t want = align256(bytes + bytes / 4);
-    cudaError_t e = cudaMalloc(&ctx->aux, want);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "buffer allocation");
-    ctx->aux_bytes = want;
-    return SP_OK;
+    return ::grow_buffer(ctx, &ctx->aux, &ctx->aux_bytes, bytes, "second buffer");
 }
 
 static int solve_batch_device_locked(sp_ctx* ctx, const double* d_m, const double* d_r, size_t n,

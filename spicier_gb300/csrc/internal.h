@@ -107,6 +107,12 @@ struct sp_ctx {
     // Newton launches (parameters, derived constants, fallback list)
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
+    // stream of the call that holds the scratch (set by the call's ordering
+    // guard): growth frees and allocates in that stream's order, after every
+    // earlier user, instead of synchronising the device
+    cudaStream_t order_stream = nullptr;
+    bool order_active = false;
+    bool order_capturing = false;
     // kernel timing records (sp_profile_enable)
     bool profiling = false;
     struct Rec {
@@ -146,6 +152,40 @@ inline int tune_bucket(long long n) {
 }
 // The tuned value of setting `name` at size n, or dflt when none was set.
 int tune_get(sp_ctx* ctx, const char* name, long long n, int dflt);
+
+// Grow a context-owned device buffer (*buf, *have bytes) to at least `bytes`;
+// see api.cu.  Returns an SP_* status.
+int grow_buffer(sp_ctx* ctx, void** buf, size_t* have, size_t bytes, const char* what);
+
+// Calls on different streams share the context's buffers (scratch, second
+// buffer, network workspaces): each call orders itself after the previous user
+// (skipped while the stream is being captured into a CUDA graph, where the
+// caller orders the work), and buffer growth inside the guard is ordered on
+// the call's stream.
+struct ScratchOrder {
+    sp_ctx* ctx;
+    cudaStream_t st;
+    bool capturing = false;
+    cudaStream_t prev_stream;
+    bool prev_active, prev_capturing;
+    ScratchOrder(sp_ctx* c, cudaStream_t s)
+        : ctx(c), st(s), prev_stream(c->order_stream), prev_active(c->order_active),
+          prev_capturing(c->order_capturing) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cs);
+        capturing = cs != cudaStreamCaptureStatusNone;
+        if (!capturing) cudaStreamWaitEvent(st, ctx->scratch_done, 0);
+        ctx->order_stream = st;
+        ctx->order_active = true;
+        ctx->order_capturing = capturing;
+    }
+    ~ScratchOrder() {
+        if (!capturing) cudaEventRecord(ctx->scratch_done, st);
+        ctx->order_stream = prev_stream;
+        ctx->order_active = prev_active;
+        ctx->order_capturing = prev_capturing;
+    }
+};
 
 // Brackets one kernel launch with events when the context is profiling.
 struct ProfScope {

@@ -564,11 +564,6 @@ constexpr uint64_t kMaxRows = 1u << 22;  // keeps every element index of the wor
 int ensure_ws(sp_mlp* m, int rows) {
     const int rp = (rows + 63) & ~63;
     if (rp <= m->ws_rows) return SP_OK;
-    if (m->ws) {
-        cudaDeviceSynchronize();
-        cudaFree(m->ws);
-        m->ws = nullptr;
-    }
     const int Hd = m->H, nl = m->L - 1;
     size_t b = 0;
     auto take = [&](size_t bytes) {
@@ -590,10 +585,14 @@ int ensure_ws(sp_mlp* m, int rows) {
     size_t maxw = (size_t)Hd * std::max(Hd, std::max(m->kin, m->kout));
     size_t opart = take(4ull * splits * maxw);
     size_t oloss = take(256);
-    cudaError_t e = cudaMalloc(&m->ws, b);
-    if (e != cudaSuccess) return SP_ERR_MEMORY_ALLOC;
+    // the callers hold the context's ordering guard: the old workspace is
+    // freed in stream order after its last user
+    const int rc = grow_buffer(m->ctx, &m->ws, &m->ws_bytes, b, "MLP workspace");
+    if (rc != SP_OK) {
+        m->ws_rows = 0;
+        return rc;
+    }
     char* p = (char*)m->ws;
-    m->ws_bytes = b;
     m->ws_rows = rp;
     m->X = (bf16*)(p + oX);
     m->Xt = (bf16*)(p + oXt);
@@ -843,8 +842,12 @@ int sp_mlp_destroy(sp_mlp* m) {
     if (!m) return SP_OK;
     cudaSetDevice(m->ctx->device);
     cudaDeviceSynchronize();
+    if (m->ws) {  // from the stream-ordered allocator
+        cudaFreeAsync(m->ws, m->ctx->stream);
+        cudaStreamSynchronize(m->ctx->stream);
+    }
     for (void* p : {(void*)m->params, (void*)m->adam_m, (void*)m->adam_v, (void*)m->grads, (void*)m->wt_bf,
-                    (void*)m->w_bf, (void*)m->step, (void*)m->io_slots, (void*)m->io, m->ws, (void*)m->lin,
+                    (void*)m->w_bf, (void*)m->step, (void*)m->io_slots, (void*)m->io, (void*)m->lin,
                     (void*)m->lin_f32, m->tc_img, (void*)m->tc_bias, (void*)m->tc_err})
         if (p) cudaFree(p);
     delete m;
@@ -907,6 +910,7 @@ int sp_mlp_forward_device(sp_mlp* m, const float* d_x, uint64_t rows, float* d_y
     std::lock_guard<std::mutex> g(m->ctx->mu);
     cudaSetDevice(m->ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
+    ScratchOrder order(m->ctx, st);  // orders workspace reuse and growth after earlier users
     if (ensure_ws(m, (int)rows) != SP_OK) return mlp_fail(m->ctx, SP_ERR_MEMORY_ALLOC, "MLP workspace");
     const int rp = ((int)rows + 63) & ~63;
     ProfScope prof(m->ctx, "mlp_forward", st);
@@ -927,6 +931,7 @@ int sp_mlp_gradients_device(sp_mlp* m, const float* d_x, const float* d_t, uint6
     std::lock_guard<std::mutex> g(m->ctx->mu);
     cudaSetDevice(m->ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
+    ScratchOrder order(m->ctx, st);  // orders workspace reuse and growth after earlier users
     if (ensure_ws(m, (int)rows) != SP_OK) return mlp_fail(m->ctx, SP_ERR_MEMORY_ALLOC, "MLP workspace");
     const int rp = (int)rows;
     pack_inputs<<<(rp * m->kin + 255) / 256, 256, 0, st>>>(d_x, rp, rp, m->d.n_in, m->kin, m->X, m->Xt);
@@ -946,6 +951,7 @@ int sp_mlp_train_device(sp_mlp* m, const float* d_x, const float* d_t, uint64_t 
     std::lock_guard<std::mutex> g(m->ctx->mu);
     cudaSetDevice(m->ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
+    ScratchOrder order(m->ctx, st);  // orders workspace reuse and growth after earlier users
     if (ensure_ws(m, batch) != SP_OK) return mlp_fail(m->ctx, SP_ERR_MEMORY_ALLOC, "MLP workspace");
     const uint64_t steps_per_epoch = rows / batch;
     const int total = (int)(steps_per_epoch * epochs);
@@ -1014,6 +1020,7 @@ extern "C" int sp_mlp_warm_start_device(sp_mlp* m, const double* d_params_soa, u
     std::lock_guard<std::mutex> g(m->ctx->mu);
     cudaSetDevice(m->ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
+    ScratchOrder order(m->ctx, st);  // orders workspace reuse and growth after earlier users
     ProfScope prof(m->ctx, "mlp_warm_start", st);
     if (sp::mlp_warm_start(m, d_params_soa, (size_t)stride, (int)rows, d_x0, st) != cudaSuccess)
         return mlp_fail(m->ctx, SP_ERR_BACKEND, "warm-start inference launch");

@@ -686,16 +686,34 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots
                     float v[32];
                     tmem_ld32(tmem + lane_base + (uint32_t)(T * 256), v);  // the output layer is 32 wide
                     if (live) {
-                        // x[o] = out_mean + out_scale (y + b), then the linear term input by
-                        // input (the centred inputs are re-read: they were not kept live)
+                        // x[o] = out_mean + out_scale (y + b) + sum_j lin[o][j] (p_j - in_mean[j]);
+                        // the centred inputs are read again, sixteen at a time with every load
+                        // of a group issued before its first use
 #pragma unroll
                         for (int o = 0; o < 32; ++o)
                             v[o] = o < a.n_out ? out_mean[o] + out_scale[o] * (v[o] + bias[o]) : 0.f;
-                        for (int j = 0; j < a.n_in; ++j) {
-                            const float pj = f64_to_f32(a.params_soa[(size_t)slots_s[j] * a.stride + s]) - in_mean[j];
+                        const bool wide = a.n_out > 16;
+                        for (int jb = 0; jb < a.n_in; jb += 16) {
+                            float pc[16];
 #pragma unroll
-                            for (int o = 0; o < 32; ++o)
-                                if (o < a.n_out) v[o] = fmaf(lin_s[o * a.n_in + j], pj, v[o]);
+                            for (int t = 0; t < 16; ++t)
+                                pc[t] = jb + t < a.n_in
+                                            ? f64_to_f32(a.params_soa[(size_t)slots_s[jb + t] * a.stride + s]) - in_mean[jb + t]
+                                            : 0.f;
+#pragma unroll
+                            for (int t = 0; t < 16; ++t) {
+                                if (jb + t < a.n_in) {
+                                    const int j = jb + t;
+#pragma unroll
+                                    for (int o = 0; o < 16; ++o)
+                                        if (o < a.n_out) v[o] = fmaf(lin_s[o * a.n_in + j], pc[t], v[o]);
+                                    if (wide) {
+#pragma unroll
+                                        for (int o = 16; o < 32; ++o)
+                                            if (o < a.n_out) v[o] = fmaf(lin_s[o * a.n_in + j], pc[t], v[o]);
+                                    }
+                                }
+                            }
                         }
 #pragma unroll
                         for (int o = 0; o < 32; ++o)
