@@ -147,8 +147,11 @@ __global__ void fma_chain(T* out, int iters, T a, T b) {
     }
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
-// one three-input logic operation per value and step, each mixing two
-// values so that no step folds away: the integer ALU pipe alone
+// three-input logic operations mixing the eight values: the integer ALU
+// pipe alone.  nvcc 13.0 emits four ALU instructions per iteration for these
+// eight lines (ncu: smsp__inst_executed_pipe_alu.sum = 4 x iterations x
+// threads / 32, with the ALU pipe at 99.98 % of its peak), so the rate below
+// counts four instructions per iteration and thread
 __global__ void alu_chain(unsigned* out, int iters, unsigned a, unsigned b) {
     unsigned x0 = threadIdx.x ^ b, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
              x7 = x0 + 7;
@@ -174,7 +177,7 @@ static float timed(K k, int blocks, A... a) {
     cudaEventDestroy(e1);
     return ms;
 }
-// out: FP64 TFLOP/s, FP32 TFLOP/s (an FMA counts two), integer ALU Tops/s
+// out: FP64 TFLOP/s, FP32 TFLOP/s (an FMA counts two), integer ALU T instructions/s (per thread)
 extern "C" int pipe_peaks(double* out) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
@@ -187,7 +190,7 @@ extern "C" int pipe_peaks(double* out) {
     ms = timed(fma_chain<float>, blocks, (float*)buf, i32, 0.999f, 0.001f);
     out[1] = 2.0 * 8 * (double)i32 * blocks * threads / (ms * 1e9);
     ms = timed(alu_chain, blocks, (unsigned*)buf, ialu, 0x9e3779b9u, 0x7f4a7c15u);
-    out[2] = 8.0 * (double)ialu * blocks * threads / (ms * 1e9);
+    out[2] = 4.0 * (double)ialu * blocks * threads / (ms * 1e9);
     cudaFree(buf);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
@@ -660,10 +663,13 @@ def main():
         entry = {"avg_launch_ms": ms, "bytes_per_launch": by,
                  "hbm_frac": by / (ms * 1e-3) / 1e9 / hbm_peak,
                  "traffic": read_profile_number("draw_params_opamp.md", "dram_bytes_per_launch")}
+        f64i = read_profile_number("draw_params_opamp.md", "fp64_warp_instructions_per_sample")
+        if f64i:
+            entry["fp64_frac"] = f64i * 32 * N / (ms * 1e-3) / 1e12 / (fp64_peak / 2)
         if inst and alu_peak:
             a = inst * 32 * N / (ms * 1e-3) / 1e12
-            entry.update({"bound": "int_alu", "achieved": a, "peak": alu_peak, "unit": "T ALU ops/s",
-                          "frac": a / alu_peak, "peak_source": "logic-op chains measured live by this bench",
+            entry.update({"bound": "int_alu", "achieved": a, "peak": alu_peak, "unit": "T ALU instructions/s",
+                          "frac": a / alu_peak, "peak_source": "logic-op chains measured live by this bench (instruction count per iteration from ncu)",
                           "note": "integer ALU ops per sample from the committed ncu capture "
                                   "(sm__inst_executed_pipe_alu), times the live launch duration"})
         else:

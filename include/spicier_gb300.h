@@ -634,6 +634,16 @@ enum sp_mlp_kernel {
     SP_MLP_KERNEL_LAYERED = 3
 };
 int sp_mlp_set_inference_kernel(sp_mlp* mlp, int kind);
+/* Kernel of the training GEMMs (forward, data gradient, weight gradient):
+ * AUTO and TCGEN05 run them on the tensor cores (tcgen05.mma, FP32
+ * accumulators in TMEM; TCGEN05 requires a hidden width that is a multiple of
+ * 16), MMA_SYNC on the legacy mma.sync kernel.  LAYERED is not a training
+ * kernel. */
+int sp_mlp_set_training_kernel(sp_mlp* mlp, int kind);
+/* Waits for the device, then *fault = 1 if a tcgen05 training GEMM gave up a
+ * bounded wait (its results are invalid), | 2 if the tcgen05 warm start did
+ * (those samples started cold); 0 otherwise.  The flags are sticky. */
+int sp_mlp_fault(sp_mlp* mlp, int* fault);
 /* The warm start alone: x0[rows][n_out] (FP64) from per-sample parameters in
  * structure-of-arrays layout (parameter slot s of sample i at
  * d_params_soa[s * stride + i]), with the I/O mapping and linear term above. */

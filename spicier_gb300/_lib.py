@@ -93,6 +93,8 @@ def _bind(L):
         "sp_mlp_set_io": (i32, [vp, vp, vp, vp, vp, vp]),
         "sp_mlp_set_linear": (i32, [vp, vp]),
         "sp_mlp_set_inference_kernel": (i32, [vp, i32]),
+        "sp_mlp_set_training_kernel": (i32, [vp, i32]),
+        "sp_mlp_fault": (i32, [vp, P(i32)]),
         "sp_mlp_warm_start_device": (i32, [vp, vp, u64, u64, vp, vp]),
         "sp_mlp_forward_device": (i32, [vp, vp, u64, vp, vp]),
         "sp_mlp_gradients_device": (i32, [vp, vp, vp, u64, vp, vp, vp]),

@@ -463,6 +463,17 @@ class Mlp:
         """abi.SP_MLP_KERNEL_{AUTO,TCGEN05,MMA_SYNC,LAYERED} for the warm start."""
         check(self.ctx._ptr, load().sp_mlp_set_inference_kernel(self._ptr, kind))
 
+    def set_training_kernel(self, kind: int):
+        """abi.SP_MLP_KERNEL_{AUTO,TCGEN05,MMA_SYNC} for the training GEMMs."""
+        check(self.ctx._ptr, load().sp_mlp_set_training_kernel(self._ptr, kind))
+
+    def fault(self) -> int:
+        """Waits for the device; 1 if a tcgen05 training GEMM gave up a bounded
+        wait, | 2 if the tcgen05 warm start did (sticky flags), else 0."""
+        v = C.c_int(0)
+        check(self.ctx._ptr, load().sp_mlp_fault(self._ptr, C.byref(v)))
+        return v.value
+
     def warm_start_device(self, params_soa, stride, rows, x0, stream=0):
         """x0[rows][n_out] (FP64) from SoA parameters (slot s of sample i at s*stride+i)."""
         check(self.ctx._ptr, load().sp_mlp_warm_start_device(self._ptr, _vp(params_soa), stride, rows, _vp(x0),

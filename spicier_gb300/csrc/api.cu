@@ -419,7 +419,11 @@ int sp_topology_create(sp_ctx* ctx, const sp_circuit* c, sp_topology** out) {
     size_t bu = align256(sizeof(sp_pulse) * c->num_pulses);
     size_t bo = align256(sizeof(int) * c->num_elements);
     size_t bn = align256(sizeof(double) * t->n);
-    cudaError_t e = cudaMalloc(&t->dev, be + bp + bu + bo + bn + 256);
+    std::vector<int> drawn;
+    for (int k = 0; k < c->num_params; ++k)
+        if (c->params[k].kind != SP_DRAW_FIXED) drawn.push_back(k);
+    size_t bw = align256(sizeof(int) * drawn.size());
+    cudaError_t e = cudaMalloc(&t->dev, be + bp + bu + bo + bn + bw + 256);
     if (e != cudaSuccess) {
         delete t;
         return cuda_fail(ctx, e, "topology allocation");
@@ -430,7 +434,10 @@ int sp_topology_create(sp_ctx* ctx, const sp_circuit* c, sp_topology** out) {
     sp_pulse* dpul = (sp_pulse*)(b + be + bp);
     int* ddoff = (int*)(b + be + bp + bu);
     double* dns = (double*)(b + be + bp + bu + bo);
+    int* ddrawn = (int*)(b + be + bp + bu + bo + bn);
     if (c->num_elements) e = cudaMemcpy(del, c->elements, sizeof(sp_element) * c->num_elements, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !drawn.empty())
+        e = cudaMemcpy(ddrawn, drawn.data(), sizeof(int) * drawn.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && c->num_params)
         e = cudaMemcpy(dpar, c->params, sizeof(sp_param) * c->num_params, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && c->num_pulses)
@@ -445,6 +452,8 @@ int sp_topology_create(sp_ctx* ctx, const sp_circuit* c, sp_topology** out) {
     }
     t->dc = DevCircuit{c->num_nodes, c->num_branches, t->n, c->num_elements, c->num_params, nd,
                        del, dpar, dpul, ddoff, c->nodeset ? dns : nullptr};
+    t->d_drawn = ddrawn;
+    t->num_drawn = (int)drawn.size();
     t->h_elements.assign(c->elements, c->elements + c->num_elements);
     t->h_params.assign(c->params, c->params + c->num_params);
     if (c->nodeset) t->h_nodeset.assign(c->nodeset, c->nodeset + t->n);
@@ -567,10 +576,11 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     NewtonScratch s;
     int rc = newton_scratch(ctx, t, count, s, warm != nullptr);
     if (rc) return rc;
-    // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64)
-    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 16, st), "clear counters");
+    // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64),
+    // [4] draw group counter
+    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 32, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
-                 s.counters + 1};
+                 s.counters + 1, t->d_drawn, t->num_drawn, s.counters + 4};
     {
         ProfScope prof(ctx, "draw_params", st);
         SP_CUDA(ctx, launch_draw(D, st), "draw launch");
@@ -802,9 +812,9 @@ int sp_draw_params_device(sp_ctx* ctx, const sp_topology* t, uint64_t seed, uint
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     ScratchOrder order(ctx, st);
-    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 8, st), "clear counters");
+    SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 32, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, num_samples, d_table, table_cols, s.params, s.derived, d_params,
-                 s.counters + 1};
+                 s.counters + 1, t->d_drawn, t->num_drawn, s.counters + 4};
     SP_CUDA(ctx, launch_draw(D, st), "draw launch");
     return SP_OK;
 }

@@ -29,6 +29,9 @@ struct DrawLaunch {
     double* derived_soa;  // [num_derived][count]
     double* params_out;   // [count][num_params] or nullptr
     unsigned int* hard;   // count of draws whose rounding was undecided (or nullptr)
+    const int* drawn;     // [num_drawn] slots whose kind is not SP_DRAW_FIXED (device), ascending
+    int num_drawn;
+    unsigned int* next;   // zeroed group counter of the persistent draw kernel, or nullptr
 };
 
 cudaError_t launch_bsim3_eval(int pmos, const double* card, const double* bias, uint64_t count, double* out,
@@ -223,8 +226,10 @@ struct sp_topology {
     int num_pulses = 0;
     bool has_table = false;
     uint32_t min_table_cols = 0;  // 1 + largest table column any parameter reads
-    void* dev = nullptr;  // one allocation: elements, params, pulses, doff, nodeset
+    void* dev = nullptr;  // one allocation: elements, params, pulses, doff, nodeset, drawn slots
     sp::DevCircuit dc{};
+    int* d_drawn = nullptr;  // slots whose kind is not SP_DRAW_FIXED, ascending (inside `dev`)
+    int num_drawn = 0;
     // host copy of the description (for the specialiser)
     std::vector<sp_element> h_elements;
     std::vector<sp_param> h_params;

@@ -27,43 +27,78 @@ __device__ inline double draw_one(const sp_param& p, uint64_t seed, uint32_t swe
     return CUDART_NAN;
 }
 
-// One block = 32 samples x 8 lanes: lane y draws parameter slots y, y+8, ...
-// of its sample (the draws are long integer computations, so eight threads
-// per sample keep the SMs busy), then, after the block barrier, derives the
-// constants of elements y, y+8, ... from the slots the block just wrote.
+// Persistent draw kernel: each block takes groups of 32 samples from a
+// device counter (a static stride without one) and, per group,
+//
+//   draws     warp w draws the non-fixed slots drawn[w], drawn[w + 8], ...
+//             of the 32 samples (one distribution per warp), then writes
+//             its share of the fixed slots;
+//   derives   after the block barrier, lane y derives the constants of
+//             elements y, y + 8, ... of each sample (fixed slots read from
+//             the circuit, drawn ones from the values just written).
+//
+// A Gaussian is about a thousand integer instructions plus a few FP64 ones
+// (the products and the square root), so the kernel is bound by the integer
+// ALU pipe; taking groups from a counter keeps every SM busy to the end,
+// where a fixed grid of short blocks would leave its last partial wave.
 constexpr int kDrawSamples = 32, kDrawLanes = 8;
 
 __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_kernel(DrawLaunch L) {
     pdl_wait();
     pdl_trigger();
-    const uint64_t s = (uint64_t)blockIdx.x * kDrawSamples + threadIdx.x;
-    const bool live = s < L.count;
+    __shared__ unsigned int group_s;
     const DevCircuit& c = L.c;
-    const uint32_t sweep = (uint32_t)(L.first_index + s);
-    const double* row = (L.table && live) ? L.table + s * L.table_cols : nullptr;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const uint64_t groups = (L.count + kDrawSamples - 1) / kDrawSamples;
     unsigned hard = 0;
-    if (live) {
-        for (int k = threadIdx.y; k < c.num_params; k += kDrawLanes) {
-            const double v = draw_one(c.par[k], L.seed, sweep, row, &hard);
-            L.params_soa[(size_t)k * L.count + s] = v;
-            if (L.params_out) L.params_out[s * c.num_params + k] = v;
+    for (uint64_t it = 0;; ++it) {
+        if (lane == 0 && warp == 0) group_s = L.next ? atomicAdd(L.next, 1u) : (unsigned)(blockIdx.x + it * gridDim.x);
+        __syncthreads();
+        const uint64_t g = L.next ? (uint64_t)group_s : blockIdx.x + it * gridDim.x;
+        if (g >= groups) break;  // the same value in every thread of the block
+        const uint64_t s = g * kDrawSamples + (uint64_t)lane;
+        const bool live = s < L.count;
+        const uint32_t sweep = (uint32_t)(L.first_index + s);
+        if (live) {
+            const double* row = L.table ? L.table + s * L.table_cols : nullptr;
+            for (int d = warp; d < L.num_drawn; d += kDrawLanes) {
+                const int k = L.drawn[d];
+                const double v = draw_one(c.par[k], L.seed, sweep, row, &hard);
+                L.params_soa[(size_t)k * L.count + s] = v;
+                if (L.params_out) L.params_out[s * c.num_params + k] = v;
+            }
+            for (int k = warp; k < c.num_params; k += kDrawLanes) {
+                const sp_param p = c.par[k];
+                if (p.kind != SP_DRAW_FIXED) continue;
+                L.params_soa[(size_t)k * L.count + s] = p.a;
+                if (L.params_out) L.params_out[s * c.num_params + k] = p.a;
+            }
+        }
+        __syncthreads();  // this group's parameter slots are written (group_s is read by all)
+        if (!live) continue;
+        auto P = [&](int slot) {
+            const sp_param& p = c.par[slot];
+            return p.kind == SP_DRAW_FIXED ? p.a : L.params_soa[(size_t)slot * L.count + s];
+        };
+        for (int e = warp; e < c.num_elements; e += kDrawLanes) {
+            const sp_element el = c.el[e];
+            double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
+            const size_t st = L.count;
+            derive_element(el, P, [&](int k, double v) { out[k * st] = v; });
         }
     }
     if (hard && L.hard) atomicAdd(L.hard, hard);
-    __syncthreads();  // this block's parameter slots are written
-    if (!live) return;
-    auto P = [&](int slot) { return L.params_soa[(size_t)slot * L.count + s]; };
-    for (int e = threadIdx.y; e < c.num_elements; e += kDrawLanes) {
-        const sp_element el = c.el[e];
-        double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
-        const size_t st = L.count;
-        derive_element(el, P, [&](int k, double v) { out[k * st] = v; });
-    }
 }
 
 cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st) {
     if (L.count == 0) return cudaSuccess;
-    const uint64_t grid = (L.count + kDrawSamples - 1) / kDrawSamples;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t groups = (L.count + kDrawSamples - 1) / kDrawSamples;
+    // resident blocks (four per SM at 64 registers); without a counter one block per group
+    const uint64_t grid = L.next ? std::min<uint64_t>(groups, (uint64_t)sms * 4) : groups;
     return launch_chained(draw_kernel, dim3((unsigned)grid), dim3(kDrawSamples, kDrawLanes), 0, st, L);
 }
 

@@ -46,6 +46,7 @@ struct GemmArgs {
     bf16* Ht;           // transposed copy [N][ldt]
     const bf16* Zin;    // EPI_GELU_BWD: stored pre-activation [M][ld]
     int ld, ldt;
+    int* tc_err = nullptr;  // non-null: run on the tensor cores (mlptc::gemm) where the shape allows
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
@@ -182,6 +183,14 @@ __global__ void __launch_bounds__(128) gemm_tn(GemmArgs g) {
 
 template <int EPI>
 cudaError_t gemm(const GemmArgs& g, int splits, cudaStream_t st) {
+    if (g.tc_err) {
+        static_assert(EPI_F32 == mlptc::kEpiF32 && EPI_BIAS_F32 == mlptc::kEpiBiasF32 &&
+                          EPI_BIAS_GELU == mlptc::kEpiBiasGelu && EPI_GELU_BWD == mlptc::kEpiGeluBwd,
+                      "epilogue codes");
+        mlptc::GemmTcArgs t{g.A, g.lda, g.B, g.ldb, g.M, g.N, g.K, g.k_split, g.C32, g.ldc, g.bias,
+                            g.Z, g.H, g.Ht, g.Zin, g.ld, g.ldt, EPI, g.tc_err, 0};
+        if (mlptc::gemm_supported(t)) return mlptc::gemm(t, splits, st);
+    }
     dim3 grid((g.M + BM - 1) / BM, (g.N + BN - 1) / BN, splits);
     gemm_tn<EPI><<<grid, 128, 0, st>>>(g);
     return cudaGetLastError();
@@ -525,6 +534,7 @@ struct sp_mlp {
     bool fused_ready = false;
     // tcgen05 inference (mlp_tc.cu): packed weight image, gathered biases
     int kernel_kind = SP_MLP_KERNEL_AUTO;
+    int train_kind = SP_MLP_KERNEL_AUTO;  // GEMMs of training: tcgen05 where the shape allows, or mma.sync
     bool tc_dirty = true;     // weights changed since the image was packed
     void* tc_img = nullptr;
     float* tc_bias = nullptr;
@@ -618,12 +628,19 @@ int ensure_ws(sp_mlp* m, int rows) {
 }
 
 // Forward over rows already packed into m->X (rows_pad rows); Y = outputs.
+// Error flag of the tcgen05 training GEMMs (an int inside the step block,
+// zeroed at creation), or nullptr when training runs on mma.sync.
+int* train_tc_err(const sp_mlp* m) {
+    return m->train_kind == SP_MLP_KERNEL_MMA_SYNC ? nullptr : m->step + 16;
+}
+
 cudaError_t forward(sp_mlp* m, int rows_pad, bool keep, cudaStream_t st) {
     const int nl = m->L - 1;
     const bf16* in = m->X;
     int kin = m->kin;
     for (int l = 0; l < nl; ++l) {
         GemmArgs g{};
+        g.tc_err = train_tc_err(m);
         g.A = in;
         g.lda = kin;
         g.B = m->wt_bf + m->woff[l];
@@ -645,6 +662,7 @@ cudaError_t forward(sp_mlp* m, int rows_pad, bool keep, cudaStream_t st) {
         (void)keep;
     }
     GemmArgs g{};
+    g.tc_err = train_tc_err(m);
     g.A = in;
     g.lda = kin;
     g.B = m->wt_bf + m->woff[nl];
@@ -679,6 +697,7 @@ cudaError_t backward(sp_mlp* m, int rows_pad, const float* targets, int ldt_in, 
         const int in_w = (l == 0) ? m->kin : m->H;
         // weight gradient: dWt[out][in] = dZ^T [out][rows] * (H^T [in][rows])^T
         GemmArgs g{};
+        g.tc_err = train_tc_err(m);
         g.A = dcurT;
         g.lda = rows_pad;
         g.B = inT;
@@ -707,6 +726,7 @@ cudaError_t backward(sp_mlp* m, int rows_pad, const float* targets, int ldt_in, 
         bf16* dnT = toggle ? m->dBt : m->dAt;
         toggle = !toggle;
         GemmArgs h{};
+        h.tc_err = train_tc_err(m);
         h.A = dcur;
         h.lda = width;
         h.B = m->w_bf + m->woff[l];  // W [in][out]
@@ -1011,6 +1031,29 @@ extern "C" int sp_mlp_set_inference_kernel(sp_mlp* m, int kind) {
     return SP_OK;
 }
 
+extern "C" int sp_mlp_set_training_kernel(sp_mlp* m, int kind) {
+    if (!m || (kind != SP_MLP_KERNEL_AUTO && kind != SP_MLP_KERNEL_TCGEN05 && kind != SP_MLP_KERNEL_MMA_SYNC))
+        return SP_ERR_INVALID_ARGUMENT;
+    if (kind == SP_MLP_KERNEL_TCGEN05 && m->H % 16 != 0)
+        return mlp_fail(m->ctx, SP_ERR_INVALID_DIMENSION, "tcgen05 training needs a hidden width that is a multiple of 16");
+    std::lock_guard<std::mutex> g(m->ctx->mu);
+    m->train_kind = kind;
+    return SP_OK;
+}
+
+extern "C" int sp_mlp_fault(sp_mlp* m, int* fault) {
+    if (!m || !fault) return SP_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(m->ctx->mu);
+    cudaSetDevice(m->ctx->device);
+    int a = 0, b = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&a, m->step + 16, 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && m->tc_err) e = cudaMemcpy(&b, m->tc_err, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return SP_ERR_TRANSFER;
+    *fault = (a ? 1 : 0) | (b ? 2 : 0);
+    return SP_OK;
+}
+
 extern "C" int sp_mlp_warm_start_device(sp_mlp* m, const double* d_params_soa, uint64_t stride, uint64_t rows,
                                         double* d_x0, void* stream) {
     if (!m || !d_params_soa || !d_x0) return SP_ERR_INVALID_ARGUMENT;
@@ -1042,6 +1085,9 @@ cudaError_t tc_warm_start(sp_mlp* m, const double* params_soa, size_t stride, in
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
         if (e != cudaSuccess) return e;
     }
+    // weights packed by an earlier call are complete before this call's kernels
+    // start; weights packed now are not (the copies below precede the kernel)
+    a.early_prologue = m->tc_dirty ? 0 : 1;
     if (m->tc_dirty) {
         cudaError_t e = mlptc::pack(m->wt_bf, m->woff.data(), a, m->tc_img, st);
         for (int l = 0; l < m->L && e == cudaSuccess; ++l)

@@ -253,7 +253,11 @@ __host__ __device__ inline int teams_for(const Args& a) {
 
 __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int teams) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    pdl_wait();  // the drawn parameters (and the packed weights) are complete and visible
+    // Under programmatic dependent launch a CTA can start while the previous
+    // kernel (the parameter draws) drains.  Only the drawn parameters depend
+    // on it: with early_prologue the weight copy, the constants and the TMEM
+    // allocation run first, overlapping that kernel's tail.
+    if (!a.early_prologue) pdl_wait();
     pdl_trigger();
     // 1024-byte alignment of the swizzled operands (the dynamic window may start lower)
     unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
@@ -298,6 +302,7 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
     tc_before();
     __syncthreads();
     tc_after();
+    if (a.early_prologue) pdl_wait();  // the drawn parameters are complete and visible
     const uint32_t tmem = *tmem_slot + (uint32_t)(team * 128);  // this team's 128 columns
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     unsigned char* abuf = sm + cv.abuf + team * kAbytes;
@@ -495,7 +500,10 @@ __device__ __forceinline__ int layer_units(const Layer& ly) { return ((ly.N + 12
 
 __global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    pdl_wait();  // the drawn parameters (and the packed weights) are complete and visible
+    // with early_prologue only the teams (which read the drawn parameters)
+    // wait for the previous kernel: the set-up and the producer's first
+    // weight copies overlap its tail (as in infer_kernel)
+    if (!a.early_prologue) pdl_wait();
     pdl_trigger();
     unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
     const SCarve cv = scarve(a, nslots);
@@ -531,6 +539,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots
     tc_before();
     __syncthreads();
     tc_after();
+    if (a.early_prologue && warp < kSProducerWarp) pdl_wait();  // teams: the drawn parameters are visible
     const uint32_t tmem = *tmem_slot;
     const int ntiles = (a.rows + kTile - 1) / kTile;
     // this CTA's tiles: k-th = blockIdx.x + k gridDim.x; tile k belongs to team k % 2
@@ -744,6 +753,157 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Training GEMMs: C[M][N] = A[M][K] B[N][K]^T with both operands K-major BF16
+// (the layouts the trainer keeps, transposed copies included) and FP32
+// accumulators in TMEM; the epilogues are those of the trainer's GEMMs.
+// One CTA of four warps per 128 x BN output tile (BN <= 256) and K range
+// (split-K along blockIdx.z): all threads copy 64-wide K-blocks of A and B
+// into a two-stage ring of 128-byte-swizzled tiles (cp.async, zero-filled
+// outside M, N and the K range); thread 0 issues the K-block's tcgen05.mma
+// (M = 128, N = BN, K = 16 each) and commits them to the stage's mbarrier,
+// which the copies into that stage wait for two K-blocks later; warp q then
+// reads accumulator lanes 32q..32q+31 (its 32 output rows) for the epilogue.
+// Waits are bounded: on a timeout the CTA raises *err, writes nothing and
+// frees its TMEM after the copies and MMAs it started have drained.
+constexpr int kGThreads = 128;
+constexpr uint32_t kGAbytes = 128u * 128u;  // one K-block of A: 128 rows x 64 BF16
+
+__host__ __device__ inline uint32_t gemm_stage_bytes(int bn) { return kGAbytes + (uint32_t)bn * 128u; }
+__host__ __device__ inline uint32_t gemm_smem_bytes(int bn) { return 1024u + 2u * gemm_stage_bytes(bn) + 64u; }
+
+__device__ __forceinline__ void cp_async16_zfill(uint32_t dst, const void* src, bool ok) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(kGThreads) gemm_kernel(GemmTcArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    const int bn = g.bn;
+    const uint32_t stage_bytes = gemm_stage_bytes(bn);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + 2 * stage_bytes);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + 2 * stage_bytes + 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * bn;
+    const int kb = blockIdx.z * g.k_split;
+    const int ke = min(g.K, kb + g.k_split);
+    const int natoms = ke > kb ? (ke - kb + 63) / 64 : 0;
+    const uint32_t tcols = bn <= 32 ? 32u : (bn <= 64 ? 64u : (bn <= 128 ? 128u : 256u));
+    if (tid == 0) {
+        for (int t = 0; t < 2; ++t)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[t])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(tcols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t base = smem_u32(sm);
+
+    // K-block t into stage t & 1: A rows m0.., B rows n0.., 16-byte chunks
+    auto load = [&](int t) {
+        const uint32_t sa = base + (uint32_t)(t & 1) * stage_bytes, sb = sa + kGAbytes;
+        const int k0 = kb + t * 64;
+        for (int i = tid; i < (128 + bn) * 8; i += kGThreads) {
+            const int r = i >> 3, c = i & 7, k = k0 + c * 8;
+            if (r < 128) {
+                const bool ok = m0 + r < g.M && k < ke;
+                cp_async16_zfill(sa + sw128_offset(128, r, c), ok ? (const void*)(g.A + (size_t)(m0 + r) * g.lda + k)
+                                                               : (const void*)g.A, ok);
+            } else {
+                const int rb = r - 128;
+                const bool ok = n0 + rb < g.N && k < ke;
+                cp_async16_zfill(sb + sw128_offset(bn, rb, c), ok ? (const void*)(g.B + (size_t)(n0 + rb) * g.ldb + k)
+                                                                : (const void*)g.B, ok);
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+
+    bool ok = true;
+    if (natoms > 0) load(0);
+    for (int t = 0; t < natoms; ++t) {
+        if (t + 1 < natoms) {
+            // stage (t + 1) & 1 was last read by the MMAs of K-block t - 1
+            // (the vote keeps the block's barriers uniform if a wait gives up)
+            if (t >= 1) ok = __syncthreads_and(mbar_wait(smem_u32(&mbar[(t + 1) & 1]), (uint32_t)(((t - 1) >> 1) & 1)));
+            if (!ok) break;
+            load(t + 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        fence_async_smem();  // this thread's copies -> visible to the tensor cores
+        tc_before();
+        __syncthreads();
+        tc_after();
+        if (tid == 0) {
+            const uint32_t sa = base + (uint32_t)(t & 1) * stage_bytes, sb = sa + kGAbytes;
+            const int rem = ke - (kb + t * 64);
+            const int ksteps = rem >= 64 ? 4 : (rem + 15) / 16;
+            const uint32_t id = idesc_bf16(bn);
+            for (int k = 0; k < ksteps; ++k)
+                mma_bf16_ss(tmem, sdesc(sa + (uint32_t)k * 32u), sdesc(sb + (uint32_t)k * 32u), id, (t | k) != 0);
+            mma_commit(smem_u32(&mbar[t & 1]));
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    // the last K-block's MMAs (every earlier commit completes before it)
+    if (ok && natoms > 0) ok = mbar_wait(smem_u32(&mbar[(natoms - 1) & 1]), (uint32_t)(((natoms - 1) >> 1) & 1));
+    ok = __syncthreads_and(ok);
+    tc_after();
+    if (!ok) {
+        if (tid == 0) atomicExch(g.err, 1);
+    } else {
+        const int row = m0 + warp * 32 + lane;
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        for (int c0 = 0; c0 < bn; c0 += 32) {
+            float v[32];
+            if (natoms > 0) {
+                tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = 0.f;
+            }
+            if (row >= g.M) continue;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int col = n0 + c0 + j;
+                if (c0 + j >= bn || col >= g.N) continue;
+                if (EPI == kEpiF32) {
+                    g.C32[((size_t)blockIdx.z * g.M + row) * g.ldc + col] = v[j];
+                } else if (EPI == kEpiBiasF32) {
+                    g.C32[(size_t)row * g.ldc + col] = v[j] + g.bias[col];
+                } else if (EPI == kEpiBiasGelu) {
+                    const float z = v[j] + g.bias[col];
+                    const __nv_bfloat16 h = __float2bfloat16(act::gelu(z));
+                    g.Z[(size_t)row * g.ld + col] = __float2bfloat16(z);
+                    g.H[(size_t)row * g.ld + col] = h;
+                    g.Ht[(size_t)col * g.ldt + row] = h;
+                } else {
+                    const float z = __bfloat162float(g.Zin[(size_t)row * g.ld + col]);
+                    const __nv_bfloat16 d = __float2bfloat16(v[j] * act::gelu_grad(z));
+                    g.H[(size_t)row * g.ld + col] = d;
+                    g.Ht[(size_t)col * g.ldt + row] = d;
+                }
+            }
+        }
+    }
+    // every MMA has completed (waited above, or the bounded wait gave up)
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols) : "memory");
+}
+
 }  // namespace
 
 bool supported(int n_in, int n_out, int hidden, int gemm_layers) {
@@ -829,6 +989,45 @@ cudaError_t launch(const Args& a, int num_sms, cudaStream_t st) {
     if (grid > num_sms) grid = num_sms;
     if (grid < 1) return cudaSuccess;
     return launch_chained(infer_kernel, dim3(grid), dim3(teams * kTeam), smem, st, a, teams);
+}
+
+bool gemm_supported(const GemmTcArgs& g) {
+    return g.M > 0 && g.N > 0 && g.N % 16 == 0 && g.K % 8 == 0 && g.k_split % 8 == 0 && g.k_split > 0 &&
+           g.lda % 8 == 0 && g.ldb % 8 == 0 && g.epi >= kEpiF32 && g.epi <= kEpiGeluBwd && g.err != nullptr;
+}
+
+cudaError_t gemm(GemmTcArgs g, int splits, cudaStream_t st) {
+    if (!gemm_supported(g) || splits < 1) return cudaErrorInvalidValue;
+    g.bn = g.N <= 256 ? g.N : 256;  // a multiple of 16
+    const uint32_t smem = gemm_smem_bytes(g.bn);
+    static std::mutex mu;
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (dev < 0 || dev >= 64 || !configured[dev]) {
+            const int lim = (int)gemm_smem_bytes(256);
+            e = cudaFuncSetAttribute(gemm_kernel<kEpiF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(gemm_kernel<kEpiBiasF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(gemm_kernel<kEpiBiasGelu>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(gemm_kernel<kEpiGeluBwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+            if (e != cudaSuccess) return e;
+            if (dev >= 0 && dev < 64) configured[dev] = true;
+        }
+    }
+    const dim3 grid((unsigned)((g.M + 127) / 128), (unsigned)((g.N + g.bn - 1) / g.bn), (unsigned)splits);
+    switch (g.epi) {
+        case kEpiF32: gemm_kernel<kEpiF32><<<grid, kGThreads, smem, st>>>(g); break;
+        case kEpiBiasF32: gemm_kernel<kEpiBiasF32><<<grid, kGThreads, smem, st>>>(g); break;
+        case kEpiBiasGelu: gemm_kernel<kEpiBiasGelu><<<grid, kGThreads, smem, st>>>(g); break;
+        default: gemm_kernel<kEpiGeluBwd><<<grid, kGThreads, smem, st>>>(g); break;
+    }
+    return cudaGetLastError();
 }
 
 }  // namespace mlptc

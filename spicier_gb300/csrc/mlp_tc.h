@@ -33,6 +33,8 @@ struct Args {
     int* err;                  // set to 1 when a bounded wait timed out
     int n_in, n_out, L, img_bytes, bias_total;
     int teams_pref;            // 0: the most tiles in flight that fit; else at most this many (tuned)
+    int early_prologue;        // 1: the weights, biases and I/O constants were complete before the previous
+                               // kernel of the stream began, so the CTA loads them before its dependency wait
     Layer layer[kMaxLayers];
 };
 
@@ -46,6 +48,36 @@ size_t smem_bytes(const Args& a);
 // Packs the row-major BF16 weights (layer l at wt + woff[l]) into the image.
 cudaError_t pack(const __nv_bfloat16* wt, const size_t* woff, const Args& a, void* img, cudaStream_t st);
 cudaError_t launch(const Args& a, int num_sms, cudaStream_t st);
+
+// Training GEMM C[M][N] = A[M][K] B[N][K]^T (BF16, K-major operands, FP32
+// accumulation) with one of the trainer's epilogues:
+//   kEpiF32       C32[z][M][ldc] = the partial sum of split z (split-K)
+//   kEpiBiasF32   C32[M][ldc] = C + bias
+//   kEpiBiasGelu  Z = C + bias, H = gelu(Z) (BF16 [M][ld]) and Ht = H^T ([N][ldt])
+//   kEpiGeluBwd   H = Ht^T = C * gelu'(Zin) (BF16)
+enum { kEpiF32 = 0, kEpiBiasF32 = 1, kEpiBiasGelu = 2, kEpiGeluBwd = 3 };
+struct GemmTcArgs {
+    const __nv_bfloat16* A;
+    int lda;
+    const __nv_bfloat16* B;
+    int ldb;
+    int M, N, K;
+    int k_split;  // K elements per blockIdx.z (multiple of 8)
+    float* C32;
+    int ldc;
+    const float* bias;
+    __nv_bfloat16* Z;
+    __nv_bfloat16* H;
+    __nv_bfloat16* Ht;
+    const __nv_bfloat16* Zin;
+    int ld, ldt;
+    int epi;
+    int* err;  // set to 1 when a bounded wait timed out
+    int bn;    // tile width (set by gemm())
+};
+// N a multiple of 16, K, k_split, lda and ldb multiples of 8.
+bool gemm_supported(const GemmTcArgs& g);
+cudaError_t gemm(GemmTcArgs g, int splits, cudaStream_t st);
 
 }  // namespace mlptc
 }  // namespace sp

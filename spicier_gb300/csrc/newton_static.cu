@@ -176,8 +176,9 @@ extern "C" int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_co
     const size_t bu = a256(sizeof(sp_pulse) * circuit->num_pulses);
     const size_t bo = a256(sizeof(int) * circuit->num_elements);
     const size_t bn = a256(sizeof(double) * n);
-    const size_t bc = 256;  // counters: [0] miss count, [1] undecided roundings
-    const size_t fixed = be + bp + bu + bo + bn + bc;
+    const size_t bc = 256;  // counters: [0] miss count, [1] undecided roundings, [4] draw groups
+    const size_t bw = a256(sizeof(int) * circuit->num_params);  // drawn (non-fixed) slots
+    const size_t fixed = be + bp + bu + bo + bn + bc + bw;
     const size_t per_sample = 8 * (size_t)(circuit->num_params + nd) + 4;
     const uint64_t max_samples = fixed + 3 * 256 < kStaticScratchBytes
                                      ? (kStaticScratchBytes - fixed - 3 * 256) / per_sample : 0;
@@ -210,6 +211,7 @@ extern "C" int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_co
     int* ddoff = (int*)(base + be + bp + bu);
     double* dns = (double*)(base + be + bp + bu + bo);
     unsigned int* counters = (unsigned int*)(base + be + bp + bu + bo + bn);
+    int* ddrawn = (int*)(base + be + bp + bu + bo + bn + bc);
     unsigned char* dyn = base + fixed;
     double* params_soa = (double*)dyn;
     double* derived_soa = (double*)(dyn + a256(8 * (size_t)circuit->num_params * num_samples));
@@ -218,6 +220,12 @@ extern "C" int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_co
     int doff[1024];
     if (circuit->num_elements > 1024)
         return report(err, err_len, SP_ERR_INVALID_DIMENSION, "more than 1024 elements");
+    int drawn[1024];
+    int num_drawn = 0;
+    if (circuit->num_params > 1024)
+        return report(err, err_len, SP_ERR_INVALID_DIMENSION, "more than 1024 parameters");
+    for (int k = 0; k < circuit->num_params; ++k)
+        if (circuit->params[k].kind != SP_DRAW_FIXED) drawn[num_drawn++] = k;
     for (int e = 0, o = 0; e < circuit->num_elements; ++e) {
         doff[e] = o;
         o += derived_count(circuit->elements[e].kind);
@@ -234,15 +242,17 @@ extern "C" int sp_newton_dc_static(const sp_circuit* circuit, const sp_newton_co
         e = cudaMemcpyAsync(ddoff, doff, sizeof(int) * circuit->num_elements, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && circuit->nodeset)
         e = cudaMemcpyAsync(dns, circuit->nodeset, sizeof(double) * n, cudaMemcpyHostToDevice, st);
-    // the miss counter starts at zero on every call
-    if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, 8, st);
+    if (e == cudaSuccess && num_drawn)
+        e = cudaMemcpyAsync(ddrawn, drawn, sizeof(int) * num_drawn, cudaMemcpyHostToDevice, st);
+    // the counters (misses, undecided roundings, draw groups) start at zero on every call
+    if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, 32, st);
     if (e != cudaSuccess)
         return report(err, err_len, SP_ERR_TRANSFER, "circuit upload: %s", cudaGetErrorString(e));
 
     DevCircuit dc{circuit->num_nodes, circuit->num_branches, n, circuit->num_elements, circuit->num_params, nd,
                   del, dpar, dpul, ddoff, circuit->nodeset ? dns : nullptr};
     DrawLaunch D{dc, seed, first_index, num_samples, d_table, table_cols, params_soa, derived_soa, nullptr,
-                 counters + 1};
+                 counters + 1, ddrawn, num_drawn, counters + 4};
     e = launch_draw(D, st);
     if (e != cudaSuccess) return report(err, err_len, SP_ERR_BACKEND, "draw launch: %s", cudaGetErrorString(e));
 

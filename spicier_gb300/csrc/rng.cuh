@@ -50,9 +50,17 @@ SP_HD double rng_gaussian(uint64_t seed, uint32_t sweep, uint32_t param, unsigne
     // max(u1, 1e-10) on the bit patterns (both non-negative)
     u1 = cr::dbits(u1) > 0x3DDB7CDFD9D7BDBBULL ? u1 : 1e-10;
     const double l = cr_log(u1, hard);  // < 0, normal
-    const double c = cr_cos(ieee_mul(6.283185307179586, u2), hard);
     // -2 l exactly: flip the sign and raise the exponent by one
-    return ieee_mul(ieee_sqrt(cr::bdouble((cr::dbits(l) ^ (1ULL << 63)) + (1ULL << 52))), c);
+    const double m2l = cr::bdouble((cr::dbits(l) ^ (1ULL << 63)) + (1ULL << 52));
+#if defined(__CUDA_ARCH__)
+    // the two products and the square root on the FP64 pipe (IEEE round to
+    // nearest, never contracted), which the integer-bound ln and cos leave idle
+    const double c = cr_cos(__dmul_rn(6.283185307179586, u2), hard);
+    return __dmul_rn(__dsqrt_rn(m2l), c);
+#else
+    const double c = cr_cos(6.283185307179586 * u2, hard);
+    return sqrt(m2l) * c;
+#endif
 }
 
 // FP32 variant (rng.rs:138-145): the reference's f32 ln/cos are not pinned

@@ -25,34 +25,84 @@ def net(ctx):
     m.close()
 
 
-def test_forward_matches_oracle(ctx, net):
+TRAIN_KINDS = [abi.SP_MLP_KERNEL_TCGEN05, abi.SP_MLP_KERNEL_MMA_SYNC]
+
+
+@pytest.mark.parametrize("kind", TRAIN_KINDS)
+def test_forward_matches_oracle(ctx, net, kind):
     rng = np.random.default_rng(0)
     rows = 200
     X = rng.standard_normal((rows, 10)).astype(np.float32)
     y = torch.empty((rows, 12), dtype=torch.float32, device="cuda")
-    net.forward_device(torch.tensor(X, device="cuda"), rows, y)
-    torch.cuda.synchronize()
+    net.set_training_kernel(kind)
+    try:
+        net.forward_device(torch.tensor(X, device="cuda"), rows, y)
+        torch.cuda.synchronize()
+    finally:
+        net.set_training_kernel(abi.SP_MLP_KERNEL_AUTO)
     layers = net.unflatten(net.get_params())
     Yo, _, _ = mo.forward_backward(layers, X, np.zeros((rows, 12), np.float32), 12)
     assert rel(y.cpu().numpy(), Yo[:, :12]) < 1e-2
 
 
-def test_gradients_match_oracle(ctx, net):
+def gradients(m, X, T, rows):
+    g = torch.empty(m.num_params, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    m.gradients_device(torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda"), rows, g, loss)
+    torch.cuda.synchronize()
+    return m.unflatten(g.cpu().numpy()), loss.item()
+
+
+@pytest.mark.parametrize("kind", TRAIN_KINDS)
+def test_gradients_match_oracle(ctx, net, kind):
     rng = np.random.default_rng(1)
     rows = 512
     X = rng.standard_normal((rows, 10)).astype(np.float32)
     T = rng.standard_normal((rows, 12)).astype(np.float32)
-    g = torch.empty(net.num_params, dtype=torch.float32, device="cuda")
-    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
-    net.gradients_device(torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda"), rows, g, loss)
-    torch.cuda.synchronize()
+    net.set_training_kernel(kind)
+    try:
+        gpu, loss = gradients(net, X, T, rows)
+    finally:
+        net.set_training_kernel(abi.SP_MLP_KERNEL_AUTO)
     layers = net.unflatten(net.get_params())
     _, lo, go = mo.forward_backward(layers, X, T, 12)
-    gpu = net.unflatten(g.cpu().numpy())
-    assert abs(loss.item() - lo) <= 1e-2 * lo
+    assert abs(loss - lo) <= 1e-2 * lo
     for l, ((dW, db), (oW, ob)) in enumerate(zip(gpu, go)):
         assert rel(dW, oW) < 3e-2, f"layer {l} weight gradient"
         assert rel(db, ob) < 3e-2, f"layer {l} bias gradient"
+    assert net.fault() == 0
+
+
+@pytest.mark.parametrize("H,nl,rows", [(128, 3, 576), (64, 2, 64), (256, 1, 1088), (96, 2, 320)])
+def test_tcgen05_training_gemms_against_mma_sync(ctx, H, nl, rows):
+    """The tcgen05 training GEMMs (every epilogue: bias + GELU with the
+    transposed copy, bias only, split-K weight gradients, GELU backward)
+    against the mma.sync kernel and the numpy oracle, on widths 64..256 and
+    row counts that leave partial 128-row tiles and single split-K chunks."""
+    n_in, n_out = 17, 12
+    m = Mlp(ctx, n_in, n_out, H, nl, seed=H + nl)
+    rng = np.random.default_rng(rows)
+    X = rng.standard_normal((rows, n_in)).astype(np.float32)
+    T = rng.standard_normal((rows, n_out)).astype(np.float32)
+    out = {}
+    for kind in TRAIN_KINDS:
+        m.set_training_kernel(kind)
+        out[kind] = gradients(m, X, T, rows)
+    layers = m.unflatten(m.get_params())
+    _, lo, go = mo.forward_backward(layers, X, T, n_out)
+    (gt, lt), (gm, lm) = out[TRAIN_KINDS[0]], out[TRAIN_KINDS[1]]
+    assert abs(lt - lo) <= 1e-2 * lo and abs(lm - lo) <= 1e-2 * lo
+    for l in range(len(go)):
+        for a, b, o in ((gt[l][0], gm[l][0], go[l][0]), (gt[l][1], gm[l][1], go[l][1])):
+            assert rel(a, o) < 3e-2 and rel(b, o) < 3e-2, l
+            assert rel(a, b) < 3e-2, l
+    assert m.fault() == 0
+    m.close()
+
+
+def test_training_kernel_selector_rejects_bad_kinds(ctx, net):
+    with pytest.raises(sg.SpicierError):
+        net.set_training_kernel(abi.SP_MLP_KERNEL_LAYERED)
 
 
 def test_training_is_deterministic_and_learns(ctx):
