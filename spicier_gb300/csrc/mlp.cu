@@ -568,7 +568,7 @@ int mlp_fail(sp_ctx* ctx, int code, const char* msg) {
     return code;
 }
 
-constexpr int kSplitRows = 512;  // batch rows per split of a weight-gradient GEMM
+constexpr int kSplitRows = 128;  // batch rows per split of a weight-gradient GEMM (one CTA each)
 constexpr uint64_t kMaxRows = 1u << 22;  // keeps every element index of the workspace within int
 
 int ensure_ws(sp_mlp* m, int rows) {

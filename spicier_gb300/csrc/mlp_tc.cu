@@ -321,12 +321,18 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
         const int s = tile * kTile + row;
         const bool live = s < a.rows;
         // inputs 0..31 of row `row` (chunks 0..3, kept in registers for the
-        // linear term); chunks 4..7 of the first K-block are zero
+        // linear term); chunks 4..7 of the first K-block are zero.  Every load
+        // is issued before the first conversion (the conversion branches, so
+        // interleaving them would serialise the loads' latencies)
         float pc[kMaxIn];
+        {
+            double raw[kMaxIn];
 #pragma unroll
-        for (int j = 0; j < kMaxIn; ++j)
-            pc[j] = (j < a.n_in && live) ? f64_to_f32(a.params_soa[(size_t)slots_s[j] * a.stride + s]) - in_mean[j]
-                                         : 0.f;
+            for (int j = 0; j < kMaxIn; ++j)
+                raw[j] = (j < a.n_in && live) ? __ldg(a.params_soa + (size_t)slots_s[j] * a.stride + s) : 0.0;
+#pragma unroll
+            for (int j = 0; j < kMaxIn; ++j) pc[j] = j < a.n_in && live ? f64_to_f32(raw[j]) - in_mean[j] : 0.f;
+        }
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             uint32_t w[4];
@@ -873,25 +879,48 @@ __global__ void __launch_bounds__(kGThreads) gemm_kernel(GemmTcArgs g) {
                 for (int j = 0; j < 32; ++j) v[j] = 0.f;
             }
             if (row >= g.M) continue;
+            // eight columns at a time: N and the tile width are multiples of 16, so a group
+            // of eight is wholly inside or wholly outside the output; row-major outputs are
+            // written 16 bytes per thread, the transposed copy 64 bytes per warp
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int col = n0 + c0 + j;
-                if (c0 + j >= bn || col >= g.N) continue;
-                if (EPI == kEpiF32) {
-                    g.C32[((size_t)blockIdx.z * g.M + row) * g.ldc + col] = v[j];
-                } else if (EPI == kEpiBiasF32) {
-                    g.C32[(size_t)row * g.ldc + col] = v[j] + g.bias[col];
-                } else if (EPI == kEpiBiasGelu) {
-                    const float z = v[j] + g.bias[col];
-                    const __nv_bfloat16 h = __float2bfloat16(act::gelu(z));
-                    g.Z[(size_t)row * g.ld + col] = __float2bfloat16(z);
-                    g.H[(size_t)row * g.ld + col] = h;
-                    g.Ht[(size_t)col * g.ldt + row] = h;
+            for (int q = 0; q < 4; ++q) {
+                const int col = n0 + c0 + 8 * q;
+                if (c0 + 8 * q >= bn || col >= g.N) continue;
+                const float* w = v + 8 * q;
+                if (EPI == kEpiF32 || EPI == kEpiBiasF32) {
+                    float o[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) o[j] = EPI == kEpiF32 ? w[j] : w[j] + g.bias[col + j];
+                    float* dst = EPI == kEpiF32 ? g.C32 + ((size_t)blockIdx.z * g.M + row) * g.ldc + col
+                                                : g.C32 + (size_t)row * g.ldc + col;
+                    reinterpret_cast<float4*>(dst)[0] = make_float4(o[0], o[1], o[2], o[3]);
+                    reinterpret_cast<float4*>(dst)[1] = make_float4(o[4], o[5], o[6], o[7]);
                 } else {
-                    const float z = __bfloat162float(g.Zin[(size_t)row * g.ld + col]);
-                    const __nv_bfloat16 d = __float2bfloat16(v[j] * act::gelu_grad(z));
-                    g.H[(size_t)row * g.ld + col] = d;
-                    g.Ht[(size_t)col * g.ldt + row] = d;
+                    uint32_t hz[4], hh[4];
+                    __nv_bfloat16 hb[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j += 2) {
+                        float a0, a1;
+                        if (EPI == kEpiBiasGelu) {
+                            const float z0 = w[j] + g.bias[col + j], z1 = w[j + 1] + g.bias[col + j + 1];
+                            hz[j / 2] = pack2(z0, z1);
+                            a0 = act::gelu(z0);
+                            a1 = act::gelu(z1);
+                        } else {
+                            const __nv_bfloat162 zin =
+                                *reinterpret_cast<const __nv_bfloat162*>(g.Zin + (size_t)row * g.ld + col + j);
+                            a0 = w[j] * act::gelu_grad(__low2float(zin));
+                            a1 = w[j + 1] * act::gelu_grad(__high2float(zin));
+                        }
+                        hh[j / 2] = pack2(a0, a1);
+                        hb[j] = __float2bfloat16(a0);
+                        hb[j + 1] = __float2bfloat16(a1);
+                    }
+                    if (EPI == kEpiBiasGelu)
+                        *reinterpret_cast<uint4*>(g.Z + (size_t)row * g.ld + col) = make_uint4(hz[0], hz[1], hz[2], hz[3]);
+                    *reinterpret_cast<uint4*>(g.H + (size_t)row * g.ld + col) = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) g.Ht[(size_t)(col + j) * g.ldt + row] = hb[j];
                 }
             }
         }
@@ -998,16 +1027,18 @@ bool gemm_supported(const GemmTcArgs& g) {
 
 cudaError_t gemm(GemmTcArgs g, int splits, cudaStream_t st) {
     if (!gemm_supported(g) || splits < 1) return cudaErrorInvalidValue;
-    g.bn = g.N <= 256 ? g.N : 256;  // a multiple of 16
-    const uint32_t smem = gemm_smem_bytes(g.bn);
     static std::mutex mu;
     static bool configured[64] = {};
+    static int sms_of[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    int sms = 0;
     {
         std::lock_guard<std::mutex> lk(mu);
         if (dev < 0 || dev >= 64 || !configured[dev]) {
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
             const int lim = (int)gemm_smem_bytes(256);
             e = cudaFuncSetAttribute(gemm_kernel<kEpiF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
             if (e == cudaSuccess)
@@ -1017,9 +1048,22 @@ cudaError_t gemm(GemmTcArgs g, int splits, cudaStream_t st) {
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(gemm_kernel<kEpiGeluBwd>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
             if (e != cudaSuccess) return e;
-            if (dev >= 0 && dev < 64) configured[dev] = true;
+            if (dev >= 0 && dev < 64) {
+                configured[dev] = true;
+                sms_of[dev] = sms;
+            }
+        } else {
+            sms = sms_of[dev];
         }
     }
+    // tile width: the widest (<= 256, a multiple of 16) that still gives every
+    // SM a tile; these GEMMs are small, so CTAs in flight matter more than
+    // the reuse of a wide tile
+    const long long mt = (g.M + 127) / 128;
+    int bn = g.N <= 256 ? g.N : 256;
+    while (bn > 32 && mt * ((g.N + bn - 1) / bn) * splits < sms) bn = ((bn / 2 + 15) / 16) * 16;
+    g.bn = bn;
+    const uint32_t smem = gemm_smem_bytes(g.bn);
     const dim3 grid((unsigned)((g.M + 127) / 128), (unsigned)((g.N + g.bn - 1) / g.bn), (unsigned)splits);
     switch (g.epi) {
         case kEpiF32: gemm_kernel<kEpiF32><<<grid, kGThreads, smem, st>>>(g); break;

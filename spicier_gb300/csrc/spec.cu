@@ -225,6 +225,44 @@ __device__ __forceinline__ double spx_d(float x) {
     const u64 inf = (0x7ffULL << 52) | ((u64)m << 29);
     return __longlong_as_double((long long)(sign | (e == 0 ? sub : (e == 255 ? inf : nrm))));
 }
+// Double-float (an FP32 pair h + l, |l| <= ulp(h) / 2, about 48 bits) for the
+// KCL residual and device currents of the mixed kernel on topologies whose
+// elements allow it: GB300 issues FP32 at 64 times its FP64 rate.  Every
+// operation is written with the _rn intrinsics and fmaf so that the compiler
+// contracts nothing (the error terms must be the exact rounding errors).
+struct spx_df { float h, l; };
+__device__ __forceinline__ spx_df spx_two(float s, float e) {  // |s| >= |e|, or s == 0
+    const float h = __fadd_rn(s, e);
+    return spx_df{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ spx_df spx_add(spx_df a, spx_df b) {
+    const float s = __fadd_rn(a.h, b.h), bb = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    return spx_two(s, e);
+}
+__device__ __forceinline__ spx_df spx_addf(spx_df a, float b) {
+    const float s = __fadd_rn(a.h, b), bb = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    e = __fadd_rn(e, a.l);
+    return spx_two(s, e);
+}
+__device__ __forceinline__ spx_df spx_neg2(spx_df a) { return spx_df{-a.h, -a.l}; }
+__device__ __forceinline__ spx_df spx_sub(spx_df a, spx_df b) { return spx_add(a, spx_neg2(b)); }
+__device__ __forceinline__ spx_df spx_mulf(spx_df a, float b) {
+    const float p = __fmul_rn(a.h, b);
+    float e = fmaf(a.h, b, -p);
+    e = fmaf(a.l, b, e);
+    return spx_two(p, e);
+}
+__device__ __forceinline__ spx_df spx_mul(spx_df a, spx_df b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return spx_two(p, e);
+}
+__device__ __forceinline__ bool spx_finf(float v) { return (__float_as_uint(v) & 0x7f800000u) != 0x7f800000u; }
 // v < 0 from the sign bit (integer pipe); -0 is not negative
 __device__ __forceinline__ bool spx_neg(double v) {
     const long long b = __double_as_longlong(v);
@@ -426,12 +464,122 @@ void emit_linear_jacobian(std::ostringstream& o, const sp_topology* t, const Pat
 // Per-thread shared memory of the per-sample constants (0: they stay in
 // registers).  Shared memory frees ~3 registers per constant, so more warps
 // stay resident to hide the latency of the next sample's loads.
+// The mixed kernel keeps its state, KCL residual and device currents in
+// double-float when every element is linear or a Level-1 MOSFET (the diode
+// and BJT limiters and exponentials stay in FP64).
+bool df_supported(const sp_topology* t) {
+    for (const sp_element& el : t->h_elements)
+        switch (el.kind) {
+            case SP_EL_R: case SP_EL_C: case SP_EL_L: case SP_EL_V: case SP_EL_I: case SP_EL_NMOS: case SP_EL_PMOS:
+                break;
+            default:
+                return false;
+        }
+    return true;
+}
+
+// Derived constants that the mixed kernel also keeps in FP32 (cf<k>): the
+// MOSFET constants (for the FP32 Jacobian, and the currents in double-float
+// mode) and, in double-float mode, the source values.
+std::vector<int> fp32_constants(const sp_topology* t, bool fp32_jac) {
+    std::vector<int> fcs;
+    if (!fp32_jac) return fcs;
+    const bool dfm = df_supported(t);
+    for (int e = 0, o = 0; e < t->num_elements; ++e) {
+        const int kind = t->h_elements[e].kind;
+        if (kind == SP_EL_NMOS || kind == SP_EL_PMOS)
+            for (int k = 0; k < 3; ++k) fcs.push_back(o + k);
+        else if (dfm && (kind == SP_EL_V || kind == SP_EL_I))
+            fcs.push_back(o);
+        o += derived_count(kind);
+    }
+    return fcs;
+}
+
 size_t spec_smem_bytes(const sp_topology* t, bool fp32_jac) {
-    int nfc = 0;
-    if (fp32_jac)
-        for (const sp_element& el : t->h_elements) nfc += (el.kind == SP_EL_NMOS || el.kind == SP_EL_PMOS) ? 3 : 0;
-    const size_t bytes = ((size_t)t->num_derived * 8 + (size_t)nfc * 4) * 128;
+    const size_t nfc = fp32_constants(t, fp32_jac).size();
+    const size_t bytes = ((size_t)t->num_derived * 8 + nfc * 4) * 128;
     return bytes <= 48 * 1024 ? bytes : 0;
+}
+
+// Element currents into the double-float residual F (state X, double-float)
+// and conductances into the FP32 Jacobian J (from X[].h, as in
+// emit_elements' mixed mode): the same formulas, with the constants in FP32
+// (a relative change of at most 2^-24 in a device parameter or source value,
+// far inside the SPICE tolerances the mixed precision is held to).
+void emit_elements_df(std::ostringstream& o, const sp_topology* t, const Pattern& P, const std::vector<int>& doff) {
+    const int nn = t->num_nodes;
+    auto cf = [&](int e, int k) { return "cf" + std::to_string(doff[e] + k); };
+    auto XV = [&](int node) { return node >= 0 ? "X[" + std::to_string(node) + "]" : std::string("spx_df{0.f, 0.f}"); };
+    auto XF = [&](int node) { return node >= 0 ? "X[" + std::to_string(node) + "].h" : std::string("0.f"); };
+    auto J = [&](int r, int c, const std::string& expr, bool neg) {
+        if (r < 0 || c < 0) return;
+        o << "    J[" << P.at(r, c) << "] " << (neg ? "-=" : "+=") << " " << expr << ";\n";
+    };
+    auto F = [&](int r, const std::string& expr, bool neg) {
+        if (r < 0) return;
+        o << "    F[" << r << "] = spx_add(F[" << r << "], " << (neg ? "spx_neg2(" + expr + ")" : expr) << ");\n";
+    };
+    for (int e = 0; e < t->num_elements; ++e) {
+        const sp_element& el = t->h_elements[e];
+        const int a = el.node[0], b = el.node[1], c = el.node[2];
+        o << "  { // element " << e << "\n";
+        switch (el.kind) {
+            case SP_EL_R:
+                o << "    const spx_df i = spx_mulf(spx_sub(" << XV(a) << ", " << XV(b) << "), g" << e << ");\n";
+                F(a, "i", false), F(b, "i", true);
+                break;
+            case SP_EL_V:
+            case SP_EL_L: {
+                const int br = nn + el.branch;
+                F(a, "X[" + std::to_string(br) + "]", false);
+                F(b, "X[" + std::to_string(br) + "]", true);
+                o << "    F[" << br << "] = spx_add(F[" << br << "], ";
+                if (el.kind == SP_EL_V)
+                    o << "spx_addf(spx_sub(" << XV(a) << ", " << XV(b) << "), -" << cf(e, 0) << "));\n";
+                else
+                    o << "spx_sub(" << XV(a) << ", " << XV(b) << "));\n";
+                break;
+            }
+            case SP_EL_I:
+                if (a >= 0) o << "    F[" << a << "] = spx_addf(F[" << a << "], " << cf(e, 0) << ");\n";
+                if (b >= 0) o << "    F[" << b << "] = spx_addf(F[" << b << "], -" << cf(e, 0) << ");\n";
+                break;
+            case SP_EL_C:
+                break;
+            case SP_EL_NMOS:
+            case SP_EL_PMOS: {
+                const int d = a, g = b, s = c;
+                const bool pm = el.kind == SP_EL_PMOS;
+                auto dv = [&](int p, int q) { return pm ? "spx_sub(" + XV(q) + ", " + XV(p) + ")" : "spx_sub(" + XV(p) + ", " + XV(q) + ")"; };
+                auto df32 = [&](int p, int q) { return pm ? XF(q) + " - " + XF(p) : XF(p) + " - " + XF(q); };
+                o << "    float vgsf = " << df32(g, s) << ", vdsf = " << df32(d, s) << ";\n"
+                  << "    float vovf = vgsf - " << cf(e, 0) << ", qf = 1.f + " << cf(e, 2) << " * vdsf;\n"
+                  << "    bool on = vovf >= 0.f, lin = on && vdsf < vovf;\n"
+                  << "    const spx_df vds = " << dv(d, s) << ";\n"
+                  << "    const spx_df vov = spx_addf(" << dv(g, s) << ", -" << cf(e, 0) << ");\n"
+                  << "    const spx_df u = lin ? vds : vov;\n"
+                  << "    const spx_df t1 = spx_sub(vov, spx_df{0.5f * u.h, 0.5f * u.l});\n"
+                  << "    const spx_df t2 = spx_addf(spx_mulf(vds, " << cf(e, 2) << "), 1.f);\n"
+                  << "    spx_df ids = on ? spx_mul(spx_mul(spx_mulf(u, " << cf(e, 1) << "), t1), t2) : spx_df{0.f, 0.f};\n";
+                if (pm) o << "    ids = spx_neg2(ids);\n";
+                F(d, "ids", false), F(s, "ids", true);
+                o << "    float gdf = 1e-12f, gmf = 0.f;\n"
+                  << "    if (lin) { gdf = " << cf(e, 1) << " * (vovf - vdsf) * qf + " << cf(e, 1)
+                  << " * (vovf * vdsf - 0.5f * vdsf * vdsf) * " << cf(e, 2) << "; gmf = " << cf(e, 1)
+                  << " * vdsf * qf; }\n"
+                  << "    else if (on) { gdf = 0.5f * " << cf(e, 1) << " * vovf * vovf * " << cf(e, 2)
+                  << "; gmf = " << cf(e, 1) << " * vovf * qf; }\n"
+                  << "    gdf = fmaxf(gdf, 1e-12f);\n";
+                J(d, d, "gdf", false), J(s, s, "gdf", false), J(d, s, "gdf", true), J(s, d, "gdf", true);
+                J(d, g, "gmf", false), J(d, s, "gmf", true), J(s, g, "gmf", true), J(s, s, "gmf", false);
+                break;
+            }
+            default:
+                break;
+        }
+        o << "  }\n";
+    }
 }
 
 std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
@@ -442,13 +590,8 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
         o += derived_count(t->h_elements[e].kind);
     }
     const bool sm = spec_smem_bytes(t, fp32_jac) > 0;
-    std::vector<int> fcs;
-    if (fp32_jac)
-        for (int e = 0; e < t->num_elements; ++e) {
-            const int kind = t->h_elements[e].kind;
-            if (kind != SP_EL_NMOS && kind != SP_EL_PMOS) continue;
-            for (int k = 0; k < 3; ++k) fcs.push_back(doff[e] + k);
-        }
+    const std::vector<int> fcs = fp32_constants(t, fp32_jac);
+    const bool dfm = fp32_jac && df_supported(t);  // double-float state and residual
     std::ostringstream o;
     o << kPreamble << "typedef " << (fp32_jac ? "float" : "double") << " JT;\n";
     if (sm) {  // constant k of this thread at [k][threadIdx.x]; volatile keeps them out of registers
@@ -474,10 +617,13 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     }
     for (int e = 0; e < t->num_elements; ++e)
         if (t->h_elements[e].kind == SP_EL_R) o << "  JT g" << e << ";\n";
-    o << "  double x[" << n << "];\n";
+    if (dfm)
+        o << "  spx_df X[" << n << "];\n";
+    else
+        o << "  double x[" << n << "];\n";
+    if (fp32_jac && !dfm) o << "  float xf[" << n << "];\n";
     if (fp32_jac)
-        o << "  float xf[" << n << "];\n"
-          << "  const float reltolf = spx_f(a.reltol), vabstolf = spx_f(a.vabstol), iabstolf = spx_f(a.iabstol);\n";
+        o << "  const float reltolf = spx_f(a.reltol), vabstolf = spx_f(a.vabstol), iabstolf = spx_f(a.iabstol);\n";
     o << "  int it, code;\n";
     // per-sample set-up: constants, linear Jacobian, start point
     std::ostringstream ld;
@@ -487,19 +633,30 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     for (int e = 0; e < t->num_elements; ++e)
         if (t->h_elements[e].kind == SP_EL_R)
             ld << "  g" << e << " = " << (fp32_jac ? "spx_f(c" : "(JT)(c") << doff[e] << ");\n";
-    ld << "  if (warm) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n
-       << " + i];\n"
-       << "  } else if (a.nodeset) {\n    #pragma unroll\n    for (int i = 0; i < " << n
-       << "; ++i) x[i] = a.nodeset[i];\n"
-       << "  } else {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = 0.0;\n  }\n";
-    if (fp32_jac) ld << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) xf[i] = spx_f(x[i]);\n";
+    if (dfm)  // the start point rounded to FP32 (a starting guess: its low part is not needed)
+        ld << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i)\n"
+           << "    X[i] = spx_df{warm ? spx_f(a.x0[s * " << n << " + i]) : (a.nodeset ? spx_f(a.nodeset[i]) : 0.f), 0.f};\n";
+    else
+        ld << "  if (warm) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n
+           << " + i];\n"
+           << "  } else if (a.nodeset) {\n    #pragma unroll\n    for (int i = 0; i < " << n
+           << "; ++i) x[i] = a.nodeset[i];\n"
+           << "  } else {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = 0.0;\n  }\n";
+    if (fp32_jac && !dfm) ld << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) xf[i] = spx_f(x[i]);\n";
     ld << "  it = 0; code = 1;\n  }\n";
     o << ld.str();
-    o << "  while (true) {\n    ++it;\n"
-      << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n"
-      << "    JT J[" << P.nnz << "];\n";
+    o << "  while (true) {\n    ++it;\n";
+    if (dfm)
+        o << "    spx_df F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n
+          << "; ++i) F[i] = spx_df{0.f, 0.f};\n";
+    else
+        o << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n";
+    o << "    JT J[" << P.nnz << "];\n";
     emit_linear_jacobian(o, t, P);
-    emit_elements(o, t, P, doff, true, fp32_jac);
+    if (dfm)
+        emit_elements_df(o, t, P, doff);
+    else
+        emit_elements(o, t, P, doff, true, fp32_jac);
     // factorisation over the static pattern
     o << "    bool sing = false;\n";
     for (int k = 0; k < n; ++k) {
@@ -516,7 +673,10 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     // forward and back substitution on -F (rows permuted)
     o << "    JT y[" << n << "];\n";
     for (int i = 0; i < n; ++i) {
-        o << "    y[" << i << "] = " << (fp32_jac ? "spx_fneg(F[" : "(JT)(-F[") << P.perm[i] << "])";
+        if (dfm)
+            o << "    y[" << i << "] = -__fadd_rn(F[" << P.perm[i] << "].h, F[" << P.perm[i] << "].l)";
+        else
+            o << "    y[" << i << "] = " << (fp32_jac ? "spx_fneg(F[" : "(JT)(-F[") << P.perm[i] << "])";
         for (int k = 0; k < i; ++k)
             if (P.has(i, k)) o << " - J[" << P.slot[i * n + k] << "] * y[" << k << "]";
         o << ";\n";
@@ -529,7 +689,11 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     }
     o << "    bool conv = true;\n";
     for (int i = 0; i < n; ++i) {
-        if (fp32_jac)  // FP64 update; the test (newton.rs:134-159) on the FP32 step and shadows
+        if (dfm)  // double-float update; the same test on the FP32 step and the high parts
+            o << "    { const float xof = X[" << i << "].h; X[" << i << "] = spx_addf(X[" << i << "], y[" << i << "]);\n"
+              << "      conv = conv && !(fabsf(y[" << i << "]) > reltolf * fmaxf(fabsf(X[" << i << "].h), fabsf(xof)) + "
+              << (i < nn ? "vabstolf" : "iabstolf") << "); }\n";
+        else if (fp32_jac)  // FP64 update; the test (newton.rs:134-159) on the FP32 step and shadows
             o << "    { double xn = x[" << i << "] + spx_d(y[" << i << "]); float xnf = spx_f(xn);\n"
               << "      conv = conv && !(fabsf(y[" << i << "]) > reltolf * fmaxf(fabsf(xnf), fabsf(xf[" << i
               << "])) + " << (i < nn ? "vabstolf" : "iabstolf") << ");\n      x[" << i << "] = xn; xf[" << i
@@ -542,6 +706,9 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     o << "    code = sing ? 2 : (conv ? 0 : 1);\n"
       << "    if (sing || conv || it >= a.max_it) {\n";
     // status, outputs, miss list, residual of sample s
+    if (dfm)
+        o << "    double x[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n
+          << "; ++i) x[i] = spx_d(X[i].h) + spx_d(X[i].l);\n";
     o << "    bool fin = true;\n    #pragma unroll\n    for (int i = 0; i < " << n
       << "; ++i) fin = fin && spx_fin(x[i]);\n"
       << "    unsigned char st8 = !fin ? 3 : (unsigned char)code;\n"
