@@ -631,7 +631,12 @@ enum sp_mlp_kernel {
     SP_MLP_KERNEL_AUTO = 0,
     SP_MLP_KERNEL_TCGEN05 = 1,
     SP_MLP_KERNEL_MMA_SYNC = 2,
-    SP_MLP_KERNEL_LAYERED = 3
+    SP_MLP_KERNEL_LAYERED = 3,
+    /* the linear term alone (sp_mlp_set_linear and the I/O mapping, no
+     * network): x0[k] = out_mean[k] + sum_j lin[k][j] (p_j - in_mean[j]) in
+     * FP32, evaluated by the learned sweep's draw kernel from the parameters
+     * it has just drawn, so no inference kernel runs */
+    SP_MLP_KERNEL_LINEAR = 4
 };
 int sp_mlp_set_inference_kernel(sp_mlp* mlp, int kind);
 /* Kernel of the training GEMMs (forward, data gradient, weight gradient):

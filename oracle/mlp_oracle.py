@@ -12,6 +12,12 @@ from __future__ import annotations
 import numpy as np
 
 
+def f16(a: np.ndarray) -> np.ndarray:
+    """Round to FP16 (nearest even) and back to FP32: the tcgen05 inference
+    kernels' operands and stored activations."""
+    return np.asarray(a, dtype=np.float32).astype(np.float16).astype(np.float32)
+
+
 def bf16(a: np.ndarray) -> np.ndarray:
     a = np.ascontiguousarray(a, dtype=np.float32)
     b = a.view(np.uint32).astype(np.uint64)
@@ -38,11 +44,12 @@ def pad(a, cols):
     return out
 
 
-def forward_backward(layers, X, T, n_out, exact=False):
+def forward_backward(layers, X, T, n_out, exact=False, rounding="bf16"):
     """layers: [(Wt[out_pad][in_pad], b[out_pad])] FP32 masters.
-    Returns (Y[rows][out_pad], loss, [(dWt, db)])."""
+    rounding: "bf16" (the trainer and the mma.sync kernels) or "f16" (the
+    tcgen05 inference kernels).  Returns (Y[rows][out_pad], loss, [(dWt, db)])."""
     dt = np.float64 if exact else np.float32
-    rnd = (lambda a: np.asarray(a, dtype=np.float64)) if exact else bf16
+    rnd = (lambda a: np.asarray(a, dtype=np.float64)) if exact else (f16 if rounding == "f16" else bf16)
     rows = X.shape[0]
     kin = layers[0][0].shape[1]
     A = rnd(pad(X.astype(dt), kin))

@@ -65,6 +65,7 @@ SP_FALLBACK_SOURCE = 2
 
 # sp_sample_status
 SP_MLP_KERNEL_AUTO, SP_MLP_KERNEL_TCGEN05, SP_MLP_KERNEL_MMA_SYNC, SP_MLP_KERNEL_LAYERED = 0, 1, 2, 3
+SP_MLP_KERNEL_LINEAR = 4
 
 SP_ST_CONVERGED = 0
 SP_ST_FAILED = 1

@@ -460,7 +460,8 @@ class Mlp:
         check(self.ctx._ptr, load().sp_mlp_set_linear(self._ptr, _vp(arr)))
 
     def set_inference_kernel(self, kind: int):
-        """abi.SP_MLP_KERNEL_{AUTO,TCGEN05,MMA_SYNC,LAYERED} for the warm start."""
+        """abi.SP_MLP_KERNEL_{AUTO,TCGEN05,MMA_SYNC,LAYERED,LINEAR} for the warm start
+        (LINEAR: the linear term alone, evaluated by the learned sweep's draw kernel)."""
         check(self.ctx._ptr, load().sp_mlp_set_inference_kernel(self._ptr, kind))
 
     def set_training_kernel(self, kind: int):

@@ -581,11 +581,16 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 32, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
                  s.counters + 1, t->d_drawn, t->num_drawn, s.counters + 4};
+    // a linear warm start is evaluated by the draw kernel itself
+    const bool linear_warm = warm && mlp_linear_only(warm, &D);
+    if (linear_warm) D.x0_out = s.x0;
     {
         ProfScope prof(ctx, "draw_params", st);
         SP_CUDA(ctx, launch_draw(D, st), "draw launch");
     }
-    if (warm) {
+    if (linear_warm) {
+        d_x0 = s.x0;
+    } else if (warm) {
         ProfScope prof(ctx, "mlp_warm_start", st);
         SP_CUDA(ctx, mlp_warm_start(warm, s.params, (size_t)count, (int)count, s.x0, st), "network warm start");
         d_x0 = s.x0;

@@ -32,6 +32,13 @@ struct DrawLaunch {
     const int* drawn;     // [num_drawn] slots whose kind is not SP_DRAW_FIXED (device), ascending
     int num_drawn;
     unsigned int* next;   // zeroed group counter of the persistent draw kernel, or nullptr
+    // optional linear warm start (SP_MLP_KERNEL_LINEAR): x0_out[s][lin_nout] =
+    // lin_io[2 nin + k] + sum_j lin[k][j] (p[lin_slots[j]] - lin_io[j])
+    const float* lin = nullptr;
+    const float* lin_io = nullptr;  // in_mean[nin], in_scale[nin], out_mean[nout], out_scale[nout]
+    const int* lin_slots = nullptr;
+    int lin_nin = 0, lin_nout = 0;
+    double* x0_out = nullptr;
 };
 
 cudaError_t launch_bsim3_eval(int pmos, const double* card, const double* bias, uint64_t count, double* out,
@@ -89,6 +96,9 @@ constexpr int kMaxDenseN = 28;
 cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, int rows, double* x0,
                            cudaStream_t st);
 int mlp_outputs(const sp_mlp* m);
+// True when the warm start is the linear term alone (SP_MLP_KERNEL_LINEAR);
+// then fills the draw launch's linear-warm-start fields (x0_out left to the caller).
+bool mlp_linear_only(const sp_mlp* m, DrawLaunch* d);
 int mlp_max_slot(const sp_mlp* m);
 uint64_t mlp_max_rows();
 bool mlp_io_ready(const sp_mlp* m);

@@ -47,8 +47,22 @@ __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_kernel(Draw
     pdl_wait();
     pdl_trigger();
     __shared__ unsigned int group_s;
+    // linear warm start (x0_out set): weights lin[nout][nin], in_mean[nin],
+    // out_mean[nout], then the group's centred inputs pin[nin][32]
+    extern __shared__ float lsm[];
+    const int nin = L.lin_nin, nout = L.lin_nout;
+    float* lin_s = lsm;
+    float* inm_s = lsm + nout * nin;
+    float* outm_s = inm_s + nin;
+    float* pin_s = outm_s + nout;
     const DevCircuit& c = L.c;
     const int lane = threadIdx.x, warp = threadIdx.y;
+    const int tid = warp * kDrawSamples + lane;
+    if (L.x0_out) {
+        for (int i = tid; i < nout * nin; i += kDrawSamples * kDrawLanes) lin_s[i] = L.lin[i];
+        for (int i = tid; i < nin; i += kDrawSamples * kDrawLanes) inm_s[i] = L.lin_io[i];
+        for (int i = tid; i < nout; i += kDrawSamples * kDrawLanes) outm_s[i] = L.lin_io[2 * nin + i];
+    }
     const uint64_t groups = (L.count + kDrawSamples - 1) / kDrawSamples;
     unsigned hard = 0;
     for (uint64_t it = 0;; ++it) {
@@ -75,17 +89,30 @@ __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_kernel(Draw
             }
         }
         __syncthreads();  // this group's parameter slots are written (group_s is read by all)
-        if (!live) continue;
         auto P = [&](int slot) {
             const sp_param& p = c.par[slot];
             return p.kind == SP_DRAW_FIXED ? p.a : L.params_soa[(size_t)slot * L.count + s];
         };
+        if (L.x0_out) {  // the group's centred warm-start inputs, input j by warp j % 8
+            for (int j = warp; j < nin; j += kDrawLanes)
+                pin_s[j * kDrawSamples + lane] = live ? __double2float_rn(P(L.lin_slots[j])) - inm_s[j] : 0.f;
+            __syncthreads();
+        }
+        if (!live) continue;
         for (int e = warp; e < c.num_elements; e += kDrawLanes) {
             const sp_element el = c.el[e];
             double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
             const size_t st = L.count;
             derive_element(el, P, [&](int k, double v) { out[k * st] = v; });
         }
+        // linear warm start: lane y evaluates unknowns y, y + 8, ... in FP32 (as
+        // the network kernels' linear term), inputs and weights from shared memory
+        if (L.x0_out)
+            for (int k = warp; k < nout; k += kDrawLanes) {
+                float x = outm_s[k];
+                for (int j = 0; j < nin; ++j) x = fmaf(lin_s[k * nin + j], pin_s[j * kDrawSamples + lane], x);
+                L.x0_out[s * nout + k] = (double)x;
+            }
     }
     if (hard && L.hard) atomicAdd(L.hard, hard);
 }
@@ -99,7 +126,10 @@ cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st) {
     const uint64_t groups = (L.count + kDrawSamples - 1) / kDrawSamples;
     // resident blocks (four per SM at 64 registers); without a counter one block per group
     const uint64_t grid = L.next ? std::min<uint64_t>(groups, (uint64_t)sms * 4) : groups;
-    return launch_chained(draw_kernel, dim3((unsigned)grid), dim3(kDrawSamples, kDrawLanes), 0, st, L);
+    const size_t smem = L.x0_out ? sizeof(float) * ((size_t)L.lin_nout * L.lin_nin + L.lin_nin + L.lin_nout +
+                                                    (size_t)L.lin_nin * kDrawSamples)
+                                 : 0;
+    return launch_chained(draw_kernel, dim3((unsigned)grid), dim3(kDrawSamples, kDrawLanes), smem, st, L);
 }
 
 // Batched Bsim3Mosfet::evaluate (one thread per device): the per-sample

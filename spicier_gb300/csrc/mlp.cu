@@ -1020,7 +1020,9 @@ extern "C" int sp_mlp_set_linear(sp_mlp* m, const double* lin) {
 }
 
 extern "C" int sp_mlp_set_inference_kernel(sp_mlp* m, int kind) {
-    if (!m || kind < SP_MLP_KERNEL_AUTO || kind > SP_MLP_KERNEL_LAYERED) return SP_ERR_INVALID_ARGUMENT;
+    if (!m || kind < SP_MLP_KERNEL_AUTO || kind > SP_MLP_KERNEL_LINEAR) return SP_ERR_INVALID_ARGUMENT;
+    if (kind == SP_MLP_KERNEL_LINEAR && !m->has_lin)
+        return mlp_fail(m->ctx, SP_ERR_INVALID_ARGUMENT, "the linear warm start needs sp_mlp_set_linear first");
     if (kind == SP_MLP_KERNEL_TCGEN05 && !sp::tc_eligible(m))
         return mlp_fail(m->ctx, SP_ERR_INVALID_DIMENSION,
                         "tcgen05 inference needs n_in <= 32, n_out <= 32, hidden 64, 128 or 256, 1..4 hidden layers");
@@ -1089,7 +1091,7 @@ cudaError_t tc_warm_start(sp_mlp* m, const double* params_soa, size_t stride, in
     // start; weights packed now are not (the copies below precede the kernel)
     a.early_prologue = m->tc_dirty ? 0 : 1;
     if (m->tc_dirty) {
-        cudaError_t e = mlptc::pack(m->wt_bf, m->woff.data(), a, m->tc_img, st);
+        cudaError_t e = mlptc::pack(m->params, m->woff.data(), a, m->tc_img, st);
         for (int l = 0; l < m->L && e == cudaSuccess; ++l)
             e = cudaMemcpyAsync(m->tc_bias + a.layer[l].bias_off, m->params + m->boff[l], 4 * (size_t)a.layer[l].N,
                                 cudaMemcpyDeviceToDevice, st);
@@ -1110,9 +1112,29 @@ cudaError_t tc_warm_start(sp_mlp* m, const double* params_soa, size_t stride, in
     return mlptc::launch(a, m->num_sms, st);
 }
 
+// The linear warm start alone (SP_MLP_KERNEL_LINEAR) for a standalone call;
+// the learned sweep evaluates the same formula in its draw kernel.
+__global__ void linear_warm_kernel(const double* __restrict__ params_soa, size_t stride, int rows,
+                                   const int* __restrict__ slots, const float* __restrict__ io,
+                                   const float* __restrict__ lin, int n_in, int n_out, double* __restrict__ x0) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= rows) return;
+    for (int k = 0; k < n_out; ++k) {
+        float x = io[2 * n_in + k];
+        for (int j = 0; j < n_in; ++j)
+            x = fmaf(lin[k * n_in + j], __double2float_rn(params_soa[(size_t)slots[j] * stride + s]) - io[j], x);
+        x0[(size_t)s * n_out + k] = (double)x;
+    }
+}
+
 cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, int rows, double* x0,
                            cudaStream_t st) {
     const int kind = m->kernel_kind;
+    if (kind == SP_MLP_KERNEL_LINEAR) {
+        linear_warm_kernel<<<(rows + 127) / 128, 128, 0, st>>>(params_soa, stride, rows, m->io_slots, m->io,
+                                                               m->lin_f32, m->d.n_in, m->d.n_out, x0);
+        return cudaGetLastError();
+    }
     if (kind == SP_MLP_KERNEL_TCGEN05 || (kind == SP_MLP_KERNEL_AUTO && tc_eligible(m)))
         return tc_warm_start(m, params_soa, stride, rows, x0, st);
     if (kind != SP_MLP_KERNEL_LAYERED && m->H <= FH && m->L <= 9) {
@@ -1161,6 +1183,15 @@ cudaError_t mlp_warm_start(sp_mlp* m, const double* params_soa, size_t stride, i
     return cudaGetLastError();
 }
 int mlp_outputs(const sp_mlp* m) { return m->d.n_out; }
+bool mlp_linear_only(const sp_mlp* m, DrawLaunch* d) {
+    if (m->kernel_kind != SP_MLP_KERNEL_LINEAR || !m->has_lin) return false;
+    d->lin = m->lin_f32;
+    d->lin_io = m->io;
+    d->lin_slots = m->io_slots;
+    d->lin_nin = m->d.n_in;
+    d->lin_nout = m->d.n_out;
+    return true;
+}
 int mlp_max_slot(const sp_mlp* m) { return m->max_slot; }
 uint64_t mlp_max_rows() { return kMaxRows; }
 bool mlp_io_ready(const sp_mlp* m) { return m->io_set; }

@@ -1,7 +1,7 @@
 // Warm-start inference on the 5th-generation tensor cores (tcgen05, TMEM).
 //
 // One persistent CTA per SM keeps the whole network in shared memory: every
-// layer's BF16 weight matrix W[N][K] is packed once, on the device, into the
+// layer's weight matrix W[N][K] is packed once, on the device, as FP16 into the
 // tensor cores' K-major 128-byte-swizzled layout (8-row x 128-byte atoms,
 // 16-byte chunks XOR-ed with the row), so a CTA fills its shared memory with
 // one linear copy.  Up to four teams of 128 threads (four warps, warp q
@@ -11,16 +11,22 @@
 //
 //   stage inputs  centred parameters p - in_mean in FP32 (kept in registers
 //                 for the FP32 linear term; relative error ~2^-24 /
-//                 |p/in_mean - 1|), scaled to BF16 and written as row t of
+//                 |p/in_mean - 1|), scaled to FP16 and written as row t of
 //                 the A operand;
 //   per layer     one thread issues K/16 tcgen05.mma (M=128, N=layer width,
-//                 K=16, BF16 x BF16 -> FP32 in TMEM) and commits them to the
+//                 K=16, FP16 x FP16 -> FP32 in TMEM) and commits them to the
 //                 team's mbarrier; after the wait every thread reads its
 //                 TMEM lane 32 columns at a time (tcgen05.ld 32x32b.x32),
-//                 adds the bias, applies GELU and writes the BF16
-//                 activations back as the next layer's A;
+//                 adds the bias (FP32), applies GELU in packed FP16
+//                 arithmetic (two activations per instruction) and writes
+//                 the FP16 activations back as the next layer's A;
 //   output        x0[k] = out_mean[k] + out_scale[k] y[k]
 //                         + sum_j lin[k][j] (p_j - in_mean[j])    (FP32, then FP64)
+//
+// FP16 rather than the trainer's BF16: the inputs are normalised and the
+// activations of a warm-start network stay far inside FP16's range, FP16
+// keeps three more mantissa bits, and packed FP16 arithmetic halves the
+// epilogue's instructions, which (not the tensor cores) bound a layer.
 //
 // With four teams a 65,536-sample sweep is one tile per team on 128 SMs: the
 // teams' MMAs, TMEM reads and epilogues interleave on the SM, and no team
@@ -48,13 +54,14 @@
 //                  the epilogue of one layer while the tensor cores run the
 //                  other team's layer: jobs alternate team 0 / team 1 layer
 //                  by layer, so the MMA chain of one tile overlaps the
-//                  bias + GELU + BF16 repack of the other.
+//                  bias + GELU + FP16 repack of the other.
 // The weights never depend on the activations, so the producer runs ahead of
 // the MMA warp by the ring's depth across layers and tiles.
 //
 // Scope: n_in <= 32, n_out <= 32, hidden width 64, 128 or 256, 1..4 hidden
 // layers; the mma.sync kernel in mlp.cu serves every other shape.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 #include <mutex>
@@ -89,6 +96,10 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
 // K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+}
+// The same with FP16 A and B (the inference kernels).
+__host__ __device__ constexpr uint32_t idesc_f16(int n) {
+    return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_bf16_ss(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
@@ -196,6 +207,28 @@ __device__ __forceinline__ double f32_to_f64(float x) {
     return __longlong_as_double((long long)b);
 }
 
+__device__ __forceinline__ uint32_t pack2h(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// GELU (tanh form) of two FP16 values in packed FP16 arithmetic: z/2 (1 +
+// tanh(c z (1 + a z^2))), six instructions for two activations.  Large |z|
+// saturates through infinities to z or 0 (tanh of +-inf is +-1), as the FP32
+// form does.
+__device__ __forceinline__ uint32_t gelu_h2(float z0, float z1) {
+    const __half2 z = __floats2half2_rn(z0, z1);
+    const __half2 ca = __float2half2_rn(act::kC * act::kA), c = __float2half2_rn(act::kC), hf = __float2half2_rn(0.5f);
+    const __half2 u = __hmul2(z, z);
+    const __half2 w = __hfma2(ca, u, c);
+    const __half2 arg = __hmul2(z, w);
+    uint32_t t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const uint32_t*>(&arg)));
+    const __half2 hz = __hmul2(z, hf);
+    const __half2 g = __hfma2(hz, *reinterpret_cast<const __half2*>(&t), hz);
+    return *reinterpret_cast<const uint32_t*>(&g);
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&h);
@@ -208,7 +241,7 @@ __host__ __device__ __forceinline__ uint32_t sw128_offset(int rows, int r, int c
     return (uint32_t)((c >> 3) * rows * 128 + (r >> 3) * 1024 + (r & 7) * 128 + (((c & 7) ^ (r & 7)) << 4));
 }
 
-__global__ void pack_kernel(const __nv_bfloat16* __restrict__ wt, int N, int K, int Kp, unsigned char* __restrict__ dst) {
+__global__ void pack_kernel(const float* __restrict__ wt, int N, int K, int Kp, unsigned char* __restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;  // one 16-byte chunk
     const int chunks = Kp / 8;
     if (i >= N * chunks) return;
@@ -217,10 +250,9 @@ __global__ void pack_kernel(const __nv_bfloat16* __restrict__ wt, int N, int K, 
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
         const int k0 = c * 8 + 2 * h;
-        const __nv_bfloat16 z = __float2bfloat16(0.f);
-        const __nv_bfloat16 a = k0 < K ? wt[(size_t)r * K + k0] : z;
-        const __nv_bfloat16 b = k0 + 1 < K ? wt[(size_t)r * K + k0 + 1] : z;
-        w[h] = (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+        const float a = k0 < K ? wt[(size_t)r * K + k0] : 0.f;
+        const float b = k0 + 1 < K ? wt[(size_t)r * K + k0 + 1] : 0.f;
+        w[h] = pack2h(a, b);
     }
     *reinterpret_cast<uint4*>(dst + sw128_offset(N, r, c)) = make_uint4(w[0], w[1], w[2], w[3]);
 }
@@ -341,7 +373,7 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
                 const int j = c * 8 + 2 * h;
                 const float x0v = j < a.n_in ? pc[j] * in_rscale[j] : 0.f;
                 const float x1v = j + 1 < a.n_in ? pc[j + 1] * in_rscale[j + 1] : 0.f;
-                w[h] = pack2(x0v, x1v);
+                w[h] = pack2h(x0v, x1v);
             }
             *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
@@ -360,7 +392,7 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
                 if (!ok) break;
             }
             if (tt == 0) {
-                const uint32_t id = idesc_bf16(ly.N);
+                const uint32_t id = idesc_f16(ly.N);
                 const uint32_t wb = wimg_s + (uint32_t)ly.img_off;
                 for (int kb = 0; kb < ly.Kp / 64; ++kb)
 #pragma unroll
@@ -381,8 +413,7 @@ __global__ void __launch_bounds__(kMaxTeams * kTeam, 1) infer_kernel(Args a, int
                     uint32_t w[16];
 #pragma unroll
                     for (int i = 0; i < 16; ++i)
-                        w[i] = pack2(act::gelu(v[2 * i] + bias[c0 + 2 * i]),
-                                     act::gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
+                        w[i] = gelu_h2(v[2 * i] + bias[c0 + 2 * i], v[2 * i + 1] + bias[c0 + 2 * i + 1]);
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
                         *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8 + q)) =
@@ -436,8 +467,8 @@ constexpr int kSTeamThreads = kSTeamWarps * 32;       // 256
 constexpr int kSProducerWarp = kSTeams * kSTeamWarps;  // warp 16
 constexpr int kSIssuerWarp = kSProducerWarp + 1;       // warp 17
 constexpr int kSThreads = (kSIssuerWarp + 1) * 32;     // 576
-constexpr uint32_t kSUnit = 16384;                    // one ring slot: 128 rows x 64 K of BF16
-constexpr uint32_t kSAbytes = 128u * 256u * 2u;       // one activation tile: 128 samples x 256 BF16
+constexpr uint32_t kSUnit = 16384;                    // one ring slot: 128 rows x 64 K of FP16
+constexpr uint32_t kSAbytes = 128u * 256u * 2u;       // one activation tile: 128 samples x 256 FP16
 constexpr int kSMaxSlots = 6;
 
 struct SCarve {
@@ -615,7 +646,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots
                             }
                             tc_after();
                             const int rows_u = min(128, ly.N - nh * 128);
-                            const uint32_t id = idesc_bf16(rows_u);
+                            const uint32_t id = idesc_f16(rows_u);
                             const uint32_t d = tmem + (uint32_t)(T * 256 + nh * 128);
                             const uint32_t ab = abuf_s + (uint32_t)kb * (kTile * 128), bb = ring_s + slot * kSUnit;
 #pragma unroll
@@ -662,7 +693,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots
                                               ? (f64_to_f32(a.params_soa[(size_t)slots_s[j + 1] * a.stride + s]) -
                                                  in_mean[j + 1]) * in_rscale[j + 1]
                                               : 0.f;
-                        w[h] = pack2(x0v, x1v);
+                        w[h] = pack2h(x0v, x1v);
                     }
                     *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c)) = make_uint4(w[0], w[1], w[2], w[3]);
                 }
@@ -690,8 +721,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_kernel(Args a, int nslots
                         uint32_t w[16];
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
-                            w[i] = pack2(act::gelu(v[2 * i] + bias[c0 + 2 * i]),
-                                         act::gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
+                            w[i] = gelu_h2(v[2 * i] + bias[c0 + 2 * i], v[2 * i + 1] + bias[c0 + 2 * i + 1]);
 #pragma unroll
                         for (int q = 0; q < 4; ++q)
                             *reinterpret_cast<uint4*>(abuf + sw128_offset(kTile, row, c0 / 8 + q)) =
@@ -971,7 +1001,7 @@ size_t smem_bytes(const Args& a) {
     return t ? 1024 + (size_t)carve(a, t).total : 0;
 }
 
-cudaError_t pack(const __nv_bfloat16* wt, const size_t* woff, const Args& a, void* img, cudaStream_t st) {
+cudaError_t pack(const float* wt, const size_t* woff, const Args& a, void* img, cudaStream_t st) {
     for (int l = 0; l < a.L; ++l) {
         const Layer& ly = a.layer[l];
         const int n = ly.N * ly.Kp / 8;

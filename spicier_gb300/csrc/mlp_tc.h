@@ -45,8 +45,8 @@ bool supported(int n_in, int n_out, int hidden, int gemm_layers);
 // Fills the layer table of `a` (and n_in, n_out); returns the image size.
 int plan(int n_in, int n_out, int hidden, int gemm_layers, Args* a);
 size_t smem_bytes(const Args& a);
-// Packs the row-major BF16 weights (layer l at wt + woff[l]) into the image.
-cudaError_t pack(const __nv_bfloat16* wt, const size_t* woff, const Args& a, void* img, cudaStream_t st);
+// Packs the row-major FP32 weights (layer l at wt + woff[l]) into the image as FP16.
+cudaError_t pack(const float* wt, const size_t* woff, const Args& a, void* img, cudaStream_t st);
 cudaError_t launch(const Args& a, int num_sms, cudaStream_t st);
 
 // Training GEMM C[M][N] = A[M][K] B[N][K]^T (BF16, K-major operands, FP32

@@ -184,12 +184,13 @@ class WarmStart:
         return np.sqrt((err ** 2).mean(0)) / self.tolerance
 
     def use_network(self, on: bool = True):
-        """With on=False the warm start is the FP64-fitted linear term alone,
-        out_mean + lin (p - in_mean): the network's output is scaled by zero.
-        This isolates what the trained network adds over the linear fit."""
-        out_mean, out_scale = self._io
-        self.mlp.set_io(self.inputs, self._in[0], self._in[1], out_mean,
-                        out_scale if on else np.zeros_like(out_scale))
+        """With on=False the warm start is the fitted linear term alone,
+        out_mean + lin (p - in_mean) in FP32, evaluated by the sweep's draw
+        kernel (SP_MLP_KERNEL_LINEAR: no inference kernel runs); on=True
+        restores the network (the tcgen05 kernel where the shape allows).
+        Comparing the two isolates what the trained network adds over the
+        linear fit, and what it costs."""
+        self.mlp.set_inference_kernel(abi.SP_MLP_KERNEL_AUTO if on else abi.SP_MLP_KERNEL_LINEAR)
 
     WARM_MAX_ITERATIONS = 8  # a miss restarts cold after this many iterations
 
