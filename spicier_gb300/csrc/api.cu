@@ -581,15 +581,35 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 32, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
                  s.counters + 1, t->d_drawn, t->num_drawn, s.counters + 4};
-    // a linear warm start is evaluated by the draw kernel itself
-    const bool linear_warm = warm && mlp_linear_only(warm, &D);
-    if (linear_warm) D.x0_out = s.x0;
+    // topology-specialised primary kernel when enabled and buildable
+    const int sidx = prec == SP_PREC_MIXED ? 0 : (prec == SP_PREC_FP64 ? 1 : -1);
+    bool use_spec = false;
+    if (sidx >= 0 && t->spec_enabled[sidx] && !std::getenv("SPICIER_GB300_GENERIC")) {
+        std::string why;
+        use_spec = spec_prepare(const_cast<sp_topology*>(t), prec, why) == SP_OK;
+    }
+    // the double-float specialised kernel computes its constants from the
+    // parameters: the draw kernel skips the derived constants
+    const bool pmode = use_spec && spec_params_mode(t, prec);
+    D.derive = !pmode;
+    // a linear warm start is evaluated by the specialised kernel from each
+    // sample's parameters, or by the draw kernel into x0 for the generic kernels
+    DrawLaunch lin{};
+    const bool linear_warm = warm && mlp_linear_only(warm, &lin);
+    if (linear_warm && !use_spec) {
+        D.lin = lin.lin;
+        D.lin_io = lin.lin_io;
+        D.lin_slots = lin.lin_slots;
+        D.lin_nin = lin.lin_nin;
+        D.lin_nout = lin.lin_nout;
+        D.x0_out = s.x0;
+    }
     {
         ProfScope prof(ctx, "draw_params", st);
         SP_CUDA(ctx, launch_draw(D, st), "draw launch");
     }
     if (linear_warm) {
-        d_x0 = s.x0;
+        if (!use_spec) d_x0 = s.x0;
     } else if (warm) {
         ProfScope prof(ctx, "mlp_warm_start", st);
         SP_CUDA(ctx, mlp_warm_start(warm, s.params, (size_t)count, (int)count, s.x0, st), "network warm start");
@@ -608,6 +628,20 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     L.fail_list = s.fail_list;
     L.fail_count = s.counters;
     L.work_next = reinterpret_cast<unsigned long long*>(s.counters + 2);
+    if (linear_warm && use_spec) {
+        L.lin_params = s.params;
+        L.lin_pstride = count;
+        L.lin = lin.lin;
+        L.lin_io = lin.lin_io;
+        L.lin_slots = lin.lin_slots;
+        L.lin_nin = lin.lin_nin;
+    }
+    if (pmode) {
+        L.params = s.params;
+        L.params_stride = count;
+        L.derived_out = s.derived;
+    }
+    const bool warm_start = d_x0 || L.lin;
     const int kprec = prec == SP_PREC_MIXED ? SP_PREC_MIXED : SP_PREC_FP64;
     size_t per = kprec == SP_PREC_MIXED ? work_bytes_per_thread<SP_PREC_MIXED>(t->n)
                                         : work_bytes_per_thread<SP_PREC_FP64>(t->n);
@@ -624,16 +658,9 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     static const char* kname[3] = {"newton_primary_fp64", "newton_primary_mixed", "newton_primary_fp64_exact"};
     static const char* fname[3] = {"newton_fallback_fp64", "newton_fallback_mixed", "newton_fallback_fp64_exact"};
     static const char* sname[2] = {"newton_primary_mixed_spec", "newton_primary_fp64_spec"};
-    // topology-specialised primary kernel when enabled and buildable
-    const int sidx = prec == SP_PREC_MIXED ? 0 : (prec == SP_PREC_FP64 ? 1 : -1);
-    bool use_spec = false;
-    if (sidx >= 0 && t->spec_enabled[sidx] && !std::getenv("SPICIER_GB300_GENERIC")) {
-        std::string why;
-        use_spec = spec_prepare(const_cast<sp_topology*>(t), prec, why) == SP_OK;
-    }
     // the attempt from a warm start may carry its own iteration cap
     NewtonLaunch Lp = L;
-    if (d_x0 && cfg->warm_max_iterations > 0 && cfg->warm_max_iterations < cfg->max_iterations)
+    if (warm_start && cfg->warm_max_iterations > 0 && cfg->warm_max_iterations < cfg->max_iterations)
         Lp.cfg.max_iterations = cfg->warm_max_iterations;
     cudaError_t e;
     {
@@ -645,7 +672,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
                                            : launch_newton_fast(kprec, Lp, false, grid, block, smem, st);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "newton launch");
-    const bool any_fallback = d_x0 || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE));
+    const bool any_fallback = warm_start || (cfg->fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE));
     if (any_fallback) {
         // one-warp blocks (a few KB of shared memory each) fit beside the
         // primary kernel's blocks, so under programmatic dependent launch they

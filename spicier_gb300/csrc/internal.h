@@ -39,6 +39,9 @@ struct DrawLaunch {
     const int* lin_slots = nullptr;
     int lin_nin = 0, lin_nout = 0;
     double* x0_out = nullptr;
+    // false: skip the derived constants (the consumer, the double-float
+    // specialised kernel, computes its constants from the parameters)
+    bool derive = true;
 };
 
 cudaError_t launch_bsim3_eval(int pmos, const double* card, const double* bias, uint64_t count, double* out,
@@ -255,6 +258,9 @@ struct sp_topology {
 
 namespace sp {
 int spec_prepare(sp_topology* t, int prec, std::string& err);
+// True when the specialised kernel of t at `prec` reads each sample's
+// parameters (and computes its constants) rather than the derived constants.
+bool spec_params_mode(const sp_topology* t, int prec);
 cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, cudaStream_t st);
 void spec_release_all(sp_ctx* ctx);
 }  // namespace sp

@@ -99,12 +99,13 @@ __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_kernel(Draw
             __syncthreads();
         }
         if (!live) continue;
-        for (int e = warp; e < c.num_elements; e += kDrawLanes) {
-            const sp_element el = c.el[e];
-            double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
-            const size_t st = L.count;
-            derive_element(el, P, [&](int k, double v) { out[k * st] = v; });
-        }
+        if (L.derive)
+            for (int e = warp; e < c.num_elements; e += kDrawLanes) {
+                const sp_element el = c.el[e];
+                double* out = L.derived_soa + (size_t)c.doff[e] * L.count + s;
+                const size_t st = L.count;
+                derive_element(el, P, [&](int k, double v) { out[k * st] = v; });
+            }
         // linear warm start: lane y evaluates unknowns y, y + 8, ... in FP32 (as
         // the network kernels' linear term), inputs and weights from shared memory
         if (L.x0_out)

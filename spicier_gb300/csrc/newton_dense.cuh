@@ -283,6 +283,21 @@ struct NewtonLaunch {
     uint32_t* fail_list;    // [count]
     unsigned int* fail_count;
     unsigned long long* work_next = nullptr;  // zeroed work counter of the persistent kernels
+    // learned linear warm start evaluated by the topology-specialised kernel
+    // (x0 == nullptr): x0[k] = lin_io[2 nin + k] + sum_j lin[k][j] (p[lin_slots[j]] - lin_io[j])
+    // with p the sample's parameters at lin_params[slot * lin_pstride + s]
+    const double* lin_params = nullptr;
+    uint64_t lin_pstride = 0;
+    const float* lin = nullptr;
+    const float* lin_io = nullptr;
+    const int* lin_slots = nullptr;
+    int lin_nin = 0;
+    // per-sample parameters [slot][params_stride] for the specialised kernel's
+    // parameters mode, which writes the FP64 derived constants of the samples it
+    // lists for the fallback into derived_out (same layout as dv)
+    const double* params = nullptr;
+    uint64_t params_stride = 0;
+    double* derived_out = nullptr;
 };
 
 __device__ inline void load_start(const NewtonLaunch& L, size_t s, Work& w, bool warm) {
@@ -419,7 +434,7 @@ __global__ void newton_fallback_kernel(NewtonLaunch L) {
     pdl_trigger();
     Work w = make_work<PREC>(smem, L.c.n, blockDim.x, threadIdx.x);
     const int n = L.c.n;
-    const bool warm = L.x0 != nullptr;
+    const bool warm = L.x0 != nullptr || L.lin != nullptr;  // listed samples started warm
     const unsigned int misses = *L.fail_count;
     for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < misses; j += gridDim.x * blockDim.x) {
         const size_t s = L.fail_list[j];

@@ -185,6 +185,8 @@ struct SpecArgs {
     unsigned int* fail_list; unsigned int* fail_count;
     double reltol, vabstol, iabstol; int max_it; int fallback_any;
     u64* next;
+    const double* lp; u64 lpstride; const float* lw; const float* lio; const int* lslots; int lnin;
+    double* dvo;
 };
 __device__ __forceinline__ bool spx_fin(double v) {  // not Inf / NaN, on the integer pipe
     return ((unsigned int)(__double_as_longlong(v) >> 32) & 0x7ff00000u) != 0x7ff00000u;
@@ -582,6 +584,78 @@ void emit_elements_df(std::ostringstream& o, const sp_topology* t, const Pattern
     }
 }
 
+// C++ literal of a double (exact, hexadecimal) and of its FP32 rounding.
+std::string lit64(double v) {
+    char b[64];
+    snprintf(b, sizeof b, "%a", v);
+    return std::string("(") + b + ")";
+}
+std::string lit32(double v) {
+    char b[64];
+    snprintf(b, sizeof b, "%af", (double)(float)v);
+    return std::string("(") + b + ")";
+}
+
+// Parameters mode of the double-float kernel: the per-sample constants are
+// computed from the sample's parameters (drawn slots loaded, fixed slots
+// compiled in as literals) instead of read from the draw kernel's derived
+// constants, so that kernel skips its derivation.  pd<slot> is the loaded
+// FP64 value of drawn slot `slot`.
+struct ParamExpr {
+    const sp_topology* t;
+    std::string d(int slot) const {  // FP64 value
+        const sp_param& p = t->h_params[slot];
+        return p.kind == SP_DRAW_FIXED ? lit64(p.a) : "pd" + std::to_string(slot);
+    }
+    std::string f(int slot) const {  // FP32 value
+        const sp_param& p = t->h_params[slot];
+        return p.kind == SP_DRAW_FIXED ? lit32(p.a) : "__double2float_rn(pd" + std::to_string(slot) + ")";
+    }
+};
+
+// Drawn parameter slots that the elements of t read (parameters mode loads these).
+std::vector<int> drawn_slots_used(const sp_topology* t) {
+    std::vector<int> out;
+    auto use = [&](int slot) {
+        if (slot >= 0 && slot < t->num_params && t->h_params[slot].kind != SP_DRAW_FIXED &&
+            std::find(out.begin(), out.end(), slot) == out.end())
+            out.push_back(slot);
+    };
+    for (const sp_element& el : t->h_elements) {
+        if (el.kind == SP_EL_NMOS || el.kind == SP_EL_PMOS)
+            for (int k : {0, 1, 2, 3, 4, 5}) use(el.field[k]);
+        else if (el.kind == SP_EL_R || el.kind == SP_EL_C || el.kind == SP_EL_L || el.kind == SP_EL_V ||
+                 el.kind == SP_EL_I)
+            use(el.field[0]);
+    }
+    return out;
+}
+
+// FP64 derived constants of element e (derive_element's operations in its
+// order: IEEE division and products, so the values equal the draw kernel's).
+void emit_derive64(std::ostringstream& o, const sp_topology* t, const std::vector<int>& doff, const ParamExpr& pe,
+                   const char* indent) {
+    for (int e = 0; e < t->num_elements; ++e) {
+        const sp_element& el = t->h_elements[e];
+        const int d0 = doff[e];
+        switch (el.kind) {
+            case SP_EL_R:
+                o << indent << "c" << d0 << " = 1.0 / " << pe.d(el.field[0]) << ";\n";
+                break;
+            case SP_EL_NMOS:
+            case SP_EL_PMOS:
+                o << indent << "c" << d0 << " = fabs(" << pe.d(el.field[0]) << ");\n"
+                  << indent << "c" << d0 + 1 << " = ((" << pe.d(el.field[1]) << " * " << pe.d(el.field[5]) << ") * "
+                  << pe.d(el.field[3]) << ") / " << pe.d(el.field[4]) << ";\n"
+                  << indent << "c" << d0 + 2 << " = " << pe.d(el.field[2]) << ";\n";
+                break;
+            default:  // C, L, V, I
+                o << indent << "c" << d0 << " = " << pe.d(el.field[0]) << ";\n";
+                break;
+        }
+    }
+}
+
 std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     const int n = t->n, nn = t->num_nodes;
     std::vector<int> doff(t->num_elements);
@@ -603,12 +677,24 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
       << "  asm volatile(\"griddepcontrol.launch_dependents;\" ::: \"memory\");\n"
       << "  const u64 nthreads = (u64)gridDim.x * blockDim.x;\n"
       << "  u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
+      << "  extern __shared__ __align__(16) unsigned char spx_smem[];\n"
+      // learned linear warm start: weights lw[n][lnin], in_mean, out_mean and the input slots,
+      // staged by the block (behind the per-thread constants) before any thread leaves
+      << "  float* const spx_lw = reinterpret_cast<float*>(spx_smem + " << spec_smem_bytes(t, fp32_jac) << ");\n"
+      << "  float* const spx_linm = spx_lw + " << n << " * a.lnin;\n"
+      << "  float* const spx_lout = spx_linm + a.lnin;\n"
+      << "  int* const spx_lslot = reinterpret_cast<int*>(spx_lout + " << n << ");\n"
+      << "  if (a.lw) {\n"
+      << "    for (int i = threadIdx.x; i < " << n << " * a.lnin; i += blockDim.x) spx_lw[i] = a.lw[i];\n"
+      << "    for (int i = threadIdx.x; i < a.lnin; i += blockDim.x) { spx_linm[i] = a.lio[i]; spx_lslot[i] = a.lslots[i]; }\n"
+      << "    for (int i = threadIdx.x; i < " << n << "; i += blockDim.x) spx_lout[i] = a.lio[2 * a.lnin + i];\n"
+      << "    __syncthreads();\n"
+      << "  }\n"
       << "  if (s >= a.count) return;\n"
       << "  const u64 st = a.stride;\n"
-      << "  const bool warm = a.x0 != 0;\n";
+      << "  const bool warm = a.x0 != 0 || a.lw != 0;\n";
     if (sm) {
-        o << "  extern __shared__ __align__(16) unsigned char spx_smem[];\n"
-          << "  volatile double* const spx_cd = reinterpret_cast<volatile double*>(spx_smem) + threadIdx.x;\n"
+        o << "  volatile double* const spx_cd = reinterpret_cast<volatile double*>(spx_smem) + threadIdx.x;\n"
           << "  volatile float* const spx_cf = reinterpret_cast<volatile float*>(spx_smem + " << t->num_derived * 8 * 128
           << ") + threadIdx.x;\n";
     } else {
@@ -627,17 +713,67 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     o << "  int it, code;\n";
     // per-sample set-up: constants, linear Jacobian, start point
     std::ostringstream ld;
-    ld << "  {\n  const double* dv = a.dv + s;\n";
-    for (int k = 0; k < t->num_derived; ++k) ld << "  c" << k << " = __ldg(dv + " << k << " * st);\n";
-    for (int k : fcs) ld << "  cf" << k << " = spx_f(c" << k << ");\n";
-    for (int e = 0; e < t->num_elements; ++e)
-        if (t->h_elements[e].kind == SP_EL_R)
-            ld << "  g" << e << " = " << (fp32_jac ? "spx_f(c" : "(JT)(c") << doff[e] << ");\n";
+    const ParamExpr pe{t};
+    const std::vector<int> pslots = drawn_slots_used(t);
+    if (dfm) {
+        // parameters mode: the drawn parameters (loads issued together), then the
+        // FP32 constants: |VTO|, ((KP NF) W) / L and LAMBDA, 1 / R, source values
+        // (at most a few FP32 roundings from the FP64 constants rounded to FP32)
+        ld << "  {\n";
+        for (int slot : pslots)
+            ld << "  const double pd" << slot << " = __ldg(a.lp + (u64)" << slot << " * a.lpstride + s);\n";
+        for (int e = 0; e < t->num_elements; ++e) {
+            const sp_element& el = t->h_elements[e];
+            const int d0 = doff[e];
+            switch (el.kind) {
+                case SP_EL_R:
+                    ld << "  g" << e << " = __fdiv_rn(1.f, " << pe.f(el.field[0]) << ");\n";
+                    break;
+                case SP_EL_NMOS:
+                case SP_EL_PMOS:
+                    ld << "  cf" << d0 << " = fabsf(" << pe.f(el.field[0]) << ");\n"
+                       << "  cf" << d0 + 1 << " = __fdiv_rn(__fmul_rn(__fmul_rn(" << pe.f(el.field[1]) << ", "
+                       << pe.f(el.field[5]) << "), " << pe.f(el.field[3]) << "), " << pe.f(el.field[4]) << ");\n"
+                       << "  cf" << d0 + 2 << " = " << pe.f(el.field[2]) << ";\n";
+                    break;
+                case SP_EL_V:
+                case SP_EL_I:
+                    ld << "  cf" << d0 << " = " << pe.f(el.field[0]) << ";\n";
+                    break;
+                default:
+                    break;
+            }
+        }
+    } else {
+        ld << "  {\n  const double* dv = a.dv + s;\n";
+        for (int k = 0; k < t->num_derived; ++k) ld << "  c" << k << " = __ldg(dv + " << k << " * st);\n";
+        for (int k : fcs) ld << "  cf" << k << " = spx_f(c" << k << ");\n";
+        for (int e = 0; e < t->num_elements; ++e)
+            if (t->h_elements[e].kind == SP_EL_R)
+                ld << "  g" << e << " = " << (fp32_jac ? "spx_f(c" : "(JT)(c") << doff[e] << ");\n";
+    }
+    // the learned linear warm start of sample s into xl[] (FP32, inputs eight at a
+    // time with their loads in flight together; the same operations in the same
+    // order as the draw kernel's evaluation of it)
+    ld << "  float xl[" << n << "];\n"
+       << "  if (a.lw) {\n"
+       << "    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) xl[i] = spx_lout[i];\n"
+       << "    for (int j0 = 0; j0 < a.lnin; j0 += 8) {\n"
+       << "      float pv[8];\n"
+       << "      #pragma unroll\n      for (int u = 0; u < 8; ++u)\n"
+       << "        pv[u] = j0 + u < a.lnin ? __double2float_rn(__ldg(a.lp + (u64)spx_lslot[j0 + u] * a.lpstride + s))"
+          " - spx_linm[j0 + u] : 0.f;\n"
+       << "      #pragma unroll\n      for (int u = 0; u < 8; ++u)\n"
+       << "        if (j0 + u < a.lnin) {\n"
+       << "          #pragma unroll\n          for (int i = 0; i < " << n << "; ++i) xl[i] = fmaf(spx_lw[i * a.lnin + j0 + u], pv[u], xl[i]);\n"
+       << "        }\n    }\n  }\n";
     if (dfm)  // the start point rounded to FP32 (a starting guess: its low part is not needed)
         ld << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i)\n"
-           << "    X[i] = spx_df{warm ? spx_f(a.x0[s * " << n << " + i]) : (a.nodeset ? spx_f(a.nodeset[i]) : 0.f), 0.f};\n";
+           << "    X[i] = spx_df{a.lw ? xl[i] : (a.x0 ? __double2float_rn(a.x0[s * " << n
+           << " + i]) : (a.nodeset ? __double2float_rn(a.nodeset[i]) : 0.f)), 0.f};\n";
     else
-        ld << "  if (warm) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n
+        ld << "  if (a.lw) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = (double)xl[i];\n"
+           << "  } else if (a.x0) {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = a.x0[s * " << n
            << " + i];\n"
            << "  } else if (a.nodeset) {\n    #pragma unroll\n    for (int i = 0; i < " << n
            << "; ++i) x[i] = a.nodeset[i];\n"
@@ -708,16 +844,28 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     // status, outputs, miss list, residual of sample s
     if (dfm)
         o << "    double x[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n
-          << "; ++i) x[i] = spx_d(X[i].h) + spx_d(X[i].l);\n";
+          << "; ++i) x[i] = (double)X[i].h + (double)X[i].l;\n";
     o << "    bool fin = true;\n    #pragma unroll\n    for (int i = 0; i < " << n
       << "; ++i) fin = fin && spx_fin(x[i]);\n"
       << "    unsigned char st8 = !fin ? 3 : (unsigned char)code;\n"
       << "    if (warm) st8 |= 0x10;\n"
       << "    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) a.x[s * " << n << " + i] = x[i];\n"
       << "    if (a.iters) a.iters[s] = it;\n"
-      << "    if ((st8 & 15) != 0 && (warm || a.fallback_any)) {\n"
-      << "      unsigned int k = atomicAdd(a.fail_count, 1u); a.fail_list[k] = (unsigned int)s;\n"
-      << "    } else if (a.resid) {\n"
+      << "    const bool spx_miss = (st8 & 15) != 0 && (warm || a.fallback_any);\n";
+    if (dfm) {
+        // parameters mode: the FP64 constants of a listed sample (for the generic
+        // fallback) or of a residual, from the sample's parameters
+        o << "    if (spx_miss || a.resid) {\n";
+        for (int slot : pslots)
+            o << "      const double pd" << slot << " = __ldg(a.lp + (u64)" << slot << " * a.lpstride + s);\n";
+        emit_derive64(o, t, doff, pe, "      ");
+        o << "    }\n";
+    }
+    o << "    if (spx_miss) {\n"
+      << "      unsigned int k = atomicAdd(a.fail_count, 1u); a.fail_list[k] = (unsigned int)s;\n";
+    if (dfm)
+        for (int k = 0; k < t->num_derived; ++k) o << "      a.dvo[" << k << " * st + s] = c" << k << ";\n";
+    o << "    } else if (a.resid) {\n"
       << "    double F[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) F[i] = 0.0;\n";
     emit_elements(o, t, P, doff, false);
     o << "    double r = 0.0;\n";
@@ -751,7 +899,17 @@ struct SpecArgsHost {
     int max_it;
     int fallback_any;
     unsigned long long* next;
+    // learned linear warm start (lw != nullptr): see NewtonLaunch
+    const double* lp;
+    unsigned long long lpstride;
+    const float* lw;
+    const float* lio;
+    const int* lslots;
+    int lnin;
+    double* dvo;  // parameters mode: FP64 derived constants of the samples put on the miss list
 };
+
+bool spec_params_mode(const sp_topology* t, int prec) { return prec == SP_PREC_MIXED && df_supported(t); }
 
 // Build (once) the specialised kernel of topology t for `prec` (MIXED: FP32
 // Jacobian; FP64: FP64 Jacobian).  Returns SP_OK or an error with the reason.
@@ -854,6 +1012,14 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     a.fallback_any = (L.cfg.fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE)) ? 1 : 0;
     a.next = L.work_next;
     if (!a.next) return cudaErrorInvalidValue;
+    a.lp = L.params ? L.params : L.lin_params;
+    a.lpstride = L.params ? L.params_stride : L.lin_pstride;
+    a.dvo = L.derived_out;
+    if (spec_params_mode(t, prec) && (!a.lp || !a.dvo)) return cudaErrorInvalidValue;
+    a.lw = L.lin;
+    a.lio = L.lin_io;
+    a.lslots = L.lin_slots;
+    a.lnin = L.lin_nin;
     void* args[] = {&a};
     // tuned resident blocks per SM (setting "spec.bpsm.<precision>"), never above the occupancy limit
     int bpsm = t->spec_bpsm[slot];
@@ -861,7 +1027,14 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     if (tb >= 1 && tb < bpsm) bpsm = tb;
     const uint64_t resident = (uint64_t)t->ctx->num_sms * (uint64_t)bpsm;
     const unsigned grid = (unsigned)std::min<uint64_t>((L.count + 127) / 128, resident);
-    ChainedLaunch cl(dim3(grid), dim3(128), spec_smem_bytes(t, prec == SP_PREC_MIXED), st);
+    const size_t lin_bytes = L.lin ? sizeof(float) * ((size_t)t->n * L.lin_nin + 2 * (size_t)L.lin_nin + t->n) : 0;
+    const size_t smem = spec_smem_bytes(t, prec == SP_PREC_MIXED) + lin_bytes;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)t->spec_kernel[slot],
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    ChainedLaunch cl(dim3(grid), dim3(128), smem, st);
     return cudaLaunchKernelExC(&cl.cfg, (const void*)t->spec_kernel[slot], args);
 }
 

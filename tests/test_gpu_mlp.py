@@ -242,11 +242,14 @@ def test_tcgen05_hidden256_row_counts(ctx, rows):
     m.close()
 
 
-def test_linear_warm_start_in_the_draw_kernel(ctx):
-    """SP_MLP_KERNEL_LINEAR: the sweep's draw kernel evaluates the fitted
-    linear term (no inference kernel); the standalone warm start equals the
-    formula, the learned sweep converges every sample from it in fewer
-    iterations than the nodeset start, within SPICE tolerance of the oracle."""
+def test_linear_warm_start(ctx):
+    """SP_MLP_KERNEL_LINEAR: the fitted linear term alone, evaluated by the
+    topology-specialised Newton kernel from each sample's parameters (or by
+    the draw kernel for the generic kernels); no inference kernel runs.  The
+    standalone warm start equals the formula; the learned sweep equals, bit
+    for bit, a sweep started from that standalone warm start, and converges
+    every sample in fewer iterations than the nodeset start, within SPICE
+    tolerance of the oracle."""
     circ = configs.miller_opamp()
     topo = ctx.topology(circ)
     ws = WarmStart(ctx, circ, n_inputs=10, seed=3)
@@ -290,5 +293,16 @@ def test_linear_warm_start_in_the_draw_kernel(ctx):
     assert il.mean() < base.iters.mean() - 0.5, (il.mean(), base.iters.mean())
     xo, _io, _so, _ = oracle.newton_dc(circ, abi.newton_config(), 1, N)
     assert spice_close(xl, xo, circ.num_nodes)
+    # the same sweep from the standalone linear warm start of the same draws
+    prm = torch.empty((N, nslots), dtype=torch.float64, device=dev)
+    ctx.newton_dc_device(topo, cfg, 1, N, torch.empty_like(x), params=prm)
+    x0 = torch.empty((N, circ.n), dtype=torch.float64, device=dev)
+    m.warm_start_device(prm.t().contiguous(), N, N, x0)
+    cfg8 = abi.newton_config(precision=abi.SP_PREC_MIXED, warm_max_iterations=ws.WARM_MAX_ITERATIONS)
+    x2, it2, st2 = torch.empty_like(x), torch.empty_like(it), torch.empty_like(st)
+    ctx.newton_dc_device(topo, cfg8, 1, N, x2, x0=x0, iters=it2, status=st2)
+    torch.cuda.synchronize()
+    assert np.array_equal(x2.cpu().numpy().view(np.uint64), xl.view(np.uint64))
+    assert np.array_equal(it2.cpu().numpy(), il) and np.array_equal(st2.cpu().numpy(), sl)
     ws.use_network(True)
     ws.mlp.close()
