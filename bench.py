@@ -251,16 +251,6 @@ def structural_nnz(circuit):
     return len(pos)
 
 
-def derived_slots(circuit):
-    from spicier_gb300 import abi
-    cnt = 0
-    for e in circuit.elements:
-        k = e["kind"]
-        cnt += 3 if k in (abi.SP_EL_D, abi.SP_EL_NMOS, abi.SP_EL_PMOS) else 8 if k in (abi.SP_EL_NPN,
-                                                                                        abi.SP_EL_PNP) else 1
-    return cnt
-
-
 def cpu_baseline(circuit, samples, threads=0, min_seconds=0.0):
     """The oracle port (the reference algorithm restated in C++) timed on the
     host cores over a bounded sample of the workload: chunks of `samples`
@@ -643,23 +633,25 @@ def main():
 
     # rooflines of the headline's kernels (average launch durations, live)
     kavg = {k: v[1] / max(v[0], 1) for k, v in head["prof"].items()}
-    m_mos = sum(1 for e in circ.elements if e["kind"] in (abi.SP_EL_NMOS, abi.SP_EL_PMOS))
     rooflines = {}
     if "newton_primary_mixed_spec" in kavg:
-        # FP64 instructions per sample-iteration of the mixed specialised kernel: per MOSFET the
-        # drain current (8) and its two KCL terms, per resistor 4, per source 2-3, the update n
+        # the double-float kernel has no FP64 instruction in its iteration and is
+        # latency-bound (one sample per thread at this size): its roofline is the
+        # issue rate, warp instructions per launch (the committed ncu capture) over
+        # the live launch time, against one instruction per clock per SM sub-partition
         ms = kavg["newton_primary_mixed_spec"]
-        kinds = [e["kind"] for e in circ.elements]
-        per_it = (10 * m_mos + 4 * kinds.count(abi.SP_EL_R) + 3 * kinds.count(abi.SP_EL_V)
-                  + 2 * kinds.count(abi.SP_EL_I) + n)
-        f64 = per_it * head["iters"] * N
-        a = f64 / (ms * 1e-3) / 1e12
-        pk = fp64_peak / 2  # FP64 instructions per second (an FMA counts two flops of the measured peak)
-        rooflines["newton_primary_mixed_spec"] = {
-            "bound": "fp64", "achieved": a, "peak": pk, "unit": "T FP64 instructions/s", "frac": a / pk,
-            "traffic": read_profile_number("newton_spec_mixed_opamp.md", "dram_bytes_per_launch"),
-            "avg_launch_ms": ms, "fp64_instructions_per_launch": f64,
-            "peak_source": "FP64 FMA chains measured live by this bench (of measured)"}
+        inst = read_profile_number("newton_spec_mixed_opamp.md", "warp_instructions_per_launch")
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        clk = (head.get("clocks") or {}).get("sm_max_mhz") or 2070.0
+        pk = 4 * sms * clk * 1e6 / 1e12
+        if inst:
+            a = inst / (ms * 1e-3) / 1e12
+            rooflines["newton_primary_mixed_spec"] = {
+                "bound": "latency (issue)", "achieved": a, "peak": pk, "unit": "T warp instructions/s",
+                "frac": a / pk,
+                "traffic": read_profile_number("newton_spec_mixed_opamp.md", "dram_bytes_per_launch"),
+                "avg_launch_ms": ms, "warp_instructions_per_launch": inst,
+                "peak_source": "4 sub-partitions x SMs x the SM clock seen during the timed region"}
     if "mlp_warm_start" in kavg:
         ms = kavg["mlp_warm_start"]
         ni, H, nl = ws.mlp.n_in, ws.mlp.n_hidden, ws.mlp.n_layers
@@ -670,7 +662,9 @@ def main():
                                        "flops_per_launch": fl, "peak_source": f"bf16_tflops of {peak_src}"}
     if "draw_params" in kavg:
         ms = kavg["draw_params"]
-        by = 8 * (len(circ.params) + derived_slots(circ)) * N
+        # the headline's draw kernel writes the parameters only (the double-float
+        # Newton kernel derives its own constants)
+        by = 8 * len(circ.params) * N
         inst = read_profile_number("draw_params_opamp.md", "alu_warp_instructions_per_sample")
         entry = {"avg_launch_ms": ms, "bytes_per_launch": by,
                  "hbm_frac": by / (ms * 1e-3) / 1e9 / hbm_peak,
@@ -1012,8 +1006,9 @@ def main():
                     "warm_start": (f"MLP {ws.mlp.n_in}->{ws.mlp.n_layers}x{ws.mlp.n_hidden} GELU->{n} "
                                    "(tcgen05, FP16 operands, TMEM) + least-squares linear term")
                     if head_name == "network" else
-                    f"least-squares linear term on {ws.mlp.n_in} drawn parameters, evaluated in FP32 by the "
-                    "draw kernel (the network variant is timed beside it: learned_variants)"},
+                    f"least-squares linear term on {ws.mlp.n_in} drawn parameters, evaluated in FP32 in the "
+                    "specialised Newton kernel's sample set-up (the network variant is timed beside it: "
+                    "learned_variants)"},
             "learned_variants": {k: arm(v) for k, v in variants.items()},
             "plain_fp64": arm(plain),
             "iters_per_solve": head["iters"], "max_resid_A": head["rmax"],
