@@ -641,6 +641,9 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
         L.params_stride = count;
         L.derived_out = s.derived;
     }
+    // with one sample per thread the specialised kernel reduces its blocks'
+    // moments itself; a final kernel merges them (replacing the rows pass)
+    const bool fused_moments = d_moments && d_status && use_spec && spec_one_sample_per_thread(t, prec, count);
     const bool warm_start = d_x0 || L.lin;
     const int kprec = prec == SP_PREC_MIXED ? SP_PREC_MIXED : SP_PREC_FP64;
     size_t per = kprec == SP_PREC_MIXED ? work_bytes_per_thread<SP_PREC_MIXED>(t->n)
@@ -660,6 +663,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     static const char* sname[2] = {"newton_primary_mixed_spec", "newton_primary_fp64_spec"};
     // the attempt from a warm start may carry its own iteration cap
     NewtonLaunch Lp = L;
+    if (fused_moments) Lp.moments_partial = s.partial;
     if (warm_start && cfg->warm_max_iterations > 0 && cfg->warm_max_iterations < cfg->max_iterations)
         Lp.cfg.max_iterations = cfg->warm_max_iterations;
     cudaError_t e;
@@ -687,7 +691,12 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
                                        : launch_newton_fast(kprec, L, true, fgrid, fblock, fsmem, st);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "fallback launch");
     }
-    if (d_moments) {
+    if (d_moments && fused_moments) {
+        ProfScope prof(ctx, "moments", st);
+        e = launch_moments_from_partials(s.partial, (uint32_t)((count + 127) / 128), s.counters, d_x, count,
+                                         (uint32_t)t->n, d_status, d_moments, st);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "moments launch");
+    } else if (d_moments) {
         ProfScope prof(ctx, "moments", st);
         e = launch_moments(d_x, count, (uint32_t)t->n, (uint32_t)t->n, d_status, s.partial, s.moment_blocks,
                            d_moments, st);

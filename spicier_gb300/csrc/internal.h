@@ -90,6 +90,12 @@ cudaError_t launch_moments(const double* values, uint64_t rows, uint32_t ld, uin
                            const uint8_t* status, sp_moments* partial, uint32_t nblocks, sp_moments* out,
                            cudaStream_t st);
 cudaError_t launch_moments_merge(sp_moments* acc, const sp_moments* other, uint32_t n, cudaStream_t st);
+// Moments from the specialised kernel's per-block partials ([cols][nblocks]),
+// merged in a fixed order; when the fallback changed samples (*fail_count > 0)
+// the moments are computed from the values instead (same order for any run).
+cudaError_t launch_moments_from_partials(const sp_moments* partial, uint32_t nblocks, const unsigned int* fail_count,
+                                         const double* values, uint64_t rows, uint32_t cols, const uint8_t* status,
+                                         sp_moments* out, cudaStream_t st);
 cudaError_t prepare_fast_kernels(int max_smem);
 
 // Largest dense size of the thread-per-sample Newton kernels.
@@ -261,6 +267,9 @@ int spec_prepare(sp_topology* t, int prec, std::string& err);
 // True when the specialised kernel of t at `prec` reads each sample's
 // parameters (and computes its constants) rather than the derived constants.
 bool spec_params_mode(const sp_topology* t, int prec);
+// True when the specialised kernel's grid gives every sample its own thread
+// (then it can reduce its blocks' moments itself).
+bool spec_one_sample_per_thread(const sp_topology* t, int prec, uint64_t count);
 cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, cudaStream_t st);
 void spec_release_all(sp_ctx* ctx);
 }  // namespace sp

@@ -353,6 +353,66 @@ __global__ void moments_merge_kernel(sp_moments* __restrict__ acc, const sp_mome
     acc[i] = a;
 }
 
+// One block per column: the specialised kernel's block partials merged in
+// block order (four in flight per thread, then a pairwise tree), or, when the
+// fallback kernel changed samples after those partials were formed, the
+// column's moments over every converged row (rows t, t + 256, ... per thread,
+// then the same tree).
+__global__ void __launch_bounds__(256) moments_partials_kernel(const sp_moments* __restrict__ partial,
+                                                                uint32_t nblocks,
+                                                                const unsigned int* __restrict__ fail_count,
+                                                                const double* __restrict__ v, uint64_t rows,
+                                                                uint32_t ld, const uint8_t* __restrict__ status,
+                                                                sp_moments* __restrict__ out) {
+    __shared__ sp_moments sh[256];
+    pdl_wait();
+    pdl_trigger();
+    const uint32_t col = blockIdx.x;
+    sp_moments m{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+    if (*fail_count == 0) {
+        for (uint32_t b0 = threadIdx.x; b0 < nblocks; b0 += 4 * 256) {
+            sp_moments q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t b = b0 + (uint32_t)u * 256;
+                q[u] = b < nblocks ? partial[(size_t)col * nblocks + b] : sp_moments{0, 0.0, 0.0, CUDART_INF, -CUDART_INF};
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (b0 + (uint32_t)u * 256 < nblocks) mom_merge(m, q[u]);
+        }
+    } else {
+        long long kmin = order_key(CUDART_INF), kmax = order_key(-CUDART_INF);
+        for (uint64_t i = threadIdx.x; i < rows; i += 256) {
+            if (status && (status[i] & SP_ST_MASK) != SP_ST_CONVERGED) continue;
+            const double x = v[i * ld + col];
+            m.count += 1;
+            m.sum += x;
+            m.sum_sq += x * x;
+            const long long k = order_key(x);
+            kmin = k < kmin ? k : kmin;
+            kmax = k > kmax ? k : kmax;
+        }
+        m.min = from_key(kmin);
+        m.max = from_key(kmax);
+    }
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = 128; w >= 1; w >>= 1) {
+        if ((int)threadIdx.x < w) mom_merge(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[col] = sh[0];
+}
+
+cudaError_t launch_moments_from_partials(const sp_moments* partial, uint32_t nblocks, const unsigned int* fail_count,
+                                         const double* values, uint64_t rows, uint32_t cols, const uint8_t* status,
+                                         sp_moments* out, cudaStream_t st) {
+    if (cols == 0) return cudaSuccess;
+    return launch_chained(moments_partials_kernel, dim3(cols), dim3(256), 0, st, partial, nblocks, fail_count, values,
+                          rows, cols, status, out);
+}
+
 cudaError_t launch_moments_merge(sp_moments* acc, const sp_moments* other, uint32_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     moments_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(acc, other, n);

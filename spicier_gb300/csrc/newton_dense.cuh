@@ -298,6 +298,8 @@ struct NewtonLaunch {
     const double* params = nullptr;
     uint64_t params_stride = 0;
     double* derived_out = nullptr;
+    // per-block moments of the specialised kernel (one sample per thread), [n][grid]
+    sp_moments* moments_partial = nullptr;
 };
 
 __device__ inline void load_start(const NewtonLaunch& L, size_t s, Work& w, bool warm) {

@@ -178,6 +178,8 @@ bool plan(const sp_topology* t, Pattern& P, std::string& why) {
 
 const char* kPreamble = R"SRC(
 typedef unsigned long long u64;
+// Per-block moments of the converged samples (the layout of sp_moments).
+struct spx_mom { u64 count; double sum, sum_sq, mn, mx; };
 struct SpecArgs {
     const double* dv; u64 stride; u64 count;
     const double* x0; const double* nodeset;
@@ -187,6 +189,7 @@ struct SpecArgs {
     u64* next;
     const double* lp; u64 lpstride; const float* lw; const float* lio; const int* lslots; int lnin;
     double* dvo;
+    spx_mom* mom;
 };
 __device__ __forceinline__ bool spx_fin(double v) {  // not Inf / NaN, on the integer pipe
     return ((unsigned int)(__double_as_longlong(v) >> 32) & 0x7ff00000u) != 0x7ff00000u;
@@ -265,6 +268,14 @@ __device__ __forceinline__ spx_df spx_mul(spx_df a, spx_df b) {
     return spx_two(p, e);
 }
 __device__ __forceinline__ bool spx_finf(float v) { return (__float_as_uint(v) & 0x7f800000u) != 0x7f800000u; }
+// Order-preserving integer keys of doubles (min and max of the block moments).
+__device__ __forceinline__ long long spx_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (long long)(0x8000000000000000ULL - (unsigned long long)b) - 1;
+}
+__device__ __forceinline__ double spx_unkey(long long k) {
+    return __longlong_as_double(k >= 0 ? k : (long long)(0x8000000000000000ULL - (unsigned long long)(k + 1)));
+}
 // v < 0 from the sign bit (integer pipe); -0 is not negative
 __device__ __forceinline__ bool spx_neg(double v) {
     const long long b = __double_as_longlong(v);
@@ -690,7 +701,8 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
       << "    for (int i = threadIdx.x; i < " << n << "; i += blockDim.x) spx_lout[i] = a.lio[2 * a.lnin + i];\n"
       << "    __syncthreads();\n"
       << "  }\n"
-      << "  if (s >= a.count) return;\n"
+      << "  unsigned char spx_st = 0xff;  // status of the thread's (last) sample\n"
+      << "  if (s < a.count) {\n"
       << "  const u64 st = a.stride;\n"
       << "  const bool warm = a.x0 != 0 || a.lw != 0;\n";
     if (sm) {
@@ -870,7 +882,7 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     emit_elements(o, t, P, doff, false);
     o << "    double r = 0.0;\n";
     for (int i = 0; i < nn; ++i) o << "    r = fmax(r, fabs(F[" << i << "]));\n";
-    o << "    a.resid[s] = r;\n    }\n    if (a.status) a.status[s] = st8;\n";
+    o << "    a.resid[s] = r;\n    }\n    if (a.status) a.status[s] = st8;\n    spx_st = st8;\n";
     // next sample: warp-aggregated fetch from the counter
     o << "    {\n      const unsigned m = __activemask();\n      const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;\n"
       << "      u64 base = 0;\n      if (lane == lead) base = atomicAdd(a.next, (u64)__popc(m));\n"
@@ -878,7 +890,53 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
       << "      s = nthreads + base + (u64)__popc(m & ((1u << lane) - 1u));\n    }\n"
       << "    if (s >= a.count) break;\n";
     o << ld.str();
-    o << "    }\n  }\n}\n";
+    o << "    }\n  }\n  }\n";
+    // moments of the block's samples (the host enables this only when every
+    // thread has exactly one sample, s = blockIdx.x * 128 + threadIdx.x): its
+    // converged unknowns in shared memory, T threads per unknown (T the largest
+    // power of two with T n <= 128) over 128 / T rows each in row order, then
+    // the T partials in order: a fixed order, so the result does not depend on
+    // scheduling
+    int T = 1;
+    while (T * 2 * n <= 128 && T < 32) T *= 2;
+    const int R = 128 / T;
+    o << "  if (a.mom) {\n"
+      << "    __syncthreads();\n"
+      << "    double* const xs = reinterpret_cast<double*>(spx_smem);\n"
+      << "    unsigned char* const oks = spx_smem + 128 * " << n << " * 8;\n"
+      << "    spx_mom* const pm = reinterpret_cast<spx_mom*>(spx_smem + 128 * " << n << " * 8 + 128);\n"
+      << "    const u64 s0 = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n"
+      << "    const bool okm = s0 < a.count && (spx_st & 15) == 0;\n"
+      << "    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) xs[threadIdx.x * " << n
+      << " + i] = okm ? a.x[s0 * " << n << " + i] : 0.0;\n"
+      << "    oks[threadIdx.x] = okm ? 1 : 0;\n"
+      << "    __syncthreads();\n"
+      << "    if (threadIdx.x < " << T * n << ") {\n"
+      << "      const int col = threadIdx.x / " << T << ", q = threadIdx.x % " << T << ";\n"
+      << "      u64 cnt = 0; double sm = 0.0, sq = 0.0;\n"
+      << "      long long kmin = spx_key(__longlong_as_double(0x7ff0000000000000LL));\n"
+      << "      long long kmax = spx_key(__longlong_as_double((long long)0xfff0000000000000ULL));\n"
+      << "      for (int r = " << R << " * q; r < " << R << " * q + " << R << "; ++r) {\n"
+      << "        if (!oks[r]) continue;\n"
+      << "        const double v = xs[r * " << n << " + col];\n"
+      << "        ++cnt; sm += v; sq += v * v;\n"
+      << "        const long long k = spx_key(v); kmin = k < kmin ? k : kmin; kmax = k > kmax ? k : kmax;\n"
+      << "      }\n"
+      << "      pm[threadIdx.x] = spx_mom{cnt, sm, sq, spx_unkey(kmin), spx_unkey(kmax)};\n"
+      << "    }\n"
+      << "    __syncthreads();\n"
+      << "    if (threadIdx.x < " << n << ") {\n"
+      << "      spx_mom m = pm[threadIdx.x * " << T << "];\n"
+      << "      for (int q = 1; q < " << T << "; ++q) {\n"
+      << "        const spx_mom b = pm[threadIdx.x * " << T << " + q];\n"
+      << "        m.count += b.count; m.sum += b.sum; m.sum_sq += b.sum_sq;\n"
+      << "        m.mn = spx_key(b.mn) < spx_key(m.mn) ? b.mn : m.mn;\n"
+      << "        m.mx = spx_key(b.mx) > spx_key(m.mx) ? b.mx : m.mx;\n"
+      << "      }\n"
+      << "      a.mom[(u64)threadIdx.x * gridDim.x + blockIdx.x] = m;\n"
+      << "    }\n"
+      << "  }\n"
+      << "}\n";
     return o.str();
 }
 
@@ -907,6 +965,7 @@ struct SpecArgsHost {
     const int* lslots;
     int lnin;
     double* dvo;  // parameters mode: FP64 derived constants of the samples put on the miss list
+    sp_moments* mom;  // per-block moments [n][grid] (one sample per thread), or nullptr
 };
 
 bool spec_params_mode(const sp_topology* t, int prec) { return prec == SP_PREC_MIXED && df_supported(t); }
@@ -1015,6 +1074,7 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     a.lp = L.params ? L.params : L.lin_params;
     a.lpstride = L.params ? L.params_stride : L.lin_pstride;
     a.dvo = L.derived_out;
+    a.mom = L.moments_partial;
     if (spec_params_mode(t, prec) && (!a.lp || !a.dvo)) return cudaErrorInvalidValue;
     a.lw = L.lin;
     a.lio = L.lin_io;
@@ -1028,7 +1088,11 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     const uint64_t resident = (uint64_t)t->ctx->num_sms * (uint64_t)bpsm;
     const unsigned grid = (unsigned)std::min<uint64_t>((L.count + 127) / 128, resident);
     const size_t lin_bytes = L.lin ? sizeof(float) * ((size_t)t->n * L.lin_nin + 2 * (size_t)L.lin_nin + t->n) : 0;
-    const size_t smem = spec_smem_bytes(t, prec == SP_PREC_MIXED) + lin_bytes;
+    size_t smem = spec_smem_bytes(t, prec == SP_PREC_MIXED) + lin_bytes;
+    if (L.moments_partial) {  // the moments epilogue reuses the block's shared memory
+        if ((L.count + 127) / 128 > grid) return cudaErrorInvalidValue;  // needs one sample per thread
+        smem = std::max(smem, (size_t)128 * t->n * 8 + 128 + (size_t)128 * sizeof(sp_moments));
+    }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute((const void*)t->spec_kernel[slot],
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1036,6 +1100,14 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     }
     ChainedLaunch cl(dim3(grid), dim3(128), smem, st);
     return cudaLaunchKernelExC(&cl.cfg, (const void*)t->spec_kernel[slot], args);
+}
+
+bool spec_one_sample_per_thread(const sp_topology* t, int prec, uint64_t count) {
+    const int slot = prec == SP_PREC_MIXED ? 0 : 1;
+    int bpsm = t->spec_bpsm[slot];
+    const int tb = tune_get(t->ctx, prec == SP_PREC_MIXED ? "spec.bpsm.mixed" : "spec.bpsm.fp64", t->n, 0);
+    if (tb >= 1 && tb < bpsm) bpsm = tb;
+    return (count + 127) / 128 <= (uint64_t)t->ctx->num_sms * (uint64_t)bpsm;
 }
 
 void spec_release_all(sp_ctx* ctx) {

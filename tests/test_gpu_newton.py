@@ -238,3 +238,36 @@ def test_host_entry_mapped_output(ctx, prec):
                                         x.data_ptr(), it.data_ptr(), st.data_ptr(), None, None, None))
     assert same_bits(x.numpy(), r.x)
     assert np.array_equal(it.numpy(), r.iters) and np.array_equal(st.numpy(), r.status)
+
+
+def test_moments_with_fallback_samples(ctx):
+    """Moments of a sweep whose warm starts miss (the specialised kernel lists
+    them, the fallback kernel solves them): the per-block partials are
+    replaced by moments over every converged row; they equal numpy's over the
+    final solutions, as do those of a sweep without misses (block partials)."""
+    import torch
+    circ = configs.miller_opamp()
+    topo = ctx.topology(circ)
+    N, n = 6000, circ.n
+    dev = torch.device("cuda")
+    for bad in (False, True):
+        x = torch.empty((N, n), dtype=torch.float64, device=dev)
+        st = torch.empty(N, dtype=torch.uint8, device=dev)
+        mom = torch.empty((n, 5), dtype=torch.float64, device=dev)
+        cfg = abi.newton_config(precision=MIXED, warm_max_iterations=2)
+        x0 = torch.full((N, n), 50.0 if bad else 0.0, dtype=torch.float64, device=dev) if bad else None
+        ctx.newton_dc_device(topo, cfg, 3, N, x, x0=x0, status=st, moments=mom)
+        torch.cuda.synchronize()
+        xs, ss, m = x.cpu().numpy(), st.cpu().numpy(), mom.cpu()
+        ok = (ss & abi.SP_ST_MASK) == 0
+        assert ok.mean() > 0.99
+        if bad:
+            assert (ss & abi.SP_ST_FLAG_COLD).any()  # the fallback ran
+        counts = m.view(torch.int64)[:, 0].numpy()
+        for col in range(n):
+            v = xs[ok, col]
+            assert counts[col] == len(v)
+            assert m[col, 3].item() == v.min() and m[col, 4].item() == v.max()
+            assert abs(m[col, 1].item() - v.sum()) <= 1e-12 * np.abs(v).sum() + 1e-300
+            assert abs(m[col, 2].item() - (v * v).sum()) <= 1e-12 * (v * v).sum() + 1e-300
+    topo.close()
