@@ -142,6 +142,10 @@ SP_HD double bdouble(uint64_t b) {
 #endif
 }
 
+// -x as a sign-bit flip on the integer pipe (the IEEE negation, NaN included)
+SP_HD double dneg(double x) { return bdouble(dbits(x) ^ (1ULL << 63)); }
+SP_HD double dneg_if(bool c, double x) { return bdouble(dbits(x) ^ ((uint64_t)c << 63)); }
+
 // (a * b) >> F for unsigned fixed-point a, b (F in 65..127); the 256-bit
 // product is formed exactly and truncated, so the error is below one unit.
 template <int F>
@@ -223,7 +227,7 @@ SP_HD double ln_near1(uint64_t xb, unsigned* hard) {
     const u128 p0 = (u128)Dn * lo64(g), p1 = (u128)Dn * hi64(g);
     const u128 v = (p1 << 16) + (p0 >> 48);
     const double r = round_fixed(v, e + z + 72, 80, hard);
-    return below ? -r : r;
+    return dneg_if(below, r);
 }
 
 // IEEE-exact (round to nearest even) multiply, divide and square root of
@@ -429,7 +433,7 @@ SP_HD bool ln_fast(int e, uint64_t frac, double* out) {
     const uint64_t err = (1ULL << 44) + 8 + ae;
     unsigned undecided = 0;
     const double r = e >= 0 ? round_fixed(eln2 + lnm, 120, err, &undecided)
-                            : -round_fixed(eln2 - lnm, 120, err, &undecided);
+                            : dneg(round_fixed(eln2 - lnm, 120, err, &undecided));
     *out = r;
     return undecided == 0;
 }
@@ -470,7 +474,7 @@ SP_HD bool cos_fast(u128 a, int k, bool neg, double* out) {
     unsigned undecided = 0;
     const double r = round_fixed(v, 125, 1ULL << 47, &undecided);
     const bool negative = (q == 2) || (q == 1 && !neg) || (q == 3 && neg);
-    *out = negative ? -r : r;
+    *out = dneg_if(negative, r);
     return undecided == 0;
 }
 
@@ -511,7 +515,7 @@ SP_HD double cr_log_impl(double x, unsigned* hard, bool fast) {
     const u128 eln2 = mk(ln2w) * ae;
     const uint64_t err = 8 + ((ae + 1) >> 1);
     if (e >= 0) return round_fixed(eln2 + lnm, 120, err, hard);
-    return -round_fixed(eln2 - lnm, 120, err, hard);
+    return dneg(round_fixed(eln2 - lnm, 120, err, hard));
 }
 
 SP_HD double cr_log(double x, unsigned* hard) { return cr_log_impl(x, hard, true); }
@@ -617,7 +621,7 @@ SP_HD double cr_cos_impl(double t, unsigned* hard, bool fast) {
     // cos t = cos a, -sign(z) sin a, -cos a, sign(z) sin a for q = 0..3
     const bool negative = (q == 2) || (q == 1 && !neg) || (q == 3 && neg);
     const double r = round_fixed(v, 125, err, hard);
-    return negative ? -r : r;
+    return dneg_if(negative, r);
 }
 
 SP_HD double cr_cos(double t, unsigned* hard) { return cr_cos_impl(t, hard, true); }
