@@ -680,11 +680,12 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     if (any_fallback) {
         // one-warp blocks (a few KB of shared memory each) fit beside the
         // primary kernel's blocks, so under programmatic dependent launch they
-        // are resident while it drains and an empty miss list costs almost
-        // nothing; four per SM keep as many threads on a long miss list as
-        // one 128-thread block per SM did
+        // are resident while it drains; two per SM: the chained op-amp step
+        // measured 94.4 us with two, 95.7 with one, ~98-100 with four and
+        // 93.9 with no fallback launch at all (an empty miss list is the
+        // common case; a long list gets 64 threads per SM)
         const int fblock = 32;
-        const int fgrid = std::max(1, std::min(ctx->num_sms * 4, (int)((count + fblock - 1) / fblock)));
+        const int fgrid = std::max(1, std::min(ctx->num_sms * 2, (int)((count + fblock - 1) / fblock)));
         const size_t fsmem = per * fblock;
         ProfScope prof(ctx, fname[prec], st);
         e = prec == SP_PREC_FP64_EXACT ? launch_newton_exact(L, true, fgrid, fblock, fsmem, st)
