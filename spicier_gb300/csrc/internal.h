@@ -71,6 +71,14 @@ cudaError_t launch_rng_fill(int kind, uint64_t seed, uint64_t first, uint32_t pa
 cudaError_t launch_lu_batch_exact(const double* mats, const double* rhs, int n, uint64_t batch,
                                   double* sol, uint8_t* sing, cudaStream_t st);
 cudaError_t prepare_exact_kernels(int max_smem);
+// Opt kernel f in to the device's whole shared memory per block less its own
+// static shared memory (cudaFuncSetAttribute rejects a larger dynamic size).
+inline cudaError_t allow_dynamic_smem(const void* f, int max_smem) {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, f);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - (int)a.sharedSizeBytes);
+}
 struct AcLaunch;
 cudaError_t launch_ac(const AcLaunch& L, int grid, int block, size_t smem, cudaStream_t st);
 cudaError_t launch_ac_mixed(const AcLaunch& L, int grid, int block, size_t smem, cudaStream_t st);

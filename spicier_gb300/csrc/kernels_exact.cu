@@ -368,24 +368,16 @@ cudaError_t launch_transient_exact(const TransientLaunch& L, int block, size_t s
 }
 
 cudaError_t prepare_exact_kernels(int max_smem) {
-    cudaError_t e;
-    e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(SP_KERNEL_NS::transient_fixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(ac_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(lu_batch_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - 1024);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(lu_batch_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                max_smem);
+    const void* fns[] = {(const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>,
+                         (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
+                         (const void*)SP_KERNEL_NS::transient_fixed_kernel,
+                         (const void*)SP_KERNEL_NS::ladder_kernel<SP_PREC_FP64_EXACT>, (const void*)ac_kernel,
+                         (const void*)lu_batch_fp64_kernel, (const void*)lu_batch_cta_kernel};
+    for (const void* f : fns) {
+        cudaError_t e = allow_dynamic_smem(f, max_smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace sp

@@ -579,7 +579,7 @@ cudaError_t prepare_fast_kernels(int max_smem) {
         (const void*)SP_KERNEL_NS::newton_primary_kernel<SP_PREC_FP64>, (const void*)SP_KERNEL_NS::newton_fallback_kernel<SP_PREC_FP64>,
         (const void*)lu_batch_mixed_kernel, (const void*)lu_batch_escalate_kernel};
     for (const void* f : fns) {
-        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+        cudaError_t e = allow_dynamic_smem(f, max_smem);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

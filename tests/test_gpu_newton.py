@@ -244,17 +244,19 @@ def test_moments_with_fallback_samples(ctx):
     """Moments of a sweep whose warm starts miss (the specialised kernel lists
     them, the fallback kernel solves them): the per-block partials are
     replaced by moments over every converged row; they equal numpy's over the
-    final solutions, as do those of a sweep without misses (block partials)."""
+    final solutions, as do those of a sweep without misses (block partials)
+    and of a sweep with the fallback chain switched off (no fallback launch)."""
     import torch
     circ = configs.miller_opamp()
     topo = ctx.topology(circ)
     N, n = 6000, circ.n
     dev = torch.device("cuda")
-    for bad in (False, True):
+    for bad, fb in ((False, True), (True, True), (False, False)):
         x = torch.empty((N, n), dtype=torch.float64, device=dev)
         st = torch.empty(N, dtype=torch.uint8, device=dev)
-        mom = torch.empty((n, 5), dtype=torch.float64, device=dev)
-        cfg = abi.newton_config(precision=MIXED, warm_max_iterations=2)
+        mom = torch.full((n, 5), float("nan"), dtype=torch.float64, device=dev)
+        cfg = abi.newton_config(precision=MIXED, warm_max_iterations=2,
+                                fallback=abi.SP_FALLBACK_GMIN | abi.SP_FALLBACK_SOURCE if fb else 0)
         x0 = torch.full((N, n), 50.0 if bad else 0.0, dtype=torch.float64, device=dev) if bad else None
         ctx.newton_dc_device(topo, cfg, 3, N, x, x0=x0, status=st, moments=mom)
         torch.cuda.synchronize()
