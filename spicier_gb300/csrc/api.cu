@@ -628,6 +628,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     L.fail_list = s.fail_list;
     L.fail_count = s.counters;
     L.work_next = reinterpret_cast<unsigned long long*>(s.counters + 2);
+    L.cold_max_iterations = cfg->max_iterations;
     if (linear_warm && use_spec) {
         L.lin_params = s.params;
         L.lin_pstride = count;

@@ -197,6 +197,25 @@ SP_HD double round_fixed(u128 v, int F, uint64_t err, unsigned* hard) {
     return bdouble(((uint64_t)(ex + 1023) << 52) + (m - (1ULL << 52)) + up);  // a carry may give +Inf
 }
 
+// round_fixed for the 64-bit fast paths, whose v has at least 54 significant
+// bits and whose result is a normal double: v normalised by one shift (its
+// leading bit at 127), so that the 53 kept bits, the midpoint and the rest
+// sit at fixed positions, and err scaled by the same shift.  The same result
+// and the same count in *undecided as round_fixed, with one variable-width
+// shift of v where round_fixed needs three.
+SP_HD double round_fixed_fast(u128 v, int F, uint64_t err, unsigned* undecided) {
+    const uint64_t h0 = hi64(v);
+    const int lz = h0 ? clz64(h0) : 64 + clz64(lo64(v));
+    const u128 u = v << lz;                      // leading bit at 127
+    const uint64_t m = hi64(u) >> 11;            // the 53 kept bits
+    const u128 rem = u & (((u128)1 << 75) - 1);  // the rest; the midpoint is 2^74
+    const u128 half = (u128)1 << 74;
+    const u128 dist = rem >= half ? rem - half : half - rem;
+    if (dist <= ((u128)err << lz)) ++*undecided;
+    const uint64_t up = (rem > half || (rem == half && (m & 1))) ? 1 : 0;
+    return bdouble(((uint64_t)(127 - lz - F + 1023) << 52) + (m - (1ULL << 52)) + up);  // a carry may raise the exponent
+}
+
 // ln x for x within 2^-16 of 1, relative to d = |x - 1| = D 2^-e exactly
 // (e = 53 below 1, 52 above): ln(1 +- d) = +-d B with B = 1 -+ d/2 + d^2/3
 // -+ ... (8 terms), so the result keeps about 2^-118 relative accuracy however
@@ -432,8 +451,8 @@ SP_HD bool ln_fast(int e, uint64_t frac, double* out) {
     const u128 eln2 = mk(ln2w) * ae;
     const uint64_t err = (1ULL << 44) + 8 + ae;
     unsigned undecided = 0;
-    const double r = e >= 0 ? round_fixed(eln2 + lnm, 120, err, &undecided)
-                            : dneg(round_fixed(eln2 - lnm, 120, err, &undecided));
+    const double r = e >= 0 ? round_fixed_fast(eln2 + lnm, 120, err, &undecided)
+                            : dneg(round_fixed_fast(eln2 - lnm, 120, err, &undecided));
     *out = r;
     return undecided == 0;
 }
@@ -472,7 +491,7 @@ SP_HD bool cos_fast(u128 a, int k, bool neg, double* out) {
     const u128 ysdc = (u128)mulhi64(Y63, SDC) << 35;  // y d w Ps
     const u128 v = odd ? (X + yd) - (xcm + ysdc) : (X + ysdc) - (xcm + yd);
     unsigned undecided = 0;
-    const double r = round_fixed(v, 125, 1ULL << 47, &undecided);
+    const double r = round_fixed_fast(v, 125, 1ULL << 47, &undecided);
     const bool negative = (q == 2) || (q == 1 && !neg) || (q == 3 && neg);
     *out = dneg_if(negative, r);
     return undecided == 0;

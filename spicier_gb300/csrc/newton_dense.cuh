@@ -300,6 +300,9 @@ struct NewtonLaunch {
     double* derived_out = nullptr;
     // per-block moments of the specialised kernel (one sample per thread), [n][grid]
     sp_moments* moments_partial = nullptr;
+    // iteration limit of the specialised kernel's cold restart of a sample
+    // whose warm start missed (the full limit; cfg may hold the warm cap)
+    int cold_max_iterations = 0;
 };
 
 __device__ inline void load_start(const NewtonLaunch& L, size_t s, Work& w, bool warm) {
@@ -451,7 +454,11 @@ __global__ void newton_fallback_kernel(NewtonLaunch L) {
             return true;
         };
         int code = NR_MAXITER;
-        if (warm) {
+        // the specialised kernel has already restarted this sample cold (status
+        // flag), so the chain continues with gmin stepping
+        const bool cold_done = warm && L.status && (L.status[s] & SP_ST_FLAG_COLD);
+        if (cold_done) flags |= SP_ST_FLAG_COLD;
+        if (warm && !cold_done) {
             flags |= SP_ST_FLAG_COLD;
             load_start(L, s, w, false);
             int it = 0;

@@ -190,6 +190,7 @@ struct SpecArgs {
     const double* lp; u64 lpstride; const float* lw; const float* lio; const int* lslots; int lnin;
     double* dvo;
     spx_mom* mom;
+    int cold_max_it;
 };
 __device__ __forceinline__ bool spx_fin(double v) {  // not Inf / NaN, on the integer pipe
     return ((unsigned int)(__double_as_longlong(v) >> 32) & 0x7ff00000u) != 0x7ff00000u;
@@ -722,7 +723,9 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     if (fp32_jac && !dfm) o << "  float xf[" << n << "];\n";
     if (fp32_jac)
         o << "  const float reltolf = spx_f(a.reltol), vabstolf = spx_f(a.vabstol), iabstolf = spx_f(a.iabstol);\n";
-    o << "  int it, code;\n";
+    // it: iterations of the current attempt; spx_itlim its limit; spx_it0 the
+    // iterations of a missed warm attempt; spx_cold: the attempt is the cold restart
+    o << "  int it, code, spx_itlim, spx_it0;\n  bool spx_cold;\n";
     // per-sample set-up: constants, linear Jacobian, start point
     std::ostringstream ld;
     const ParamExpr pe{t};
@@ -791,7 +794,7 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
            << "; ++i) x[i] = a.nodeset[i];\n"
            << "  } else {\n    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) x[i] = 0.0;\n  }\n";
     if (fp32_jac && !dfm) ld << "  #pragma unroll\n  for (int i = 0; i < " << n << "; ++i) xf[i] = spx_f(x[i]);\n";
-    ld << "  it = 0; code = 1;\n  }\n";
+    ld << "  it = 0; code = 1; spx_itlim = a.max_it; spx_it0 = 0; spx_cold = false;\n  }\n";
     o << ld.str();
     o << "  while (true) {\n    ++it;\n";
     if (dfm)
@@ -852,17 +855,33 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
               << (i < nn ? "a.vabstol" : "a.iabstol") << ");\n      x[" << i << "] = xn; }\n";
     }
     o << "    code = sing ? 2 : (conv ? 0 : 1);\n"
-      << "    if (sing || conv || it >= a.max_it) {\n";
+      << "    if (sing || conv || it >= spx_itlim) {\n";
     // status, outputs, miss list, residual of sample s
     if (dfm)
         o << "    double x[" << n << "];\n    #pragma unroll\n    for (int i = 0; i < " << n
           << "; ++i) x[i] = (double)X[i].h + (double)X[i].l;\n";
     o << "    bool fin = true;\n    #pragma unroll\n    for (int i = 0; i < " << n
       << "; ++i) fin = fin && spx_fin(x[i]);\n"
-      << "    unsigned char st8 = !fin ? 3 : (unsigned char)code;\n"
-      << "    if (warm) st8 |= 0x10;\n"
+      << "    unsigned char st8 = !fin ? 3 : (unsigned char)code;\n";
+    // a warm start that missed restarts here from the nodeset (zero without
+    // one) with the full iteration limit: the fallback chain's first stage
+    // (warm -> cold), in this kernel's precision, without waiting for the
+    // fallback launch, where one sample's serial FP64 Newton would take
+    // longer than this whole kernel; the fallback kernel skips that stage
+    // for samples whose status carries the cold flag
+    o << "    if ((st8 & 15) != 0 && warm && !spx_cold && a.cold_max_it > 0) {\n"
+      << "      spx_cold = true; spx_it0 = it; it = 0; spx_itlim = a.cold_max_it;\n";
+    if (dfm)
+        o << "      #pragma unroll\n      for (int i = 0; i < " << n
+          << "; ++i) X[i] = spx_df{a.nodeset ? __double2float_rn(a.nodeset[i]) : 0.f, 0.f};\n";
+    else {
+        o << "      #pragma unroll\n      for (int i = 0; i < " << n << "; ++i) x[i] = a.nodeset ? a.nodeset[i] : 0.0;\n";
+        if (fp32_jac) o << "      #pragma unroll\n      for (int i = 0; i < " << n << "; ++i) xf[i] = spx_f(x[i]);\n";
+    }
+    o << "      continue;\n    }\n"
+      << "    if (warm) st8 |= spx_cold ? 0x30 : 0x10;\n"
       << "    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) a.x[s * " << n << " + i] = x[i];\n"
-      << "    if (a.iters) a.iters[s] = it;\n"
+      << "    if (a.iters) a.iters[s] = spx_it0 + it;\n"
       << "    const bool spx_miss = (st8 & 15) != 0 && (warm || a.fallback_any);\n";
     if (dfm) {
         // parameters mode: the FP64 constants of a listed sample (for the generic
@@ -966,6 +985,7 @@ struct SpecArgsHost {
     int lnin;
     double* dvo;  // parameters mode: FP64 derived constants of the samples put on the miss list
     sp_moments* mom;  // per-block moments [n][grid] (one sample per thread), or nullptr
+    int cold_max_it;  // iteration limit of the cold restart of a warm-start miss (0: none)
 };
 
 bool spec_params_mode(const sp_topology* t, int prec) { return prec == SP_PREC_MIXED && df_supported(t); }
@@ -1068,6 +1088,8 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     a.vabstol = L.cfg.v_abstol;
     a.iabstol = L.cfg.i_abstol;
     a.max_it = L.cfg.max_iterations;
+    // (the fallback kernel learns of the restart from the status byte)
+    a.cold_max_it = (L.x0 || L.lin) && L.status ? L.cold_max_iterations : 0;
     a.fallback_any = (L.cfg.fallback & (SP_FALLBACK_GMIN | SP_FALLBACK_SOURCE)) ? 1 : 0;
     a.next = L.work_next;
     if (!a.next) return cudaErrorInvalidValue;

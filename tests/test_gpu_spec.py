@@ -66,3 +66,44 @@ def test_specialized_and_generic_agree(ctx):
     b = run_device(ctx, circ, abi.SP_PREC_MIXED, 8, 8192, False)
     assert "newton_primary_mixed" in b[4] and "newton_primary_mixed_spec" not in b[4]
     assert spice_close(a[0], b[0], circ.num_nodes)
+
+
+@pytest.mark.parametrize("prec", [abi.SP_PREC_MIXED, abi.SP_PREC_FP64])
+@pytest.mark.parametrize("make", [configs.miller_opamp, configs.bjt_diode_bias])
+def test_warm_miss_restarts_cold_in_kernel(ctx, prec, make):
+    """A warm start that misses (its capped attempt does not converge) is
+    restarted from the nodeset inside the specialised kernel, the fallback
+    chain's first stage: the solution equals, bit for bit, that of a sweep
+    started cold; the iterations add the capped attempt's; the status carries
+    the warm and cold flags; none needs the fallback kernel's gmin stage."""
+    circ = make()
+    topo = ctx.topology(circ)
+    ctx.specialize(topo, prec, True)
+    N, n = 4096, circ.n
+    dev = torch.device("cuda")
+    outs = []
+    for x0 in (None, torch.full((N, n), 50.0, dtype=torch.float64, device=dev)):
+        x = torch.empty((N, n), dtype=torch.float64, device=dev)
+        it = torch.empty(N, dtype=torch.int32, device=dev)
+        st = torch.empty(N, dtype=torch.uint8, device=dev)
+        cfg = abi.newton_config(precision=prec, warm_max_iterations=2)
+        ctx.profile_enable(True)
+        ctx.profile_read()
+        ctx.newton_dc_device(topo, cfg, 9, N, x, x0=x0, iters=it, status=st)
+        torch.cuda.synchronize()
+        prof = ctx.profile_read()
+        ctx.profile_enable(False)
+        assert any(k.endswith("_spec") for k in prof), prof
+        outs.append((x.cpu().numpy(), it.cpu().numpy(), st.cpu().numpy()))
+    (xc, ic, sc), (xw, iw, sw) = outs
+    assert ((sc & abi.SP_ST_MASK) == 0).all()
+    missed = (sw & abi.SP_ST_FLAG_COLD) != 0
+    assert missed.mean() > 0.9  # 50 V on every unknown: two iterations do not get there
+    assert ((sw & abi.SP_ST_FLAG_GMIN) == 0).all() and ((sw & abi.SP_ST_MASK) == 0).all()
+    assert (sw[missed] == (sc[missed] | abi.SP_ST_FLAG_WARM | abi.SP_ST_FLAG_COLD)).all()
+    assert np.array_equal(xw[missed].view(np.uint64), xc[missed].view(np.uint64))
+    # the capped attempt ran its two iterations, or stopped at the first on a
+    # singular or non-finite iterate
+    d = iw[missed] - ic[missed]
+    assert ((d == 1) | (d == 2)).all() and (d == 2).mean() > 0.5
+    topo.close()
