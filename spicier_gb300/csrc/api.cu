@@ -503,7 +503,8 @@ struct NewtonScratch {
     double* params;
     double* derived;
     uint32_t* fail_list;
-    unsigned int* counters;  // [0] fail count, [1] undecided roundings, [2..3] work counter
+    unsigned int* counters;  // [0] fail count, [1] undecided roundings, [2..3] work counter,
+                             // [4] draw groups, [6..7] draw items
     sp_moments* partial;
     uint32_t moment_blocks;
     double* x0;   // learned warm starts [count][n] (when requested)
@@ -577,7 +578,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     int rc = newton_scratch(ctx, t, count, s, warm != nullptr);
     if (rc) return rc;
     // counters: [0] miss count, [1] undecided roundings, [2..3] work counter (u64),
-    // [4] draw group counter
+    // [4] draw group counter, [6..7] draw item counter (u64)
     SP_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 32, st), "clear counters");
     DrawLaunch D{t->dc, seed, first_index, count, d_table, table_cols, s.params, s.derived, d_params,
                  s.counters + 1, t->d_drawn, t->num_drawn, s.counters + 4};
@@ -604,6 +605,12 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
         D.lin_nout = lin.lin_nout;
         D.x0_out = s.x0;
     }
+    // with nothing reading a sample's parameters together inside the draw
+    // kernel, the draws run as per-warp items; the fixed slots then stay
+    // unwritten, so the warm start's inputs must all be drawn slots
+    if (!D.derive && !D.x0_out && !D.params_out &&
+        (!warm || mlp_inputs_drawn(warm, t->h_params.data(), t->num_params)))
+        D.next_items = reinterpret_cast<unsigned long long*>(s.counters + 6);
     {
         ProfScope prof(ctx, "draw_params", st);
         SP_CUDA(ctx, launch_draw(D, st), "draw launch");

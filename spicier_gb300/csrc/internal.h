@@ -42,6 +42,11 @@ struct DrawLaunch {
     // false: skip the derived constants (the consumer, the double-float
     // specialised kernel, computes its constants from the parameters)
     bool derive = true;
+    // zeroed item counter: with no per-group consumer (derive false, no
+    // x0_out, no params_out) the draws run as (group, drawn slot) items taken
+    // by warps, and the fixed slots are not written to params_soa (every
+    // consumer of that mode reads fixed values from the circuit)
+    unsigned long long* next_items = nullptr;
 };
 
 cudaError_t launch_bsim3_eval(int pmos, const double* card, const double* bias, uint64_t count, double* out,
@@ -117,6 +122,8 @@ int mlp_outputs(const sp_mlp* m);
 // then fills the draw launch's linear-warm-start fields (x0_out left to the caller).
 bool mlp_linear_only(const sp_mlp* m, DrawLaunch* d);
 int mlp_max_slot(const sp_mlp* m);
+// True when every input slot of the warm start is a drawn (not fixed) parameter.
+bool mlp_inputs_drawn(const sp_mlp* m, const sp_param* params, int num_params);
 uint64_t mlp_max_rows();
 bool mlp_io_ready(const sp_mlp* m);
 sp_ctx* mlp_ctx(const sp_mlp* m);

@@ -118,6 +118,37 @@ __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_kernel(Draw
     if (hard && L.hard) atomicAdd(L.hard, hard);
 }
 
+// The draws alone, as work items of one warp each: item i is drawn slot
+// drawn[i % num_drawn] of the 32-sample group i / num_drawn, taken from a
+// device counter by the warp's lane 0.  Used when nothing in this kernel
+// consumes a group's parameters together (no derived constants, no warm
+// start, no row-major copy), so no block barrier is needed and every warp
+// stays busy to the end: with groups per block, 17 slots over 8 warps leave
+// one warp three draws while the others have two.  Fixed slots are not
+// written (their consumers read them from the circuit).
+__global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_items_kernel(DrawLaunch L) {
+    pdl_wait();
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const DevCircuit& c = L.c;
+    const uint64_t groups = (L.count + kDrawSamples - 1) / kDrawSamples;
+    const uint64_t items = groups * (uint64_t)L.num_drawn;
+    unsigned hard = 0;
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(L.next_items, 1ULL);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= items) break;
+        const uint64_t g = item / (uint64_t)L.num_drawn;
+        const int k = L.drawn[(int)(item - g * (uint64_t)L.num_drawn)];
+        const uint64_t s = g * kDrawSamples + (uint64_t)lane;
+        if (s >= L.count) continue;
+        const double* row = L.table ? L.table + s * L.table_cols : nullptr;
+        L.params_soa[(size_t)k * L.count + s] = draw_one(c.par[k], L.seed, (uint32_t)(L.first_index + s), row, &hard);
+    }
+    if (hard && L.hard) atomicAdd(L.hard, hard);
+}
+
 cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st) {
     if (L.count == 0) return cudaSuccess;
     int dev = 0, sms = 0;
@@ -125,6 +156,12 @@ cudaError_t launch_draw(const DrawLaunch& L, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     const uint64_t groups = (L.count + kDrawSamples - 1) / kDrawSamples;
+    if (L.next_items && !L.derive && !L.x0_out && !L.params_out) {
+        if (L.num_drawn == 0) return cudaSuccess;
+        const uint64_t warps = groups * (uint64_t)L.num_drawn;
+        const uint64_t grid = std::min<uint64_t>((warps + kDrawLanes - 1) / kDrawLanes, (uint64_t)sms * 4);
+        return launch_chained(draw_items_kernel, dim3((unsigned)grid), dim3(kDrawSamples * kDrawLanes), 0, st, L);
+    }
     // resident blocks (four per SM at 64 registers); without a counter one block per group
     const uint64_t grid = L.next ? std::min<uint64_t>(groups, (uint64_t)sms * 4) : groups;
     const size_t smem = L.x0_out ? sizeof(float) * ((size_t)L.lin_nout * L.lin_nin + L.lin_nin + L.lin_nout +

@@ -527,6 +527,7 @@ struct sp_mlp {
     int* step = nullptr;
     // I/O of the warm-start path
     int* io_slots = nullptr;  // [n_in]
+    std::vector<int> h_slots; // the same on the host
     int max_slot = -1;        // largest input slot (checked against the circuit)
     double* lin = nullptr;    // linear term [n_out][n_in] of the warm start (as given)
     float* lin_f32 = nullptr; // the same in FP32 for the fused kernel
@@ -911,6 +912,7 @@ int sp_mlp_set_io(sp_mlp* m, const int32_t* in_slots, const float* in_mean, cons
         if (in_slots[j] < 0) return mlp_fail(m->ctx, SP_ERR_INVALID_ARGUMENT, "negative input slot");
         m->max_slot = std::max(m->max_slot, (int)in_slots[j]);
     }
+    m->h_slots.assign(in_slots, in_slots + m->d.n_in);
     if (cudaMemcpy(m->io, io.data(), 4 * io.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(m->io_slots, in_slots, 4 * m->d.n_in, cudaMemcpyHostToDevice) != cudaSuccess)
         return SP_ERR_TRANSFER;
@@ -1193,6 +1195,11 @@ bool mlp_linear_only(const sp_mlp* m, DrawLaunch* d) {
     return true;
 }
 int mlp_max_slot(const sp_mlp* m) { return m->max_slot; }
+bool mlp_inputs_drawn(const sp_mlp* m, const sp_param* params, int num_params) {
+    for (int k : m->h_slots)
+        if (k >= num_params || params[k].kind == SP_DRAW_FIXED) return false;
+    return true;
+}
 uint64_t mlp_max_rows() { return kMaxRows; }
 bool mlp_io_ready(const sp_mlp* m) { return m->io_set; }
 sp_ctx* mlp_ctx(const sp_mlp* m) { return m->ctx; }

@@ -107,3 +107,32 @@ def test_warm_miss_restarts_cold_in_kernel(ctx, prec, make):
     d = iw[missed] - ic[missed]
     assert ((d == 1) | (d == 2)).all() and (d == 2).mean() > 0.5
     topo.close()
+
+
+def test_item_draws_match_group_draws(ctx):
+    """The double-float kernel's sweeps draw their parameters as per-warp
+    (group, slot) items when nothing else reads them in the draw kernel; a
+    sweep that also returns the parameters draws them per 32-sample group.
+    Both give the same solutions, iterations and status bit for bit, and the
+    returned parameters are the oracle's draws (ragged last group)."""
+    circ = configs.miller_opamp()
+    topo = ctx.topology(circ)
+    ctx.specialize(topo, abi.SP_PREC_MIXED, True)
+    N, n = 5000, circ.n
+    dev = torch.device("cuda")
+    cfg = abi.newton_config(precision=abi.SP_PREC_MIXED)
+    outs = []
+    for with_params in (False, True):
+        x = torch.empty((N, n), dtype=torch.float64, device=dev)
+        it = torch.empty(N, dtype=torch.int32, device=dev)
+        st = torch.empty(N, dtype=torch.uint8, device=dev)
+        prm = torch.empty((N, len(circ.params)), dtype=torch.float64, device=dev) if with_params else None
+        ctx.newton_dc_device(topo, cfg, 21, N, x, first=77, iters=it, status=st, params=prm)
+        torch.cuda.synchronize()
+        outs.append((x.cpu().numpy(), it.cpu().numpy(), st.cpu().numpy(), prm))
+    assert np.array_equal(outs[0][0].view(np.uint64), outs[1][0].view(np.uint64))
+    assert np.array_equal(outs[0][1], outs[1][1]) and np.array_equal(outs[0][2], outs[1][2])
+    with oracle.math_mode("cr"):
+        ref = np.asarray(oracle.draw_params(circ, 21, N, first=77)).reshape(N, -1)
+    assert np.array_equal(outs[1][3].cpu().numpy().view(np.uint64), ref.view(np.uint64))
+    topo.close()
