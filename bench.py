@@ -662,9 +662,10 @@ def main():
                                        "flops_per_launch": fl, "peak_source": f"bf16_tflops of {peak_src}"}
     if "draw_params" in kavg:
         ms = kavg["draw_params"]
-        # the headline's draw kernel writes the parameters only (the double-float
-        # Newton kernel derives its own constants)
-        by = 8 * len(circ.params) * N
+        # the headline's draw kernel writes the drawn parameters only (the
+        # double-float Newton kernel derives its own constants and compiles the
+        # fixed ones in)
+        by = 8 * sum(1 for row in circ.params if row[0] != abi.SP_DRAW_FIXED) * N
         inst = read_profile_number("draw_params_opamp.md", "alu_warp_instructions_per_sample")
         entry = {"avg_launch_ms": ms, "bytes_per_launch": by,
                  "hbm_frac": by / (ms * 1e-3) / 1e9 / hbm_peak,
