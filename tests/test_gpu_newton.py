@@ -241,30 +241,32 @@ def test_host_entry_mapped_output(ctx, prec):
 
 
 def test_moments_with_fallback_samples(ctx):
-    """Moments of a sweep whose warm starts miss (the specialised kernel lists
-    them, the fallback kernel solves them): the per-block partials are
-    replaced by moments over every converged row; they equal numpy's over the
-    final solutions, as do those of a sweep without misses (block partials)
-    and of a sweep with the fallback chain switched off (no fallback launch)."""
+    """Moments of the specialised kernel's sweeps (one sample per thread): the
+    block partials merged when nothing misses, with or without a fallback
+    launch; every converged row when the fallback changed samples (warm starts
+    that miss, restarted cold from zero in the kernel, miss again and go to
+    gmin / source stepping, which solve some of them).  Each equals numpy's
+    moments over the final converged solutions."""
     import torch
-    circ = configs.miller_opamp()
-    topo = ctx.topology(circ)
-    N, n = 6000, circ.n
+    N = 6000
     dev = torch.device("cuda")
     for bad, fb in ((False, True), (True, True), (False, False)):
+        circ = zero_start_opamp() if bad else configs.miller_opamp()
+        n = circ.n
+        topo = ctx.topology(circ)
         x = torch.empty((N, n), dtype=torch.float64, device=dev)
         st = torch.empty(N, dtype=torch.uint8, device=dev)
         mom = torch.full((n, 5), float("nan"), dtype=torch.float64, device=dev)
         cfg = abi.newton_config(precision=MIXED, warm_max_iterations=2,
                                 fallback=abi.SP_FALLBACK_GMIN | abi.SP_FALLBACK_SOURCE if fb else 0)
-        x0 = torch.full((N, n), 50.0 if bad else 0.0, dtype=torch.float64, device=dev) if bad else None
+        x0 = torch.full((N, n), 50.0, dtype=torch.float64, device=dev) if bad else None
         ctx.newton_dc_device(topo, cfg, 3, N, x, x0=x0, status=st, moments=mom)
         torch.cuda.synchronize()
         xs, ss, m = x.cpu().numpy(), st.cpu().numpy(), mom.cpu()
         ok = (ss & abi.SP_ST_MASK) == 0
-        assert ok.mean() > 0.99
-        if bad:
-            assert (ss & abi.SP_ST_FLAG_COLD).any()  # the fallback ran
+        assert ok.mean() > (0.1 if bad else 0.99)
+        if bad:  # the fallback kernel changed samples
+            assert ((ss & (abi.SP_ST_FLAG_GMIN | abi.SP_ST_FLAG_SOURCE)) != 0).any()
         counts = m.view(torch.int64)[:, 0].numpy()
         for col in range(n):
             v = xs[ok, col]
@@ -272,4 +274,4 @@ def test_moments_with_fallback_samples(ctx):
             assert m[col, 3].item() == v.min() and m[col, 4].item() == v.max()
             assert abs(m[col, 1].item() - v.sum()) <= 1e-12 * np.abs(v).sum() + 1e-300
             assert abs(m[col, 2].item() - (v * v).sum()) <= 1e-12 * (v * v).sum() + 1e-300
-    topo.close()
+        topo.close()
