@@ -637,6 +637,7 @@ static int newton_dc_locked(sp_ctx* ctx, const sp_topology* t, const sp_newton_c
     L.work_next = reinterpret_cast<unsigned long long*>(s.counters + 2);
     L.cold_max_iterations = cfg->max_iterations;
     if (linear_warm && use_spec) {
+        mlp_linear_host(warm, &L.lin_host, &L.lin_io_host, &L.lin_slots_host);
         L.lin_params = s.params;
         L.lin_pstride = count;
         L.lin = lin.lin;

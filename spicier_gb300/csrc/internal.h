@@ -122,6 +122,9 @@ int mlp_outputs(const sp_mlp* m);
 // then fills the draw launch's linear-warm-start fields (x0_out left to the caller).
 bool mlp_linear_only(const sp_mlp* m, DrawLaunch* d);
 int mlp_max_slot(const sp_mlp* m);
+// Host copies of the linear term [n_out][n_in] (FP32), io and the input slots;
+// false when they are not all set.
+bool mlp_linear_host(const sp_mlp* m, const float** lin, const float** io, const int** slots);
 // True when every input slot of the warm start is a drawn (not fixed) parameter.
 bool mlp_inputs_drawn(const sp_mlp* m, const sp_param* params, int num_params);
 uint64_t mlp_max_rows();

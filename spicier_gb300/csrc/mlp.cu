@@ -528,6 +528,8 @@ struct sp_mlp {
     // I/O of the warm-start path
     int* io_slots = nullptr;  // [n_in]
     std::vector<int> h_slots; // the same on the host
+    std::vector<float> h_io;  // io on the host
+    std::vector<float> h_lin; // lin_f32 on the host
     int max_slot = -1;        // largest input slot (checked against the circuit)
     double* lin = nullptr;    // linear term [n_out][n_in] of the warm start (as given)
     float* lin_f32 = nullptr; // the same in FP32 for the fused kernel
@@ -913,6 +915,7 @@ int sp_mlp_set_io(sp_mlp* m, const int32_t* in_slots, const float* in_mean, cons
         m->max_slot = std::max(m->max_slot, (int)in_slots[j]);
     }
     m->h_slots.assign(in_slots, in_slots + m->d.n_in);
+    m->h_io = io;
     if (cudaMemcpy(m->io, io.data(), 4 * io.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(m->io_slots, in_slots, 4 * m->d.n_in, cudaMemcpyHostToDevice) != cudaSuccess)
         return SP_ERR_TRANSFER;
@@ -1018,6 +1021,7 @@ extern "C" int sp_mlp_set_linear(sp_mlp* m, const double* lin) {
         cudaMemcpy(m->lin_f32, f.data(), sizeof(float) * cnt, cudaMemcpyHostToDevice) != cudaSuccess)
         return SP_ERR_TRANSFER;
     m->has_lin = true;
+    m->h_lin = f;
     return SP_OK;
 }
 
@@ -1195,6 +1199,15 @@ bool mlp_linear_only(const sp_mlp* m, DrawLaunch* d) {
     return true;
 }
 int mlp_max_slot(const sp_mlp* m) { return m->max_slot; }
+bool mlp_linear_host(const sp_mlp* m, const float** lin, const float** io, const int** slots) {
+    if (!m->has_lin || (int)m->h_lin.size() != m->d.n_out * m->d.n_in || (int)m->h_slots.size() != m->d.n_in ||
+        (int)m->h_io.size() < 2 * m->d.n_in + m->d.n_out)
+        return false;
+    *lin = m->h_lin.data();
+    *io = m->h_io.data();
+    *slots = m->h_slots.data();
+    return true;
+}
 bool mlp_inputs_drawn(const sp_mlp* m, const sp_param* params, int num_params) {
     for (int k : m->h_slots)
         if (k >= num_params || params[k].kind == SP_DRAW_FIXED) return false;

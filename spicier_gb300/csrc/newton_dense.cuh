@@ -292,6 +292,11 @@ struct NewtonLaunch {
     const float* lin_io = nullptr;
     const int* lin_slots = nullptr;
     int lin_nin = 0;
+    // host copies of lin, lin_io and lin_slots (the specialised kernel takes the
+    // linear term as a launch parameter when its inputs allow)
+    const float* lin_host = nullptr;
+    const float* lin_io_host = nullptr;
+    const int* lin_slots_host = nullptr;
     // per-sample parameters [slot][params_stride] for the specialised kernel's
     // parameters mode, which writes the FP64 derived constants of the samples it
     // lists for the fallback into derived_out (same layout as dv)

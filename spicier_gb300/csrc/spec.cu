@@ -621,7 +621,7 @@ struct ParamExpr {
     }
     std::string f(int slot) const {  // FP32 value
         const sp_param& p = t->h_params[slot];
-        return p.kind == SP_DRAW_FIXED ? lit32(p.a) : "__double2float_rn(pd" + std::to_string(slot) + ")";
+        return p.kind == SP_DRAW_FIXED ? lit32(p.a) : "pf" + std::to_string(slot);
     }
 };
 
@@ -641,6 +641,30 @@ std::vector<int> drawn_slots_used(const sp_topology* t) {
             use(el.field[0]);
     }
     return out;
+}
+
+// The linear warm start as a launch parameter of the double-float kernel
+// (SpecLin): for each drawn slot the elements read, in ascending slot order,
+// its weights for the n unknowns, then the slots' input means, then the n
+// output means; mask bit k set where the k-th slot is an input.  The kernel
+// evaluates out + sum_k w_k (p_k - m_k) over the set bits in slot order with
+// the weights as constant-bank operands, which is the standalone evaluation's
+// order when the inputs are ascending slots.
+struct LinLayout {
+    std::vector<int> slots;  // ascending
+    int nw = 1;              // floats of SpecLin::w
+    bool usable = false;     // the kernel carries the parameter-order path
+};
+LinLayout lin_layout(const sp_topology* t, bool dfm) {
+    LinLayout l;
+    if (!dfm) return l;
+    l.slots = drawn_slots_used(t);
+    std::sort(l.slots.begin(), l.slots.end());
+    const int ps = (int)l.slots.size();
+    if (ps == 0 || ps > 64 || (size_t)(ps * t->n + ps + t->n) * 4 > 3072) return l;
+    l.nw = ps * t->n + ps + t->n;
+    l.usable = true;
+    return l;
 }
 
 // FP64 derived constants of element e (derive_element's operations in its
@@ -684,7 +708,10 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
         for (int k = 0; k < t->num_derived; ++k) o << "#define c" << k << " (spx_cd[" << k << " * 128])\n";
         for (size_t j = 0; j < fcs.size(); ++j) o << "#define cf" << fcs[j] << " (spx_cf[" << j << " * 128])\n";
     }
-    o << "extern \"C\" __global__ void __launch_bounds__(128, " << (sm ? (fp32_jac ? 4 : 2) : 1) << ") spec_newton(SpecArgs a) {\n"
+    const LinLayout ll = lin_layout(t, dfm);
+    o << "struct SpecLin { unsigned long long mask; int on; int pad; float w[" << ll.nw << "]; };\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(128, " << (sm ? (fp32_jac ? 4 : 2) : 1)
+      << ") spec_newton(SpecArgs a, SpecLin lk) {\n"
       << "  asm volatile(\"griddepcontrol.wait;\" ::: \"memory\");  // chained launch: predecessor complete\n"
       << "  asm volatile(\"griddepcontrol.launch_dependents;\" ::: \"memory\");\n"
       << "  const u64 nthreads = (u64)gridDim.x * blockDim.x;\n"
@@ -696,7 +723,7 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
       << "  float* const spx_linm = spx_lw + " << n << " * a.lnin;\n"
       << "  float* const spx_lout = spx_linm + a.lnin;\n"
       << "  int* const spx_lslot = reinterpret_cast<int*>(spx_lout + " << n << ");\n"
-      << "  if (a.lw) {\n"
+      << "  if (a.lw && !lk.on) {\n"
       << "    for (int i = threadIdx.x; i < " << n << " * a.lnin; i += blockDim.x) spx_lw[i] = a.lw[i];\n"
       << "    for (int i = threadIdx.x; i < a.lnin; i += blockDim.x) { spx_linm[i] = a.lio[i]; spx_lslot[i] = a.lslots[i]; }\n"
       << "    for (int i = threadIdx.x; i < " << n << "; i += blockDim.x) spx_lout[i] = a.lio[2 * a.lnin + i];\n"
@@ -737,6 +764,7 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
         ld << "  {\n";
         for (int slot : pslots)
             ld << "  const double pd" << slot << " = __ldg(a.lp + (u64)" << slot << " * a.lpstride + s);\n";
+        for (int slot : pslots) ld << "  const float pf" << slot << " = __double2float_rn(pd" << slot << ");\n";
         for (int e = 0; e < t->num_elements; ++e) {
             const sp_element& el = t->h_elements[e];
             const int d0 = doff[e];
@@ -770,8 +798,19 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
     // the learned linear warm start of sample s into xl[] (FP32, inputs eight at a
     // time with their loads in flight together; the same operations in the same
     // order as the draw kernel's evaluation of it)
-    ld << "  float xl[" << n << "];\n"
-       << "  if (a.lw) {\n"
+    ld << "  float xl[" << n << "];\n";
+    if (ll.usable) {
+        const int ps = (int)ll.slots.size();
+        ld << "  if (lk.on) {\n"
+           << "    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) xl[i] = lk.w[" << ps * n + ps << " + i];\n";
+        for (int k = 0; k < ps; ++k)
+            ld << "    if ((lk.mask >> " << k << ") & 1ull) {\n"
+               << "      const float v = pf" << ll.slots[k] << " - lk.w[" << ps * n + k << "];\n"
+               << "      #pragma unroll\n      for (int i = 0; i < " << n << "; ++i) xl[i] = fmaf(lk.w[" << k * n
+               << " + i], v, xl[i]);\n    }\n";
+        ld << "  } else\n";
+    }
+    ld << "  if (a.lw) {\n"
        << "    #pragma unroll\n    for (int i = 0; i < " << n << "; ++i) xl[i] = spx_lout[i];\n"
        << "    for (int j0 = 0; j0 < a.lnin; j0 += 8) {\n"
        << "      float pv[8];\n"
@@ -1102,7 +1141,35 @@ cudaError_t spec_launch(const sp_topology* t, int prec, const NewtonLaunch& L, c
     a.lio = L.lin_io;
     a.lslots = L.lin_slots;
     a.lnin = L.lin_nin;
-    void* args[] = {&a};
+    // SpecLin: the linear term in the kernel's parameter order when its inputs
+    // are ascending slots that the elements read (otherwise on = 0 and the
+    // kernel reads the term from memory)
+    const LinLayout ll = lin_layout(t, prec == SP_PREC_MIXED && df_supported(t));
+    std::vector<unsigned long long> lkbuf((16 + 4 * (size_t)ll.nw + 7) / 8, 0ull);
+    if (ll.usable && L.lin && L.lin_host && L.lin_io_host && L.lin_slots_host) {
+        const int ps = (int)ll.slots.size(), n = t->n, nin = L.lin_nin;
+        std::vector<int> at(nin, -1);
+        bool ok = nin > 0;
+        for (int j = 0; ok && j < nin; ++j) {
+            ok = j == 0 || L.lin_slots_host[j] > L.lin_slots_host[j - 1];
+            for (int k = 0; ok && k < ps; ++k)
+                if (ll.slots[k] == L.lin_slots_host[j]) at[j] = k;
+            ok = ok && at[j] >= 0;
+        }
+        if (ok) {
+            unsigned long long mask = 0;
+            float* w = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(lkbuf.data()) + 16);
+            for (int j = 0; j < nin; ++j) {
+                mask |= 1ull << at[j];
+                for (int i = 0; i < n; ++i) w[at[j] * n + i] = L.lin_host[(size_t)i * nin + j];
+                w[ps * n + at[j]] = L.lin_io_host[j];
+            }
+            for (int i = 0; i < n; ++i) w[ps * n + ps + i] = L.lin_io_host[2 * nin + i];
+            lkbuf[0] = mask;
+            reinterpret_cast<int*>(lkbuf.data())[2] = 1;
+        }
+    }
+    void* args[] = {&a, lkbuf.data()};
     // tuned resident blocks per SM (setting "spec.bpsm.<precision>"), never above the occupancy limit
     int bpsm = t->spec_bpsm[slot];
     const int tb = tune_get(t->ctx, prec == SP_PREC_MIXED ? "spec.bpsm.mixed" : "spec.bpsm.fp64", t->n, 0);

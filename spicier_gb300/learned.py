@@ -123,7 +123,9 @@ class WarmStart:
         if self.n_inputs >= len(cand):
             self.inputs = list(cand)
         else:
-            self.inputs = select_inputs(P[sub].cpu().numpy(), xs, cand, self.n_inputs, tol)
+            # ascending slots: the specialised kernel then takes the linear term
+            # as a launch parameter (the evaluation order is the slots' order)
+            self.inputs = sorted(select_inputs(P[sub].cpu().numpy(), xs, cand, self.n_inputs, tol))
         in_mean = np.array([param_normalization(c, s)[0] for s in self.inputs])
         in_scale = np.array([param_normalization(c, s)[1] for s in self.inputs])
         self.tolerance = tol

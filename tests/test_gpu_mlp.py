@@ -304,5 +304,21 @@ def test_linear_warm_start(ctx):
     torch.cuda.synchronize()
     assert np.array_equal(x2.cpu().numpy().view(np.uint64), xl.view(np.uint64))
     assert np.array_equal(it2.cpu().numpy(), il) and np.array_equal(st2.cpu().numpy(), sl)
+    # the same term with its inputs in descending slot order: the specialised
+    # kernel then reads it from memory (its launch-parameter form needs
+    # ascending slots); again bit for bit a sweep from the standalone warm start
+    assert list(ws.inputs) == sorted(ws.inputs)
+    rev = list(range(len(ws.inputs)))[::-1]
+    out_mean, out_scale = ws._io
+    m.set_io([ws.inputs[j] for j in rev], np.asarray(in_mean)[rev], np.asarray(in_scale)[rev], out_mean, out_scale)
+    m.set_linear(np.asarray(ws._lin)[:, rev])
+    xr, itr, str_ = torch.empty_like(x), torch.empty_like(it), torch.empty_like(st)
+    ws.sweep_device(topo, cfg, 1, N, xr, iters=itr, status=str_)
+    m.warm_start_device(prm.t().contiguous(), N, N, x0)
+    ctx.newton_dc_device(topo, cfg8, 1, N, x2, x0=x0, iters=it2, status=st2)
+    torch.cuda.synchronize()
+    assert np.array_equal(x2.cpu().numpy().view(np.uint64), xr.cpu().numpy().view(np.uint64))
+    assert np.array_equal(it2.cpu().numpy(), itr.cpu().numpy())
+    assert spice_close(xr.cpu().numpy(), xo, circ.num_nodes)
     ws.use_network(True)
     ws.mlp.close()
