@@ -123,9 +123,10 @@ __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_kernel(Draw
 // device counter by the warp's lane 0.  Used when nothing in this kernel
 // consumes a group's parameters together (no derived constants, no warm
 // start, no row-major copy), so no block barrier is needed and every warp
-// stays busy to the end: with groups per block, 17 slots over 8 warps leave
-// one warp three draws while the others have two.  Fixed slots are not
-// written (their consumers read them from the circuit).
+// stays busy to the end, where whole groups per block spread a group's drawn
+// slots unevenly over the 8 warps (17 slots: one warp draws three, the others
+// two, and the block waits for it).  Fixed slots are not written (their
+// consumers read them from the circuit).
 __global__ void __launch_bounds__(kDrawSamples * kDrawLanes, 4) draw_items_kernel(DrawLaunch L) {
     pdl_wait();
     pdl_trigger();

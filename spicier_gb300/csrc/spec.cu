@@ -795,9 +795,11 @@ std::string generate(const sp_topology* t, const Pattern& P, bool fp32_jac) {
             if (t->h_elements[e].kind == SP_EL_R)
                 ld << "  g" << e << " = " << (fp32_jac ? "spx_f(c" : "(JT)(c") << doff[e] << ");\n";
     }
-    // the learned linear warm start of sample s into xl[] (FP32, inputs eight at a
-    // time with their loads in flight together; the same operations in the same
-    // order as the draw kernel's evaluation of it)
+    // the learned linear warm start of sample s into xl[] in FP32, the same
+    // operations in the same order as its standalone evaluation: from the launch
+    // parameter (lk.on: weights as constant-bank operands, inputs the parameters
+    // converted above) or from memory (inputs eight at a time with their loads
+    // in flight together, weights staged in shared memory)
     ld << "  float xl[" << n << "];\n";
     if (ll.usable) {
         const int ps = (int)ll.slots.size();
