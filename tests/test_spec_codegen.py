@@ -42,3 +42,25 @@ def test_double_float_parameters_mode(product_lib):
     assert "spx_df X[" not in src64 and "a.dv + s" in src64
     srcb, _ = specialized_source(configs.bjt_diode_bias(), abi.SP_PREC_MIXED)
     assert "spx_df X[" not in srcb and "a.dv + s" in srcb
+
+
+def test_linear_warm_start_launch_parameter_and_cold_restart(product_lib):
+    """The double-float kernel carries the learned linear term's launch-parameter
+    form (SpecLin: weights for every drawn slot the elements read, in ascending
+    slot order, summed with constant-bank operands) beside the form read from
+    memory; every generated kernel restarts a missed warm start from the nodeset
+    in the same lane, with the full iteration limit."""
+    src, _ = specialized_source(configs.miller_opamp(), abi.SP_PREC_MIXED)
+    assert "struct SpecLin" in src and "spec_newton(SpecArgs a, SpecLin lk)" in src
+    assert "if (lk.on) {" in src and "if (a.lw && !lk.on) {" in src
+    # 17 drawn slots read by the op-amp's elements: 17 x 12 weights, 17 means, 12
+    # outputs; the sample set-up appears twice (first sample, then each next one)
+    assert "float w[233]" in src and src.count("if ((lk.mask >> ") == 2 * 17
+    slots = [int(line.split("pf")[1].split(" ")[0]) for line in src.splitlines()
+             if line.strip().startswith("const float v = pf")]
+    assert slots[:17] == sorted(slots[:17]) and slots[17:] == slots[:17] and len(set(slots)) == 17
+    for make, prec in ((configs.miller_opamp, abi.SP_PREC_FP64), (configs.bjt_diode_bias, abi.SP_PREC_MIXED)):
+        s, _ = specialized_source(make(), prec)
+        assert "if (lk.on) {" not in s  # only the double-float kernel takes the parameter form
+        assert "spx_itlim = a.cold_max_it" in s
+    assert "spx_itlim = a.cold_max_it" in src
